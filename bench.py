@@ -1,0 +1,301 @@
+"""Throughput benchmark of the particle-update path on one GB300.
+
+Workload (the configuration the headline metric is quoted on): the vortex
+system, N = 65,536 particles in a periodic box L = 8, natural frequencies
+omega_i ~ N(0, 0.5^2), alpha = 0, v0 = 0.02, sigma = 2, rho = 0.25,
+D = 0.01, strong-order-1.5 stochastic Runge-Kutta, dt = 0.005, seed 1.
+Synthetic inputs: x, y ~ U[0, L), phi ~ U[-pi, pi) from numpy PCG64(1).
+
+One bench step = 100 simulation steps (one CUDA-graph replay of the fused
+kernels).  L2 is flushed (a 512 MB write) between bench steps, outside the
+timed events.  `value` is the FP32-compensated form's particle-steps/s; the
+plain FP64 form is reported beside it (`fp64`).
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+WORKLOAD = dict(name="vortex_srk_n65536_L8", n=65536, L=8.0, v0=0.02, sigma=2.0, rho=0.25,
+                alpha=0.0, D_phi=0.01, dt=0.005, seed=1, omega_sd=0.5)
+SIM_STEPS_PER_BENCH_STEP = 100
+# Algorithmic (compulsory) HBM bytes per particle for one SRK step, by phase,
+# for state resident in HBM: doubles x, y, phi (24 B), omega (8 B), the cell
+# key and index (4 + 4 B written, read back by the sort), the phase rate (8 B)
+# and n_i (4 B).
+ALG_BYTES = {
+    "stage": 24 + 8,          # read x, y, phi; write key, index
+    "sort": 2 * 2 * 8,        # two 8-bit passes: read + write (key, index)
+    "gather": 8 + 40,         # read (key, index); write cell-order x, y, phi, float x/y offsets
+    "pass1": 32 + 12,         # read cell-order x, y, phi, offsets; write phase rate, n_i
+    "pass2": 32 + 12 + 8 + 24 + 24,  # + own rate/n_i, omega, state in, state out
+}
+ALG_BYTES_STEP = 168 + 8      # survey accounting for the whole SRK step (+ omega)
+
+
+def init_inputs(w, seed_offset=0):
+    rng = np.random.default_rng(w["seed"] + seed_offset)
+    n, L = w["n"], w["L"]
+    st = np.empty(3 * n)
+    st[0::3] = rng.uniform(0.0, L, n)
+    st[1::3] = rng.uniform(0.0, L, n)
+    st[2::3] = rng.uniform(-np.pi, np.pi, n)
+    omega = rng.normal(0.0, w["omega_sd"], n)
+    return st, omega
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    def __init__(self, index=0):
+        self.samples, self.proc, self.index = [], None, index
+
+    def __enter__(self):
+        q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+             "clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={q}",
+                 "--format=csv,noheader,nounits", "-lms", "100"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) >= 7:
+                self.samples.append(parts)
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(s[0]) for s in self.samples if s[0].replace(".", "").isdigit()]
+        mx = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for s in self.samples for k in range(4)
+                          if s[3 + k].lower() == "active"})
+        return {"sm_mhz": float(np.median(sm)) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": reasons,
+                "samples": len(self.samples)}
+
+
+def cpu_baseline(w, nsteps=3):
+    """The oracle port (the reference's arithmetic restated in C, one core),
+    on a bounded sample: the full N for a few SRK steps."""
+    from oracle import pyoracle as po
+    st, omega = init_inputs(w)
+    n = w["n"]
+    o = po.OracleSystem(n, w["L"], w["v0"], w["sigma"], w["rho"], w["alpha"], w["D_phi"])
+    noise = np.random.default_rng(99).standard_normal(2 * n * nsteps)
+    o.run(po.SRK, st, 0.0, w["dt"], 1, noise[:2 * n], omega)  # warm
+    t0 = time.perf_counter()
+    o.run(po.SRK, st, 0.0, w["dt"], nsteps, noise, omega)
+    dt = time.perf_counter() - t0
+    return {"value": n * nsteps / dt, "unit": "particle-steps/s", "cores": 1, "kind": "port",
+            "sample": f"N={n}, {nsteps} SRK steps of the same workload, 1 thread "
+                      f"(the reference's path is single-threaded per system)"}
+
+
+def dist_setup(args):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch.distributed as dist  # noqa: F811
+        import torch
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    return world, rank, local, dist
+
+
+def reduce_max(dist, v):
+    if dist is None:
+        return v
+    import torch
+    t = torch.tensor([v], device="cuda", dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def run_form(abi, torch, w, precision, steps, warmup, rank, dist):
+    n = w["n"]
+    st, omega = init_inputs(w, seed_offset=rank)
+    p = abi.make_params(L=w["L"], v0=w["v0"], sigma=w["sigma"], rho=w["rho"], alpha=w["alpha"],
+                        D_phi=w["D_phi"], model=abi.MODEL_VORTEX, stepper=abi.STEPPER_SRK,
+                        precision=precision, seed=w["seed"], system_id=rank)
+    s = abi.System(n, p)
+    s.upload_state(st)
+    s.upload_omega(omega)
+    stream = torch.cuda.ExternalStream(s.stream)
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    dt = w["dt"]
+    for _ in range(warmup):
+        s.step(dt, SIM_STEPS_PER_BENCH_STEP, graph=True)
+    s.synchronize()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+          for _ in range(steps)]
+    if dist is not None:
+        dist.barrier()
+    torch.cuda.synchronize()
+    for k in range(steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        ev[k][0].record(stream)
+        s.step(dt, SIM_STEPS_PER_BENCH_STEP, graph=True)
+        ev[k][1].record(stream)
+    torch.cuda.synchronize()
+    if dist is not None:
+        dist.barrier()
+    ms = sum(a.elapsed_time(b) for a, b in ev)
+    ms = reduce_max(dist, ms)
+    # e2e through the C-ABI with host buffers: pinned upload, 100 steps, download
+    import ctypes as C
+    L = abi.lib()
+    ptr = C.c_void_p()
+    L.spc_alloc_pinned(3 * n * 8, C.byref(ptr))
+    host = np.ctypeslib.as_array((C.c_double * (3 * n)).from_address(ptr.value))
+    host[:] = s.download_state()
+    e2e_ms = 0.0
+    for k in range(steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        s.upload_state(host)
+        s.step(dt, SIM_STEPS_PER_BENCH_STEP, graph=True)
+        s.download_state(host)
+        e2e_ms += (time.perf_counter() - t0) * 1e3
+    e2e_ms = reduce_max(dist, e2e_ms)
+    prof = s.profile_steps(dt, 20)
+    R = s.order_params()
+    del host
+    L.spc_free_pinned(ptr)
+    s.close()
+    return ms, e2e_ms, prof, R
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    w = WORKLOAD
+    world, rank, local, dist = dist_setup(args)
+    n_total = w["n"] * world
+    config = {"workload": w["name"], "N": w["n"], "L": w["L"], "stepper": "srk",
+              "model": "vortex (alignment + natural frequencies)", "neighbour": "cell",
+              "dt": w["dt"], "sim_steps_per_bench_step": SIM_STEPS_PER_BENCH_STEP,
+              "l2": "flushed between bench steps (512 MB write, outside the timed events)",
+              "parallelism": f"replicas{world}"}
+
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        # the reference's CPU path (restated, bit-identical) on the host cores
+        from oracle import pyoracle as po  # noqa: F401
+        vals = []
+        for _ in range(args.warmup):
+            cpu_baseline(w, nsteps=1)
+        for _ in range(args.steps):
+            vals.append(cpu_baseline(w, nsteps=1)["value"])
+        v = float(np.mean(vals))
+        cb = cpu_baseline(w, nsteps=1)
+        print(json.dumps({
+            "impl": "reference", "metric": "particle-steps/s", "value": v,
+            "unit": "particle-steps/s", "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": config,
+            "cpu_baseline": {"kind": cb["kind"], "cores": 1, "sample": cb["sample"], "value": v},
+            "e2e": {"value": v, "unit": "particle-steps/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}))
+        return
+
+    import torch
+    from spc2_langevin_integration_gb300 import abi
+    torch.cuda.set_device(local)
+    with ClockSampler(local) as clk:
+        ms32, e2e32, prof32, R32 = run_form(abi, torch, w, abi.PRECISION_FP32C, args.steps,
+                                            args.warmup, rank, dist)
+        ms64, e2e64, prof64, R64 = run_form(abi, torch, w, abi.PRECISION_FP64,
+                                            max(2, args.steps // 2), args.warmup, rank, dist)
+    steps64 = max(2, args.steps // 2)
+    psteps = n_total * SIM_STEPS_PER_BENCH_STEP
+    value = psteps * args.steps / (ms32 / 1e3)
+    value64 = psteps * steps64 / (ms64 / 1e3)
+    e2e_value = psteps * args.steps / (e2e32 / 1e3)
+    hbm, peak_kind = peaks()
+    phases = {k: prof32[k] for k in ("stage", "sort", "gather", "pass1", "pass2")}
+    dom = max(phases, key=phases.get)
+    achieved = ALG_BYTES[dom] * w["n"] / (phases[dom] * 1e-3) / 1e9
+    out = {
+        "metric": "particle-steps/s", "value": value, "unit": "particle-steps/s",
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": ms32 / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32c (f32 sums/trig/increments; f64 cutoff, positions, phase)",
+        "data": "synthetic (seeded uniform positions/phases, normal frequencies)",
+        "config": config,
+        "fp64": {"value": value64, "ms_per_step": ms64 / steps64, "profile_ms": prof64,
+                 "order_params": R64},
+        "fp32c_over_fp64": value / value64,
+        "order_params_fp32c": R32,
+        "gpu_launches": None,
+        "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm,
+                     "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / hbm,
+                     "traffic": None, "alg_bytes_per_particle": ALG_BYTES[dom],
+                     "note": "compute-bound path (float prefilter + per-pair trig); HBM fraction "
+                             "is low by construction"},
+        "profile_ms_fp32c": prof32,
+        "e2e": {"value": e2e_value, "unit": "particle-steps/s",
+                "h2d_bytes_per_step": 3 * w["n"] * 8, "d2h_bytes_per_step": 3 * w["n"] * 8},
+        "clocks": clk.summary(),
+    }
+    # launches inside the timed region per bench step (graph of 100 steps)
+    per_step = 1 + 3 * 2 + 1 + 1 + 2  # stage, 2 radix passes x 3, bounds, gather, 2 passes
+    out["gpu_launches"] = per_step * SIM_STEPS_PER_BENCH_STEP * args.steps
+    if rank == 0 and not args.no_cpu_baseline:
+        out["cpu_baseline"] = cpu_baseline(w)
+    if rank == 0:
+        print(json.dumps(out))
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

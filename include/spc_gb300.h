@@ -1,0 +1,190 @@
+/*
+ * spc_gb300.h -- C-ABI of the GB300 (sm_103a) particle-update library.
+ *
+ * The reference (raven91/spc2_langevin_integration) has no FFI: its "plugin"
+ * surface is the C++ stepper/system contract
+ *   Stepper::DoStep(System&, std::vector<Real>& state, Real t, Real dt)
+ *   System::EvaluateRhs(state, k_prev, k_next, k_coef, dt)            (RK form)
+ *   System::EvaluateRhs(state, derivative, additional_derivative, dt)  (SRK form)
+ * plus the engine's PeriodicBoundaryConditions wrap.  This header is the thin,
+ * allocation-owning C layer those classes forward to (the C++ adapters in
+ * spc2_langevin_integration_gb300/host keep the reference class names and
+ * signatures).  Each entry point names the reference interface it replaces.
+ *
+ * Conventions: every function returns 0 (SPC_OK) or a negative spc_status;
+ * spc_last_error() gives a message.  State crosses the boundary in the
+ * reference's array-of-structures layout [x0,y0,phi0,x1,...] (3N doubles);
+ * on the device it is structure-of-arrays.  A handle is used from one host
+ * thread at a time and owns one CUDA stream and all of its device memory.
+ */
+#ifndef SPC_GB300_H
+#define SPC_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SPC_ABI_VERSION 1
+
+typedef enum spc_status {
+  SPC_OK = 0,
+  SPC_ERR_INVALID = -1,   /* bad argument or parameter */
+  SPC_ERR_CUDA = -2,      /* a CUDA call failed (message has the CUDA error) */
+  SPC_ERR_NOMEM = -3,     /* device allocation failed */
+  SPC_ERR_STATE = -4,     /* call out of order (e.g. stepping before upload) */
+  SPC_ERR_NOISE = -5,     /* injected noise stream exhausted */
+  SPC_ERR_DEVICE = -6,    /* a kernel reported an error word (see message) */
+  SPC_ERR_CAPACITY = -7   /* a caller-provided buffer is too small */
+} spc_status;
+
+/* Dynamical system.  CHIMERA: ChimeraSystem (DynamicalSystems/ChimeraSystem.hpp:12-106).
+ * VORTEX: the same alignment right-hand side with per-particle natural
+ * frequencies omega_i added to the phase drift of the stochastic
+ * Runge-Kutta update, as StochasticRungeKuttaStepperPtr does
+ * (Steppers/StochasticRungeKuttaStepperPtr.hpp:27-34, :65). */
+enum { SPC_MODEL_CHIMERA = 0, SPC_MODEL_VORTEX = 1 };
+
+/* Stepper.  EULER: StochasticEulerStepper (Steppers/StochasticEulerStepper.hpp:31-47);
+ * SRK: StochasticRungeKuttaStepper(Ptr) strong order 1.5
+ * (Steppers/StochasticRungeKuttaStepper.hpp:34-61); RK4: RungeKutta4Stepper
+ * (Steppers/RungeKutta4Stepper.cpp:29-57); EULER_PTR: StochasticEulerStepperPtr
+ * (Steppers/StochasticEulerStepperPtr.hpp:32-53). */
+enum { SPC_STEPPER_EULER = 0, SPC_STEPPER_SRK = 1, SPC_STEPPER_RK4 = 2, SPC_STEPPER_EULER_PTR = 3 };
+
+/* Neighbour search.  CELL: the reference's linked-list cells of side
+ * L/int(L/rho) and 3x3 stencil (ChimeraSystem.cpp:258-426).  VERLET: a
+ * skin list (r_max = rho + skin) rebuilt when the largest displacement since
+ * the last build exceeds skin/2; its neighbour sets equal the cell search's.
+ * When rho > L/4 both fall back to all pairs, as EvaluateRhs does
+ * (ChimeraSystem.cpp:90-98). */
+enum { SPC_NEIGHBOUR_CELL = 0, SPC_NEIGHBOUR_VERLET = 1 };
+
+/* Precision.  FP64: every value and operation in double, in the reference's
+ * order.  FP32C: neighbour sums, sin/cos and stage updates in float with
+ * compensated (Kahan) accumulation; the cutoff / minimum-image decision, the
+ * wrapped positions and the accumulated phase stay double. */
+enum { SPC_PRECISION_FP64 = 0, SPC_PRECISION_FP32C = 1 };
+
+/* flags */
+#define SPC_FLAG_EXACT_ALL 0x1u /* decide every candidate pair in FP64 (no float prefilter) */
+
+typedef struct spc_params {
+  int32_t model;      /* SPC_MODEL_* */
+  int32_t stepper;    /* SPC_STEPPER_* */
+  int32_t neighbour;  /* SPC_NEIGHBOUR_* */
+  int32_t precision;  /* SPC_PRECISION_* */
+  double L;           /* periodic box side (kL, Definitions.hpp:22) */
+  double v0, sigma, rho, alpha, D_phi, rho_0; /* ChimeraSystem ctor (ChimeraSystem.hpp:16-23) */
+  double skin;        /* Verlet skin; r_max = rho + skin */
+  uint64_t seed;      /* Philox4x32-10 key */
+  uint32_t system_id; /* Philox counter word: distinguishes systems sharing a seed */
+  uint32_t flags;     /* SPC_FLAG_* */
+} spc_params;
+
+typedef struct spc_handle spc_handle;
+
+/* Library / version. */
+int spc_abi_version(void);
+const char *spc_last_error(const spc_handle *h); /* h may be NULL: last global error */
+
+/* Construct a system of n particles (replaces the ChimeraSystem ctor
+ * ChimeraSystem.cpp:11-59 + the stepper ctors + PeriodicBoundaryConditions
+ * ctor PeriodicBoundaryConditions.cpp:7-17).  Allocates all device memory. */
+int spc_create(const spc_params *p, int32_t n, spc_handle **out);
+int spc_destroy(spc_handle *h);
+int spc_get_params(const spc_handle *h, spc_params *out, int32_t *n);
+
+/* State transfer in the reference's AoS layout (replaces the engine's
+ * system_state_ vector, SimulationEngine.hpp:27, and BroadcastVector). */
+int spc_upload_state(spc_handle *h, const double *aos3n);
+int spc_download_state(spc_handle *h, double *aos3n);
+/* Natural frequencies (VORTEX model), n doubles
+ * (StochasticRungeKuttaStepperPtr.hpp:27-34 frequencies_). */
+int spc_upload_omega(spc_handle *h, const double *omega);
+/* RK4 stage buffers k1..k4 (4 x 3N, AoS each), which persist across steps
+ * (RungeKutta4Stepper.cpp:7-13); for exact resume and tests. */
+int spc_download_rk4_buffers(spc_handle *h, double *out12n);
+int spc_upload_rk4_buffers(spc_handle *h, const double *in12n);
+
+/* Advance nsteps steps: for each, t += dt; Stepper::DoStep; the engine's
+ * periodic wrap (SimulationEngine.cpp:149-155), fused on the device.
+ * Noise comes from Philox4x32-10 (counter = particle, system, step) unless an
+ * injected stream is set.  *t_inout is advanced. */
+int spc_step(spc_handle *h, double *t_inout, double dt, int32_t nsteps);
+/* Same, captured as a CUDA graph of nsteps steps on first use and replayed
+ * (fixed-length step loops; requires Philox noise). */
+int spc_step_graph(spc_handle *h, double *t_inout, double dt, int32_t nsteps);
+
+/* Step counter used as the Philox counter (the number of steps taken). */
+int spc_get_step_counter(const spc_handle *h, uint64_t *out);
+int spc_set_step_counter(spc_handle *h, uint64_t step);
+
+/* Noise-injection hook: the next steps consume these normals instead of
+ * Philox, in the reference's draw order per step (Euler: one per particle,
+ * ChimeraSystem.cpp:924-932; SRK: U1 then U2 per particle,
+ * StochasticRungeKuttaStepper.hpp:44-45).  count must be a multiple of the
+ * per-step count.  Copied to the device; stepping past the end fails with
+ * SPC_ERR_NOISE.  spc_clear_noise returns to Philox. */
+int spc_inject_noise(spc_handle *h, const double *normals, int64_t count);
+int spc_clear_noise(spc_handle *h);
+/* Export the Philox normals that steps [first_step, first_step + nsteps)
+ * use, in the injection layout, so the same increments can be fed to the
+ * reference / oracle. */
+int spc_export_noise(spc_handle *h, uint64_t first_step, int32_t nsteps, double *out);
+/* Normals per particle per step for this stepper (1, 2 or 0). */
+int spc_noise_per_particle(const spc_handle *h);
+
+/* Right-hand sides at the current state, for parity checks.
+ * RK form (ChimeraSystem::EvaluateRhs, ChimeraSystem.cpp:78-100): stage
+ * state + k_coef*dt*k_prev; k_next (3N, AoS) is read and written: its phase
+ * entry is kept where a particle has no neighbour (ChimeraSystem.cpp:421-424). */
+int spc_rhs_rk(spc_handle *h, const double *k_prev, double k_coef, double dt, double *k_next);
+/* SRK form (ChimeraSystem.cpp:102-114): derivative (3N, AoS) and
+ * additional_derivative (2N, [i][0],[i][1]), both zero-started as the
+ * steppers do (StochasticRungeKuttaStepper.hpp:36-39). */
+int spc_rhs_srk(spc_handle *h, double *derivative, double *additional);
+
+/* Neighbour sets at the current state: counts (n ints) and, if idx is not
+ * NULL, the indices of each particle's neighbours concatenated in the
+ * reference's visiting order (offsets from the counts).  *total receives the
+ * number of pairs; SPC_ERR_CAPACITY if cap is smaller. */
+int spc_neighbours(spc_handle *h, int32_t *counts, int32_t *idx, int64_t cap, int64_t *total);
+
+/* Global order parameter R = |<e^{i phi}>| and its argument psi (the
+ * observer's summary, BinaryObserver.cpp:196-210, computed in FP64), and the
+ * local order parameter mean_i |sum_{j in N_i u {i}} e^{i phi_j}| / (n_i + 1). */
+int spc_order_params(spc_handle *h, double *R, double *psi, double *R_local);
+
+/* Diagnostics: clamped cell indices (positions within an ulp of L whose
+ * cell index int(x/L*nc) came out as nc), Verlet rebuilds, device error word. */
+int spc_diagnostics(spc_handle *h, int64_t *clamped_cells, int64_t *verlet_rebuilds,
+                    int64_t *error_word);
+
+/* Per-phase device time of nsteps steps (no graph), measured with CUDA
+ * events on the handle's stream between kernel groups.  out_ms receives
+ * the average milliseconds per step of: [0] stage + cell keys, [1] radix
+ * sort, [2] cell bounds + cell-order gather, [3] first neighbour pass
+ * (with its fused epilogue), [4] second neighbour pass (SRK) or the other
+ * RK4 passes, [5] the whole step.  cap is out_ms's length (>= 6). */
+int spc_profile_steps(spc_handle *h, double dt, int32_t nsteps, double *out_ms, int32_t cap);
+
+/* Synchronise the handle's stream; the stream itself (a cudaStream_t) for
+ * callers that time or order work around the library. */
+int spc_synchronize(spc_handle *h);
+void *spc_stream(spc_handle *h);
+
+/* Philox4x32-10 evaluated on the device (the generator behind every noise
+ * draw), for checking against the published known-answer vectors. */
+int spc_philox4x32_10(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]);
+
+/* Page-locked host buffers for callers that stream state in and out. */
+int spc_alloc_pinned(size_t bytes, void **out);
+int spc_free_pinned(void *p);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

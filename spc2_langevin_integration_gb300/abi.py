@@ -1,0 +1,280 @@
+"""ctypes binding of the C-ABI in include/spc_gb300.h.
+
+This is the reference-facing boundary as a Python caller sees it (the C++
+adapters in ``host/`` are the drop-in for the reference's own C++ callers).
+The library is the in-tree ``_build/libspc_gb300.so``; if it is missing or
+fails to load, :func:`lib` raises - there is no CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import build as _build
+
+MODEL_CHIMERA, MODEL_VORTEX = 0, 1
+STEPPER_EULER, STEPPER_SRK, STEPPER_RK4, STEPPER_EULER_PTR = 0, 1, 2, 3
+NEIGHBOUR_CELL, NEIGHBOUR_VERLET = 0, 1
+PRECISION_FP64, PRECISION_FP32C = 0, 1
+FLAG_EXACT_ALL = 0x1
+
+SPC_OK = 0
+ERRORS = {
+    -1: "SPC_ERR_INVALID", -2: "SPC_ERR_CUDA", -3: "SPC_ERR_NOMEM", -4: "SPC_ERR_STATE",
+    -5: "SPC_ERR_NOISE", -6: "SPC_ERR_DEVICE", -7: "SPC_ERR_CAPACITY",
+}
+
+
+class SpcError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"{ERRORS.get(code, code)}: {msg}")
+        self.code = code
+
+
+class Params(C.Structure):
+    _fields_ = [
+        ("model", C.c_int32), ("stepper", C.c_int32), ("neighbour", C.c_int32),
+        ("precision", C.c_int32), ("L", C.c_double), ("v0", C.c_double),
+        ("sigma", C.c_double), ("rho", C.c_double), ("alpha", C.c_double),
+        ("D_phi", C.c_double), ("rho_0", C.c_double), ("skin", C.c_double),
+        ("seed", C.c_uint64), ("system_id", C.c_uint32), ("flags", C.c_uint32),
+    ]
+
+
+_lib = None
+
+
+def library_path() -> str:
+    return _build.LIB
+
+
+def lib() -> C.CDLL:
+    """Load the CUDA library (building it first when nvcc is available)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = _build.LIB
+    if not _build.up_to_date():
+        try:
+            _build.build_library()
+        except Exception as e:  # no nvcc here: only an existing build can load
+            if not os.path.exists(path):
+                raise RuntimeError(f"CUDA library missing and could not be built: {e}") from e
+    L = C.CDLL(path)
+    H = C.c_void_p
+    dp = C.POINTER(C.c_double)
+    L.spc_abi_version.restype = C.c_int
+    L.spc_last_error.restype = C.c_char_p
+    L.spc_last_error.argtypes = [H]
+    L.spc_create.argtypes = [C.POINTER(Params), C.c_int32, C.POINTER(H)]
+    L.spc_destroy.argtypes = [H]
+    L.spc_get_params.argtypes = [H, C.POINTER(Params), C.POINTER(C.c_int32)]
+    for f in ("spc_upload_state", "spc_download_state", "spc_upload_omega",
+              "spc_download_rk4_buffers", "spc_upload_rk4_buffers"):
+        getattr(L, f).argtypes = [H, C.c_void_p]
+    L.spc_step.argtypes = [H, dp, C.c_double, C.c_int32]
+    L.spc_step_graph.argtypes = [H, dp, C.c_double, C.c_int32]
+    L.spc_get_step_counter.argtypes = [H, C.POINTER(C.c_uint64)]
+    L.spc_set_step_counter.argtypes = [H, C.c_uint64]
+    L.spc_inject_noise.argtypes = [H, C.c_void_p, C.c_int64]
+    L.spc_clear_noise.argtypes = [H]
+    L.spc_export_noise.argtypes = [H, C.c_uint64, C.c_int32, C.c_void_p]
+    L.spc_noise_per_particle.argtypes = [H]
+    L.spc_rhs_rk.argtypes = [H, C.c_void_p, C.c_double, C.c_double, C.c_void_p]
+    L.spc_rhs_srk.argtypes = [H, C.c_void_p, C.c_void_p]
+    L.spc_neighbours.argtypes = [H, C.c_void_p, C.c_void_p, C.c_int64, C.POINTER(C.c_int64)]
+    L.spc_order_params.argtypes = [H, dp, dp, dp]
+    L.spc_diagnostics.argtypes = [H, C.POINTER(C.c_int64), C.POINTER(C.c_int64),
+                                  C.POINTER(C.c_int64)]
+    L.spc_synchronize.argtypes = [H]
+    L.spc_stream.restype = C.c_void_p
+    L.spc_stream.argtypes = [H]
+    L.spc_philox4x32_10.argtypes = [C.POINTER(C.c_uint32), C.POINTER(C.c_uint32),
+                                    C.POINTER(C.c_uint32)]
+    L.spc_profile_steps.argtypes = [H, C.c_double, C.c_int32, dp, C.c_int32]
+    L.spc_alloc_pinned.argtypes = [C.c_size_t, C.POINTER(C.c_void_p)]
+    L.spc_free_pinned.argtypes = [C.c_void_p]
+    _lib = L
+    return L
+
+
+def _ptr(a: np.ndarray) -> C.c_void_p:
+    return C.c_void_p(a.ctypes.data)
+
+
+def _f64(a, n: int) -> np.ndarray:
+    a = np.ascontiguousarray(a, dtype=np.float64)
+    if a.size != n:
+        raise ValueError(f"expected {n} values, got {a.size}")
+    return a
+
+
+def make_params(*, L, v0, sigma, rho, alpha, D_phi, rho_0=1.0, model=MODEL_CHIMERA,
+                stepper=STEPPER_EULER, neighbour=NEIGHBOUR_CELL, precision=PRECISION_FP64,
+                skin=0.05, seed=0, system_id=0, flags=0) -> Params:
+    return Params(model, stepper, neighbour, precision, L, v0, sigma, rho, alpha, D_phi, rho_0,
+                  skin, seed, system_id, flags)
+
+
+class System:
+    """One particle system on the GPU (a handle of the C-ABI)."""
+
+    def __init__(self, n: int, params: Params):
+        self._L = lib()
+        self.n = int(n)
+        self.params = params
+        h = C.c_void_p()
+        self._check(self._L.spc_create(C.byref(params), self.n, C.byref(h)), None)
+        self.h = h
+        self.t = 0.0
+
+    def _check(self, rc: int, h=None):
+        if rc != SPC_OK:
+            msg = self._L.spc_last_error(h if h is not None else getattr(self, "h", None))
+            raise SpcError(rc, (msg or b"").decode())
+
+    def close(self):
+        if getattr(self, "h", None):
+            self._L.spc_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    # state ---------------------------------------------------------------
+    def upload_state(self, aos):
+        a = _f64(aos, 3 * self.n)
+        self._check(self._L.spc_upload_state(self.h, _ptr(a)), self.h)
+
+    def download_state(self, out=None) -> np.ndarray:
+        out = np.empty(3 * self.n) if out is None else out
+        self._check(self._L.spc_download_state(self.h, _ptr(out)), self.h)
+        return out
+
+    def upload_omega(self, omega):
+        a = _f64(omega, self.n)
+        self._check(self._L.spc_upload_omega(self.h, _ptr(a)), self.h)
+
+    def download_rk4_buffers(self) -> np.ndarray:
+        out = np.empty(12 * self.n)
+        self._check(self._L.spc_download_rk4_buffers(self.h, _ptr(out)), self.h)
+        return out
+
+    def upload_rk4_buffers(self, buf):
+        a = _f64(buf, 12 * self.n)
+        self._check(self._L.spc_upload_rk4_buffers(self.h, _ptr(a)), self.h)
+
+    # stepping ------------------------------------------------------------
+    def step(self, dt: float, nsteps: int, graph: bool = False) -> float:
+        t = C.c_double(self.t)
+        f = self._L.spc_step_graph if graph else self._L.spc_step
+        self._check(f(self.h, C.byref(t), dt, int(nsteps)), self.h)
+        self.t = t.value
+        return self.t
+
+    @property
+    def step_counter(self) -> int:
+        v = C.c_uint64()
+        self._check(self._L.spc_get_step_counter(self.h, C.byref(v)), self.h)
+        return v.value
+
+    @step_counter.setter
+    def step_counter(self, v: int):
+        self._check(self._L.spc_set_step_counter(self.h, int(v)), self.h)
+
+    @property
+    def noise_per_particle(self) -> int:
+        return self._L.spc_noise_per_particle(self.h)
+
+    def inject_noise(self, normals):
+        a = np.ascontiguousarray(normals, dtype=np.float64)
+        self._keep_noise = a
+        self._check(self._L.spc_inject_noise(self.h, _ptr(a), a.size), self.h)
+
+    def clear_noise(self):
+        self._check(self._L.spc_clear_noise(self.h), self.h)
+
+    def export_noise(self, first_step: int, nsteps: int) -> np.ndarray:
+        out = np.empty(max(nsteps * self.n * self.noise_per_particle, 1))
+        self._check(self._L.spc_export_noise(self.h, int(first_step), int(nsteps), _ptr(out)),
+                    self.h)
+        return out[: nsteps * self.n * self.noise_per_particle]
+
+    # parity hooks --------------------------------------------------------
+    def rhs_rk(self, k_prev, k_coef: float, dt: float, k_next_init=None) -> np.ndarray:
+        kp = _f64(k_prev, 3 * self.n)
+        kn = np.zeros(3 * self.n) if k_next_init is None else _f64(k_next_init, 3 * self.n).copy()
+        self._check(self._L.spc_rhs_rk(self.h, _ptr(kp), k_coef, dt, _ptr(kn)), self.h)
+        return kn
+
+    def rhs_srk(self):
+        d = np.empty(3 * self.n)
+        a = np.empty(2 * self.n)
+        self._check(self._L.spc_rhs_srk(self.h, _ptr(d), _ptr(a)), self.h)
+        return d, a
+
+    def neighbours(self):
+        counts = np.empty(self.n, np.int32)
+        total = C.c_int64()
+        self._check(self._L.spc_neighbours(self.h, _ptr(counts), None, 0, C.byref(total)), self.h)
+        idx = np.empty(max(total.value, 1), np.int32)
+        self._check(self._L.spc_neighbours(self.h, _ptr(counts), _ptr(idx), idx.size,
+                                           C.byref(total)), self.h)
+        offsets = np.zeros(self.n + 1, np.int64)
+        np.cumsum(counts, out=offsets[1:])
+        return offsets, idx[: total.value]
+
+    def order_params(self):
+        R, psi, Rl = C.c_double(), C.c_double(), C.c_double()
+        self._check(self._L.spc_order_params(self.h, C.byref(R), C.byref(psi), C.byref(Rl)),
+                    self.h)
+        return {"R": R.value, "psi": psi.value, "R_local": Rl.value}
+
+    def diagnostics(self):
+        c, v, e = C.c_int64(), C.c_int64(), C.c_int64()
+        self._check(self._L.spc_diagnostics(self.h, C.byref(c), C.byref(v), C.byref(e)), self.h)
+        return {"clamped_cells": c.value, "verlet_rebuilds": v.value, "error_word": e.value}
+
+    def profile_steps(self, dt: float, nsteps: int) -> dict:
+        out = (C.c_double * 6)()
+        self._check(self._L.spc_profile_steps(self.h, dt, int(nsteps), out, 6), self.h)
+        keys = ("stage", "sort", "gather", "pass1", "pass2", "step")
+        return {k: out[i] for i, k in enumerate(keys)}
+
+    def synchronize(self):
+        self._check(self._L.spc_synchronize(self.h), self.h)
+
+    @property
+    def stream(self) -> int:
+        return self._L.spc_stream(self.h)
+
+
+def philox4x32_10(ctr, key):
+    """Philox4x32-10 evaluated on the device."""
+    L = lib()
+    c = (C.c_uint32 * 4)(*[int(v) & 0xFFFFFFFF for v in ctr])
+    k = (C.c_uint32 * 2)(*[int(v) & 0xFFFFFFFF for v in key])
+    o = (C.c_uint32 * 4)()
+    rc = L.spc_philox4x32_10(c, k, o)
+    if rc != SPC_OK:
+        raise SpcError(rc, (L.spc_last_error(None) or b"").decode())
+    return [int(v) for v in o]
+
+
+def header_functions() -> list[str]:
+    """Names of the functions include/spc_gb300.h declares."""
+    import re
+    path = os.path.join(_build.ROOT, "include", "spc_gb300.h")
+    text = open(path).read()
+    return sorted(set(re.findall(r"^\s*(?:int|void \*|const char \*)\s*(spc_\w+)\(", text, re.M)))

@@ -1,0 +1,133 @@
+// Device helpers shared by every kernel of the particle-update path.
+//
+// Parity-critical double arithmetic is written with the _rn intrinsics so
+// that nvcc never fuses a product into an add: the reference's C++ is plain
+// unfused IEEE double, and cutoff decisions must come out bit-identical.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace spc {
+
+constexpr int kWarp = 32;
+
+__device__ __forceinline__ double dadd(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ double dsub(double a, double b) { return __dsub_rn(a, b); }
+__device__ __forceinline__ double dmul(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ double ddiv(double a, double b) { return __ddiv_rn(a, b); }
+__device__ __forceinline__ double dsqrt(double a) { return __dsqrt_rn(a); }
+
+// Per-system constants, the reference's ChimeraSystem / PeriodicBoundaryConditions
+// members (ChimeraSystem.cpp:19-33, PeriodicBoundaryConditions.cpp:13-14).
+struct SysConst {
+  int n;          // particles
+  int nc;         // num_subcells_ = int(kL / rho)
+  int ncell;      // nc * nc
+  int allpairs;   // rho > 0.25 L: EvaluateInteractionsWithAllPairs (ChimeraSystem.cpp:90-98)
+  double L, rL;   // x_size_, x_rsize_ = 1.0 / x_size
+  double rho2;    // rho_squared_ = rho * rho
+  double v0, sigma, alpha, D;
+  double cell;    // cell side L / nc, origin of the float prefilter coordinates
+  float cell_f;
+  float lo2, hi2; // prefilter: float dr^2 < lo2 => inside, > hi2 => outside, else decide in FP64
+  int exact_all;  // decide every candidate in FP64
+};
+
+// PeriodicBoundaryConditions::ClassAEffectiveParticleDistance (PeriodicBoundaryConditions.cpp:22-35):
+// d -= static_cast<int>(d * 2.0 * rL) * L
+__device__ __forceinline__ double min_image_1d(double d, double rL, double L) {
+  const int k = __double2int_rz(dmul(dmul(d, 2.0), rL));
+  return dsub(d, dmul(__int2double_rn(k), L));
+}
+
+// The reference's cutoff test dr^2 <= rho^2 on two (already wrapped) positions
+// (ChimeraSystem.cpp:407-410), operation for operation.
+__device__ __forceinline__ bool exact_within(const SysConst &sc, double xi, double yi, double xj,
+                                             double yj) {
+  const double dx = min_image_1d(dsub(xj, xi), sc.rL, sc.L);
+  const double dy = min_image_1d(dsub(yj, yi), sc.rL, sc.L);
+  const double dr2 = dadd(dmul(dx, dx), dmul(dy, dy));
+  return dr2 <= sc.rho2;
+}
+
+// ApplyPeriodicBoundaryConditions (PeriodicBoundaryConditions.cpp:117-121): x - floor(x * rL) * L
+__device__ __forceinline__ double wrap_1d(double x, double rL, double L) {
+  return dsub(x, dmul(floor(dmul(x, rL)), L));
+}
+
+// The conditional copy-wrap inside the force loops (ChimeraSystem.cpp:299-302):
+// both coordinates are wrapped when either is outside [0, L).
+__device__ __forceinline__ void wrap_if_outside(const SysConst &sc, double &x, double &y) {
+  if (x < 0.0 || x >= sc.L || y < 0.0 || y >= sc.L) {
+    const double xw = wrap_1d(x, sc.rL, sc.L);
+    const double yw = wrap_1d(y, sc.rL, sc.L);
+    x = xw;
+    y = yw;
+  }
+}
+
+// int(x / x_size_ * num_subcells_x_) (ChimeraSystem.cpp:304-305).  An index
+// outside [0, nc) (x within an ulp of L) is clamped; *clamped is set.
+__device__ __forceinline__ int cell_coord(const SysConst &sc, double x, int &clamped) {
+  int c = __double2int_rz(dmul(ddiv(x, sc.L), (double)sc.nc));
+  if (c < 0) {
+    c = 0;
+    clamped = 1;
+  } else if (c >= sc.nc) {
+    c = sc.nc - 1;
+    clamped = 1;
+  }
+  return c;
+}
+
+// AdjustNeighboringCellToPeriodicBoundaries (ChimeraSystem.cpp:905-922)
+__device__ __forceinline__ int adjust_cell(int c, int nc) {
+  return c < 0 ? nc - 1 : (c >= nc ? 0 : c);
+}
+
+// ---------------------------------------------------------------------------
+// Philox4x32-10 (Salmon, Moraes, Dror, Shaw, "Parallel Random Numbers: As Easy
+// as 1, 2, 3", SC'11): counter-based, so every (particle, step) draw is a pure
+// function of (seed, system, step, particle) and needs no stored RNG state.
+struct U4 {
+  uint32_t x, y, z, w;
+};
+
+__device__ __forceinline__ U4 philox4x32_10(U4 c, uint32_t k0, uint32_t k1) {
+#pragma unroll
+  for (int r = 0; r < 10; ++r) {
+    const uint32_t lo0 = 0xD2511F53u * c.x, hi0 = __umulhi(0xD2511F53u, c.x);
+    const uint32_t lo1 = 0xCD9E8D57u * c.z, hi1 = __umulhi(0xCD9E8D57u, c.z);
+    c = U4{hi1 ^ c.y ^ k0, lo1, hi0 ^ c.w ^ k1, lo0};
+    k0 += 0x9E3779B9u;
+    k1 += 0xBB67AE85u;
+  }
+  return c;
+}
+
+// Two standard normals for (particle i, step) by Box-Muller on two 53-bit
+// uniforms; u1 in (0, 1] so the logarithm is finite.
+__device__ __forceinline__ void philox_normal2(uint64_t seed, uint32_t system_id, uint64_t step,
+                                               uint32_t i, double &z0, double &z1) {
+  const U4 o = philox4x32_10(U4{i, system_id, (uint32_t)step, (uint32_t)(step >> 32)},
+                             (uint32_t)seed, (uint32_t)(seed >> 32));
+  const uint64_t a = ((((uint64_t)o.x) << 32) | o.y) >> 11;
+  const uint64_t b = ((((uint64_t)o.z) << 32) | o.w) >> 11;
+  const double u1 = (double)(a + 1) * 0x1.0p-53;
+  const double u2 = (double)b * 0x1.0p-53;
+  const double r = sqrt(-2.0 * log(u1));
+  double s, c;
+  sincospi(2.0 * u2, &s, &c);
+  z0 = r * c;
+  z1 = r * s;
+}
+
+// Error word bits reported through spc_diagnostics.
+enum : unsigned long long {
+  kErrNone = 0,
+  kErrVerletOverflow = 1ull << 0,  // a Verlet row exceeded its capacity
+  kErrNoiseMissing = 1ull << 1,
+};
+
+}  // namespace spc

@@ -1,0 +1,618 @@
+// Kernels of one right-hand-side evaluation and the fused stepper updates.
+//
+// One evaluation (the reference's EvaluateInteractionsWithLinkedList,
+// ChimeraSystem.cpp:258-426 / :429-645) runs as:
+//   k_stage   stage state s + k_coef*dt*k_prev, copy-wrap, cell key  (ChimeraSystem.cpp:270-309)
+//   sort      stable radix sort of (key, index)                       (:335-338)
+//   k_gather  particles into cell order + float prefilter coordinates
+//   k_cell_pass<...>  one warp per cell tile: the 3x3 stencil in the
+//             reference's order, the exact FP64 cutoff, the alignment sums,
+//             then a fused epilogue (k_next, or the whole stepper update with
+//             noise and the engine's periodic wrap).
+// When rho > L/4 the reference switches to all pairs (ChimeraSystem.cpp:90-98)
+// on unwrapped stage positions; k_allpairs_pass does the same.
+#pragma once
+
+#include "spc_device.cuh"
+
+namespace spc {
+
+enum { kPrecFP64 = 0, kPrecFP32C = 1 };
+// what a pass accumulates over the neighbours of i
+enum { kKindSin = 0, kKindCos2 = 1, kKindNb = 2 };
+// what the pass does with the sums (runtime, warp-uniform)
+enum Epilogue {
+  kEpiRkK = 0,         // write k_next into k slot `kq_out` (RK form)
+  kEpiRk4Combine = 1,  // k4, then the RK4 combine and the wrap
+  kEpiEuler = 2,       // StochasticEulerStepper update + wrap
+  kEpiSrk1 = 3,        // SRK pass 1: phase rate and n_i in cell order
+  kEpiEulerPtr = 4,    // StochasticEulerStepperPtr update + wrap
+  kEpiSrk2 = 5,        // SRK pass 2 and the strong-1.5 update + wrap
+  kEpiSrk2Out = 6,     // SRK pass 2, derivative / additional_derivative out
+  kEpiCount = 7,       // neighbour counts
+  kEpiList = 8,        // neighbour indices in visiting order
+  kEpiLocalOrder = 9,  // per-particle local order parameter
+};
+
+constexpr int kKSlots = 6;  // RK4 k1..k4 (persistent) + two scratch slots for spc_rhs_rk
+
+struct KArgs {
+  SysConst sc;
+  // state, structure of arrays, original index order
+  double *x, *y, *phi;
+  const double *omega;
+  double *kx[kKSlots], *ky[kKSlots], *kphi[kKSlots];
+  // stage (original order)
+  double *st_x, *st_y, *st_phi;
+  uint32_t *keys, *vals;             // unsorted (key, index)
+  const uint32_t *skeys, *svals;     // sorted
+  int *cell_start;
+  // cell order
+  double *sx, *sy, *sphi;
+  float2 *fxy;                       // prefilter coordinates relative to the cell origin
+  float2 *cs;                        // FP32C: (cos phi, sin phi)
+  int *pidx;                         // original index of cell-order slot p
+  double *dphi_s;                    // SRK pass 1 phase rate, cell order
+  float *dphi_f;                     // same, float (FP32C)
+  int *cnt_s;                        // n_i, cell order
+  // parity outputs (original order)
+  double *out_d, *out_a, *out_r;
+  int *out_cnt;
+  const long long *list_off;
+  int *list_idx;
+  // stepping
+  double dt;
+  int kq_out;                        // k slot written by kEpiRkK / kEpiRk4Combine (k4)
+  const double *noise;               // injected normals of this step, or null for Philox
+  int noise_m;                       // normals per particle
+  uint64_t seed;
+  uint32_t system_id;
+  const unsigned long long *step_base;  // device step counter
+  int step_off;                      // this step = *step_base + step_off
+  int is_vortex;
+  unsigned long long *clamped;
+};
+
+// ---------------------------------------------------------------------------
+// k_stage: rk = s + (k_coef*dt) * k_prev (ChimeraSystem.cpp:274-276), the copy
+// wrap and cell key (:295-308).  kq < 0 means k_prev is all zeros (the Euler
+// stepper's zero-filled buffer, StochasticEulerStepper.hpp:34); rk_form = 0 is
+// the SRK form, whose stage state is the state itself (:456-458).
+__global__ void k_stage(KArgs a, int rk_form, int kq, double kcdt) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const SysConst &sc = a.sc;
+  if (i >= sc.n) return;
+  double x = a.x[i], y = a.y[i], ph = a.phi[i];
+  if (rk_form) {
+    const double kx = kq >= 0 ? a.kx[kq][i] : 0.0;
+    const double ky = kq >= 0 ? a.ky[kq][i] : 0.0;
+    const double kp = kq >= 0 ? a.kphi[kq][i] : 0.0;
+    x = dadd(x, dmul(kcdt, kx));
+    y = dadd(y, dmul(kcdt, ky));
+    ph = dadd(ph, dmul(kcdt, kp));
+  }
+  if (sc.allpairs) {
+    // all pairs use the unwrapped stage positions (ChimeraSystem.cpp:135-153)
+    a.sx[i] = x;
+    a.sy[i] = y;
+    a.sphi[i] = ph;
+    a.pidx[i] = i;
+    return;
+  }
+  wrap_if_outside(sc, x, y);
+  int clamped = 0;
+  const int cx = cell_coord(sc, x, clamped);
+  const int cy = cell_coord(sc, y, clamped);
+  if (clamped) atomicAdd(a.clamped, 1ull);
+  a.st_x[i] = x;
+  a.st_y[i] = y;
+  a.st_phi[i] = ph;
+  a.keys[i] = (uint32_t)(cy * sc.nc + cx);
+  a.vals[i] = (uint32_t)i;
+}
+
+// Phase reduced to about [-pi, pi] in double, then float (FP32C trig input).
+__device__ __forceinline__ float reduced_phase_f(double ph) {
+  const double two_pi = 6.283185307179586;
+  const double inv_two_pi = 0.15915494309189535;
+  return (float)(ph - two_pi * rint(ph * inv_two_pi));
+}
+
+template <int PREC>
+__global__ void k_gather(KArgs a) {
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  const SysConst &sc = a.sc;
+  if (p >= sc.n) return;
+  const int i = (int)a.svals[p];
+  const int key = (int)a.skeys[p];
+  const int cx = key % sc.nc, cy = key / sc.nc;
+  const double x = a.st_x[i], y = a.st_y[i], ph = a.st_phi[i];
+  a.sx[p] = x;
+  a.sy[p] = y;
+  a.sphi[p] = ph;
+  a.pidx[p] = i;
+  a.fxy[p] = make_float2((float)(x - (double)cx * sc.cell), (float)(y - (double)cy * sc.cell));
+  if constexpr (PREC == kPrecFP32C) {
+    float s, c;
+    sincosf(reduced_phase_f(ph), &s, &c);
+    a.cs[p] = make_float2(c, s);
+  }
+}
+
+// FP32C: in the all-pairs layout the slot is the particle itself.
+__global__ void k_fill_cs(KArgs a) {
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= a.sc.n) return;
+  float s, c;
+  sincosf(reduced_phase_f(a.sphi[p]), &s, &c);
+  a.cs[p] = make_float2(c, s);
+}
+
+// ---------------------------------------------------------------------------
+// Per-i accumulators of one pass.
+template <int PREC>
+struct Acc;
+
+template <>
+struct Acc<kPrecFP64> {
+  double s0, s1;  // sin sum | cos/n sum, (dphi) cos/n sum | cos, sin sums
+  int n;
+  __device__ void init() { s0 = 0.0; s1 = 0.0; n = 0; }
+};
+
+template <>
+struct Acc<kPrecFP32C> {
+  float s0, c0, s1, c1;  // Kahan sums and compensations
+  int n;
+  __device__ void init() { s0 = c0 = s1 = c1 = 0.0f; n = 0; }
+};
+
+__device__ __forceinline__ void kahan_add(float &sum, float &comp, float v) {
+  const float y = v - comp;
+  const float t = sum + y;
+  comp = (t - sum) - y;
+  sum = t;
+}
+
+// Everything an i lane needs inside the candidate loop.
+struct ILane {
+  int p;        // cell-order slot
+  bool valid;
+  float fx, fy; // prefilter coordinates
+  double x, y;  // wrapped stage position
+  double phi;   // stage phase
+  double card;  // pass 2: n_i from pass 1 (double, as neighborhood_cardinality_)
+  double dphi;  // pass 2: own phase rate
+  float ca, sa; // FP32C: cos(phi + alpha), sin(phi + alpha)
+  float dphif;
+};
+
+template <int PREC, int KIND>
+__device__ __forceinline__ void accept_pair(const KArgs &a, const ILane &il, Acc<PREC> &acc, int pj,
+                                            float cjc, float cjs, float dphij_f, long long &wpos) {
+  const SysConst &sc = a.sc;
+  if constexpr (KIND == kKindSin) {
+    if constexpr (PREC == kPrecFP64) {
+      // alignment_force_[i] += sin(phi_j - phi_i - alpha_) (ChimeraSystem.cpp:412)
+      acc.s0 = dadd(acc.s0, sin(dsub(dsub(a.sphi[pj], il.phi), sc.alpha)));
+    } else {
+      // sin(phi_j - (phi_i + alpha)) by the angle-difference identity
+      kahan_add(acc.s0, acc.c0, cjs * il.ca - cjc * il.sa);
+    }
+    acc.n++;
+  } else if constexpr (KIND == kKindCos2) {
+    if constexpr (PREC == kPrecFP64) {
+      // ChimeraSystem.cpp:634-637
+      const double c = cos(dsub(dsub(a.sphi[pj], il.phi), sc.alpha));
+      acc.s0 = dadd(acc.s0, ddiv(c, il.card));
+      acc.s1 = dadd(acc.s1, ddiv(dmul(dsub(a.dphi_s[pj], il.dphi), c), il.card));
+    } else {
+      const float c = cjc * il.ca + cjs * il.sa;
+      kahan_add(acc.s0, acc.c0, c);
+      kahan_add(acc.s1, acc.c1, (dphij_f - il.dphif) * c);
+    }
+    acc.n++;
+  } else {
+    if (a.list_idx) a.list_idx[wpos++] = a.pidx[pj];
+    if constexpr (PREC == kPrecFP64) {
+      if (a.out_r) {
+        acc.s0 += cos(a.sphi[pj]);
+        acc.s1 += sin(a.sphi[pj]);
+      }
+    }
+    acc.n++;
+  }
+}
+
+__device__ __forceinline__ double noise_at(const KArgs &a, int i, int k, double z0, double z1) {
+  if (a.noise) return a.noise[(size_t)i * a.noise_m + k];
+  return k == 0 ? z0 : z1;
+}
+
+// Fused epilogue for particle i (original index) at cell-order slot p.
+template <int PREC, int KIND>
+__device__ void epilogue(const KArgs &a, int epi, const ILane &il, Acc<PREC> &acc, int i) {
+  const SysConst &sc = a.sc;
+  const int p = il.p;
+  if constexpr (KIND == kKindNb) {
+    if (epi == kEpiCount) a.out_cnt[i] = acc.n;
+    if (epi == kEpiLocalOrder) {
+      const double re = acc.s0 + cos(il.phi), im = acc.s1 + sin(il.phi);
+      a.out_r[i] = sqrt(re * re + im * im) / (double)(acc.n + 1);
+    }
+    return;
+  }
+  double z0 = 0.0, z1 = 0.0;
+  if ((epi == kEpiEuler || epi == kEpiEulerPtr || epi == kEpiSrk2) && !a.noise)
+    philox_normal2(a.seed, a.system_id, *a.step_base + (unsigned long long)a.step_off, (uint32_t)i,
+                   z0, z1);
+  const double dt = a.dt;
+  if constexpr (PREC == kPrecFP64) {
+    const double cph = cos(il.phi), sph = sin(il.phi);
+    const double d0 = dmul(sc.v0, cph), d1 = dmul(sc.v0, sph);  // v_0_ * cos(phi_i) (:419-420)
+    if constexpr (KIND == kKindSin) {
+      // sigma_ * alignment_force_[i] / neighborhood_cardinality_[i] (:421-424)
+      const bool has = acc.n != 0;
+      const double rate = has ? ddiv(dmul(sc.sigma, acc.s0), (double)acc.n) : 0.0;
+      if (epi == kEpiRkK || epi == kEpiRk4Combine) {
+        const int q = a.kq_out;
+        a.kx[q][i] = d0;
+        a.ky[q][i] = d1;
+        if (has) a.kphi[q][i] = rate;  // otherwise k_next keeps its value (H5)
+        if (epi == kEpiRk4Combine) {
+          // RungeKutta4Stepper.cpp:52-54
+          const double k4p = a.kphi[q][i];
+          double xs = a.x[i], ys = a.y[i], ps = a.phi[i];
+          const double sx_ = dadd(dadd(dadd(a.kx[0][i], dmul(2.0, a.kx[1][i])), dmul(2.0, a.kx[2][i])), d0);
+          const double sy_ = dadd(dadd(dadd(a.ky[0][i], dmul(2.0, a.ky[1][i])), dmul(2.0, a.ky[2][i])), d1);
+          const double sp_ = dadd(dadd(dadd(a.kphi[0][i], dmul(2.0, a.kphi[1][i])), dmul(2.0, a.kphi[2][i])), k4p);
+          xs = dadd(xs, ddiv(dmul(sx_, dt), 6.0));
+          ys = dadd(ys, ddiv(dmul(sy_, dt), 6.0));
+          ps = dadd(ps, dmul(ddiv(sp_, 6.0), dt));
+          a.x[i] = wrap_1d(xs, sc.rL, sc.L);  // SimulationEngine.cpp:154
+          a.y[i] = wrap_1d(ys, sc.rL, sc.L);
+          a.phi[i] = ps;
+        }
+      } else if (epi == kEpiEuler) {
+        // StochasticEulerStepper.hpp:43-45 with AddNoise (ChimeraSystem.cpp:927-930)
+        const double sdt = dsqrt(dt);
+        const double sto = dmul(dsqrt(dmul(2.0, sc.D)), noise_at(a, i, 0, z0, z1));
+        const double xs = dadd(a.x[i], dadd(dmul(dt, d0), dmul(sdt, 0.0)));
+        const double ys = dadd(a.y[i], dadd(dmul(dt, d1), dmul(sdt, 0.0)));
+        a.phi[i] = dadd(a.phi[i], dadd(dmul(dt, rate), dmul(sdt, sto)));
+        a.x[i] = wrap_1d(xs, sc.rL, sc.L);
+        a.y[i] = wrap_1d(ys, sc.rL, sc.L);
+      } else if (epi == kEpiEulerPtr) {
+        // StochasticEulerStepperPtr.hpp:44-51
+        const double dW = dmul(dsqrt(dt), noise_at(a, i, 0, z0, z1));
+        const double xs = dadd(a.x[i], dmul(d0, dt));
+        const double ys = dadd(a.y[i], dmul(d1, dt));
+        a.phi[i] = dadd(a.phi[i], dadd(dmul(rate, dt), dmul(dsqrt(dmul(2.0, sc.D)), dW)));
+        a.x[i] = wrap_1d(xs, sc.rL, sc.L);
+        a.y[i] = wrap_1d(ys, sc.rL, sc.L);
+      } else if (epi == kEpiSrk1) {
+        a.dphi_s[p] = rate;  // derivative is zero-filled each step: 0 when isolated
+        a.cnt_s[p] = acc.n;
+      }
+    } else {  // kKindCos2: SRK pass 2 (ChimeraSystem.cpp:642-643)
+      const double A0 = dmul(acc.s0, -dsqrt(dmul(2.0, sc.D)));
+      const double A1 = dadd(acc.s1, dmul(dmul(-2.0, sc.D), il.dphi));
+      const double d2 = il.dphi;
+      if (epi == kEpiSrk2Out) {
+        a.out_d[3 * (size_t)i] = d0;
+        a.out_d[3 * (size_t)i + 1] = d1;
+        a.out_d[3 * (size_t)i + 2] = d2;
+        a.out_a[2 * (size_t)i] = A0;
+        a.out_a[2 * (size_t)i + 1] = A1;
+      } else {
+        // StochasticRungeKuttaStepper.hpp:44-55 (+ omega: StochasticRungeKuttaStepperPtr.hpp:65)
+        const double U1 = noise_at(a, i, 0, z0, z1), U2 = noise_at(a, i, 1, z0, z1);
+        const double sdt = dsqrt(dt);
+        const double dW = dmul(U1, sdt);
+        const double dZ = dmul(dmul(dmul(0.5, dt), sdt), dadd(U1, ddiv(U2, dsqrt(3.0))));
+        const double D = sc.D;
+        const double s2D = dsqrt(dmul(2.0, D));
+        const double dtdt_x = dmul(dmul(dmul(0.5, dadd(dmul(d2, d1), dmul(D, d0))), dt), dt);
+        const double xs = dadd(a.x[i], dsub(dsub(dmul(d0, dt), dmul(dmul(s2D, d1), dZ)), dtdt_x));
+        const double dtdt_y = dmul(dmul(dmul(0.5, dsub(dmul(d2, d0), dmul(D, d1))), dt), dt);
+        const double ys = dadd(a.y[i], dadd(dadd(dmul(d1, dt), dmul(dmul(s2D, d0), dZ)), dtdt_y));
+        const double drift = a.is_vortex ? dmul(dadd(a.omega[i], d2), dt) : dmul(d2, dt);
+        const double ps = dadd(a.phi[i], dadd(dadd(dadd(drift, dmul(s2D, dW)), dmul(A0, dZ)),
+                                              dmul(dmul(dmul(0.5, A1), dt), dt)));
+        a.x[i] = wrap_1d(xs, sc.rL, sc.L);
+        a.y[i] = wrap_1d(ys, sc.rL, sc.L);
+        a.phi[i] = ps;
+      }
+    }
+  } else {
+    // FP32C: right-hand sides and increments in float, accumulated into the
+    // double positions and phase.
+    const float ph_r = reduced_phase_f(il.phi);
+    float sph, cph;
+    sincosf(ph_r, &sph, &cph);
+    const float v0 = (float)sc.v0, D = (float)sc.D, dtf = (float)dt;
+    const float d0 = v0 * cph, d1 = v0 * sph;
+    if constexpr (KIND == kKindSin) {
+      const bool has = acc.n != 0;
+      const float rate = has ? (float)sc.sigma * acc.s0 / (float)acc.n : 0.0f;
+      if (epi == kEpiRkK || epi == kEpiRk4Combine) {
+        const int q = a.kq_out;
+        a.kx[q][i] = (double)d0;
+        a.ky[q][i] = (double)d1;
+        if (has) a.kphi[q][i] = (double)rate;
+        if (epi == kEpiRk4Combine) {
+          const float k4p = (float)a.kphi[q][i];
+          const float sx_ = (float)a.kx[0][i] + 2.0f * (float)a.kx[1][i] + 2.0f * (float)a.kx[2][i] + d0;
+          const float sy_ = (float)a.ky[0][i] + 2.0f * (float)a.ky[1][i] + 2.0f * (float)a.ky[2][i] + d1;
+          const float sp_ = (float)a.kphi[0][i] + 2.0f * (float)a.kphi[1][i] + 2.0f * (float)a.kphi[2][i] + k4p;
+          const float sixth = dtf / 6.0f;
+          a.x[i] = wrap_1d(a.x[i] + (double)(sx_ * sixth), sc.rL, sc.L);
+          a.y[i] = wrap_1d(a.y[i] + (double)(sy_ * sixth), sc.rL, sc.L);
+          a.phi[i] = a.phi[i] + (double)(sp_ * sixth);
+        }
+      } else if (epi == kEpiEuler || epi == kEpiEulerPtr) {
+        const float xi = (float)noise_at(a, i, 0, z0, z1);
+        const float sdt = sqrtf(dtf);
+        const float s2D = sqrtf(2.0f * D);
+        a.x[i] = wrap_1d(a.x[i] + (double)(dtf * d0), sc.rL, sc.L);
+        a.y[i] = wrap_1d(a.y[i] + (double)(dtf * d1), sc.rL, sc.L);
+        a.phi[i] = a.phi[i] + (double)(dtf * rate + sdt * s2D * xi);
+      } else if (epi == kEpiSrk1) {
+        a.dphi_s[p] = (double)rate;
+        a.dphi_f[p] = rate;
+        a.cnt_s[p] = acc.n;
+      }
+    } else {
+      const float inv_n = acc.n ? 1.0f / (float)acc.n : 0.0f;
+      const float s2D = sqrtf(2.0f * D);
+      const float A0 = (acc.s0 * inv_n) * (-s2D);
+      const float A1 = acc.s1 * inv_n + (-2.0f * D) * il.dphif;
+      const float d2 = il.dphif;
+      if (epi == kEpiSrk2Out) {
+        a.out_d[3 * (size_t)i] = (double)d0;
+        a.out_d[3 * (size_t)i + 1] = (double)d1;
+        a.out_d[3 * (size_t)i + 2] = (double)d2;
+        a.out_a[2 * (size_t)i] = (double)A0;
+        a.out_a[2 * (size_t)i + 1] = (double)A1;
+      } else {
+        const float U1 = (float)noise_at(a, i, 0, z0, z1), U2 = (float)noise_at(a, i, 1, z0, z1);
+        const float sdt = sqrtf(dtf);
+        const float dW = U1 * sdt;
+        const float dZ = 0.5f * dtf * sdt * (U1 + U2 * 0.57735026918962576f);
+        const float dx = d0 * dtf - s2D * d1 * dZ - 0.5f * (d2 * d1 + D * d0) * dtf * dtf;
+        const float dy = d1 * dtf + s2D * d0 * dZ + 0.5f * (d2 * d0 - D * d1) * dtf * dtf;
+        const float drift = (a.is_vortex ? (float)a.omega[i] + d2 : d2) * dtf;
+        const float dp = drift + s2D * dW + A0 * dZ + 0.5f * A1 * dtf * dtf;
+        a.x[i] = wrap_1d(a.x[i] + (double)dx, sc.rL, sc.L);
+        a.y[i] = wrap_1d(a.y[i] + (double)dy, sc.rL, sc.L);
+        a.phi[i] = a.phi[i] + (double)dp;
+      }
+    }
+  }
+}
+
+template <int PREC, int KIND>
+__device__ __forceinline__ void load_i(const KArgs &a, ILane &il, int p, bool valid) {
+  il.p = p;
+  il.valid = valid;
+  if (!valid) return;
+  il.x = a.sx[p];
+  il.y = a.sy[p];
+  il.phi = a.sphi[p];
+  if (!a.sc.allpairs) {
+    const float2 f = a.fxy[p];
+    il.fx = f.x;
+    il.fy = f.y;
+  }
+  if constexpr (PREC == kPrecFP32C) {
+    float s, c;
+    sincosf(reduced_phase_f(il.phi) + (float)a.sc.alpha, &s, &c);
+    il.ca = c;
+    il.sa = s;
+  }
+  if constexpr (KIND == kKindCos2) {
+    il.card = (double)a.cnt_s[p];
+    il.dphi = a.dphi_s[p];
+    if constexpr (PREC == kPrecFP32C) il.dphif = a.dphi_f[p];
+  } else {
+    il.dphi = 0.0;
+    il.dphif = 0.0f;
+  }
+}
+
+constexpr int kPassWarps = 4;
+constexpr int kPassThreads = kPassWarps * kWarp;
+constexpr int kIPL = 2;  // i particles per lane: a warp covers a 64-particle cell tile
+
+// One warp per cell tile: up to 64 particles of cell c, two per lane; the
+// warp walks the 9 stencil cells in the reference's order
+// (ChimeraSystem.cpp:39-44) and, within each, the members in ascending index
+// (cell order), staging 32 candidates at a time in shared memory.  The float
+// prefilter decides pairs far from the cutoff; pairs within a relative 3e-5 of
+// rho^2 are decided by the reference's own FP64 test, so neighbour sets are
+// exactly the reference's.
+template <int PREC, int KIND>
+__global__ void __launch_bounds__(kPassThreads) k_cell_pass(KArgs a, int epi) {
+  __shared__ float4 stage[kPassWarps][kWarp];
+  __shared__ float stage_d[kPassWarps][kWarp];
+  const int w = threadIdx.x / kWarp, lane = threadIdx.x % kWarp;
+  const int gwarp = blockIdx.x * kPassWarps + w;
+  const int nwarps = gridDim.x * kPassWarps;
+  const SysConst &sc = a.sc;
+  const int nc = sc.nc;
+  const bool exact_all = sc.exact_all != 0;
+  for (int c = gwarp; c < sc.ncell; c += nwarps) {
+    const int cb = a.cell_start[c], ce = a.cell_start[c + 1];
+    const int cx = c % nc, cy = c / nc;
+    for (int base = cb; base < ce; base += kIPL * kWarp) {
+      ILane il[kIPL];
+      Acc<PREC> acc[kIPL];
+      long long wpos[kIPL];
+#pragma unroll
+      for (int k = 0; k < kIPL; ++k) {
+        const int p = base + k * kWarp + lane;
+        load_i<PREC, KIND>(a, il[k], p, p < ce);
+        acc[k].init();
+        wpos[k] = (KIND == kKindNb && a.list_idx && il[k].valid) ? a.list_off[a.pidx[p]] : 0;
+      }
+      for (int q = 0; q < 9; ++q) {
+        const int ox = (q % 3) - 1, oy = (q / 3) - 1;  // {-1,-1},{0,-1},{1,-1},{-1,0},...
+        const int jx = adjust_cell(cx + ox, nc), jy = adjust_cell(cy + oy, nc);
+        const int cj = jy * nc + jx;
+        const int ja = a.cell_start[cj], jb = a.cell_start[cj + 1];
+        const float shx = (float)ox * sc.cell_f, shy = (float)oy * sc.cell_f;
+        for (int jbase = ja; jbase < jb; jbase += kWarp) {
+          const int pl = jbase + lane;
+          __syncwarp();
+          if (pl < jb) {
+            const float2 f = a.fxy[pl];
+            float cc = 0.0f, ss = 0.0f;
+            if constexpr (PREC == kPrecFP32C) {
+              const float2 t = a.cs[pl];
+              cc = t.x;
+              ss = t.y;
+              if constexpr (KIND == kKindCos2) stage_d[w][lane] = a.dphi_f[pl];
+            }
+            stage[w][lane] = make_float4(f.x + shx, f.y + shy, cc, ss);
+          }
+          __syncwarp();
+          const int cnt = min(kWarp, jb - jbase);
+          for (int t = 0; t < cnt; ++t) {
+            const float4 cj4 = stage[w][t];
+            const float dj = (PREC == kPrecFP32C && KIND == kKindCos2) ? stage_d[w][t] : 0.0f;
+            const int pj = jbase + t;
+#pragma unroll
+            for (int k = 0; k < kIPL; ++k) {
+              if (!il[k].valid || pj == il[k].p) continue;
+              const float dx = cj4.x - il[k].fx, dy = cj4.y - il[k].fy;
+              const float d2 = dx * dx + dy * dy;
+              if (exact_all || d2 <= sc.hi2) {
+                const bool in = (!exact_all && d2 < sc.lo2) ||
+                                exact_within(sc, il[k].x, il[k].y, a.sx[pj], a.sy[pj]);
+                if (in) accept_pair<PREC, KIND>(a, il[k], acc[k], pj, cj4.z, cj4.w, dj, wpos[k]);
+              }
+            }
+          }
+        }
+      }
+#pragma unroll
+      for (int k = 0; k < kIPL; ++k)
+        if (il[k].valid) epilogue<PREC, KIND>(a, epi, il[k], acc[k], a.pidx[il[k].p]);
+    }
+  }
+}
+
+// All pairs (rho > L/4): ChimeraSystem.cpp:117-255.  One thread per i in
+// index order, j ascending, exact FP64 test on unwrapped stage positions.
+constexpr int kAllPairsThreads = 128;
+
+template <int PREC, int KIND>
+__global__ void __launch_bounds__(kAllPairsThreads) k_allpairs_pass(KArgs a, int epi) {
+  __shared__ double tx[kAllPairsThreads], ty[kAllPairsThreads];
+  __shared__ float2 tcs[kAllPairsThreads];
+  __shared__ float td[kAllPairsThreads];
+  const SysConst &sc = a.sc;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  ILane il;
+  Acc<PREC> acc;
+  load_i<PREC, KIND>(a, il, i, i < sc.n);
+  acc.init();
+  long long wpos = (KIND == kKindNb && a.list_idx && il.valid) ? a.list_off[i] : 0;
+  for (int jt = 0; jt < sc.n; jt += kAllPairsThreads) {
+    const int jl = jt + threadIdx.x;
+    __syncthreads();
+    if (jl < sc.n) {
+      tx[threadIdx.x] = a.sx[jl];
+      ty[threadIdx.x] = a.sy[jl];
+      if constexpr (PREC == kPrecFP32C) {
+        tcs[threadIdx.x] = a.cs[jl];
+        if constexpr (KIND == kKindCos2) td[threadIdx.x] = a.dphi_f[jl];
+      }
+    }
+    __syncthreads();
+    const int cnt = min(kAllPairsThreads, sc.n - jt);
+    if (!il.valid) continue;
+    for (int t = 0; t < cnt; ++t) {
+      const int j = jt + t;
+      if (j == i) continue;
+      if (exact_within(sc, il.x, il.y, tx[t], ty[t])) {
+        float cc = 0.0f, ss = 0.0f, dj = 0.0f;
+        if constexpr (PREC == kPrecFP32C) {
+          cc = tcs[t].x;
+          ss = tcs[t].y;
+          if constexpr (KIND == kKindCos2) dj = td[t];
+        }
+        accept_pair<PREC, KIND>(a, il, acc, j, cc, ss, dj, wpos);
+      }
+    }
+  }
+  if (il.valid) epilogue<PREC, KIND>(a, epi, il, acc, i);
+}
+
+// ---------------------------------------------------------------------------
+__global__ void k_aos_to_soa(const double *__restrict__ aos, int n, double *x, double *y,
+                             double *phi) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  x[i] = aos[3 * (size_t)i];
+  y[i] = aos[3 * (size_t)i + 1];
+  phi[i] = aos[3 * (size_t)i + 2];
+}
+
+__global__ void k_soa_to_aos(const double *x, const double *y, const double *phi, int n,
+                             double *__restrict__ aos) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  aos[3 * (size_t)i] = x[i];
+  aos[3 * (size_t)i + 1] = y[i];
+  aos[3 * (size_t)i + 2] = phi[i];
+}
+
+__global__ void k_add_u64(unsigned long long *p, unsigned long long v) { *p += v; }
+
+// Philox normals of steps [first, first + nsteps) in the injection layout.
+__global__ void k_export_noise(uint64_t seed, uint32_t system_id, uint64_t first, int nsteps,
+                               int n, int m, double *out) {
+  const long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= (long long)nsteps * n) return;
+  const int s = (int)(g / n), i = (int)(g % n);
+  double z0, z1;
+  philox_normal2(seed, system_id, first + (uint64_t)s, (uint32_t)i, z0, z1);
+  double *o = out + ((size_t)s * n + i) * m;
+  o[0] = z0;
+  if (m > 1) o[1] = z1;
+}
+
+__global__ void k_philox_kat(U4 c, uint32_t k0, uint32_t k1, uint32_t *out) {
+  const U4 o = philox4x32_10(c, k0, k1);
+  out[0] = o.x;
+  out[1] = o.y;
+  out[2] = o.z;
+  out[3] = o.w;
+}
+
+// Global order parameter partial sums (FP64): sum cos, sum sin.
+__global__ void k_order_sum(const double *phi, int n, double *out2) {
+  __shared__ double sc_[256], ss_[256];
+  double c = 0.0, s = 0.0;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    c += cos(phi[i]);
+    s += sin(phi[i]);
+  }
+  sc_[threadIdx.x] = c;
+  ss_[threadIdx.x] = s;
+  __syncthreads();
+  for (int off = blockDim.x / 2; off > 0; off >>= 1) {
+    if (threadIdx.x < off) {
+      sc_[threadIdx.x] += sc_[threadIdx.x + off];
+      ss_[threadIdx.x] += ss_[threadIdx.x + off];
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    out2[2 * blockIdx.x] = sc_[0];
+    out2[2 * blockIdx.x + 1] = ss_[0];
+  }
+}
+
+}  // namespace spc

@@ -1,0 +1,117 @@
+// The reference's engine loop (SimulationEngine.cpp:149-161) written against
+// the drop-in classes of spc_dropin.hpp, reading the same input format as the
+// oracle's reference driver, so a test can show that a reference-style C++
+// caller gets the reference's trajectory from the GPU path.
+//
+// usage: SPC_REF_N=<N> SPC_REF_L=<L> spc_dropin_driver <input.bin> <output.bin>
+// (mode 0 = run, family 0 = vector classes, family 1 + SRK = vortex with the
+//  first N injected values as frequencies; modes 1/2 = one EvaluateRhs.)
+#include <cstdint>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <vector>
+
+#include "spc_dropin.hpp"
+
+static int env_int(const char *k) {
+  const char *v = std::getenv(k);
+  if (!v) std::exit(2);
+  return std::atoi(v);
+}
+static double env_double(const char *k) {
+  const char *v = std::getenv(k);
+  if (!v) std::exit(2);
+  return std::strtod(v, nullptr);
+}
+extern const int kN = env_int("SPC_REF_N");
+extern const Real kL = env_double("SPC_REF_L");
+
+struct Header {
+  char magic[8];
+  int32_t mode, family, stepper, nsteps, record_every, pad;
+  double v0, sigma, rho, alpha, D_phi, rho_0, t0, dt, k_coef;
+};
+
+static void read_exact(FILE *f, void *p, size_t n) {
+  if (std::fread(p, 1, n, f) != n) std::exit(2);
+}
+
+int main(int argc, char **argv) {
+  if (argc != 3) return 2;
+  FILE *in = std::fopen(argv[1], "rb");
+  if (!in) return 2;
+  Header h;
+  read_exact(in, &h, sizeof(h));
+  if (std::memcmp(h.magic, "SPCREF01", 8) != 0) return 2;
+  const size_t n3 = (size_t)kS * kN;
+  std::vector<Real> state(n3), k_prev(n3), k_next(n3);
+  read_exact(in, state.data(), n3 * 8);
+  read_exact(in, k_prev.data(), n3 * 8);
+  read_exact(in, k_next.data(), n3 * 8);
+  int64_t n_noise = 0;
+  read_exact(in, &n_noise, 8);
+  std::vector<Real> noise((size_t)n_noise);
+  if (n_noise) read_exact(in, noise.data(), (size_t)n_noise * 8);
+  std::fclose(in);
+  FILE *out = std::fopen(argv[2], "wb");
+  if (!out) return 2;
+  auto dump = [&](const Real *p, size_t n) { std::fwrite(p, 8, n, out); };
+  try {
+    Thread thread(argc, argv);
+    PeriodicBoundaryConditions pbc_config(&thread, kL, kL);
+    if (h.family == 1 && h.stepper == 1 && h.mode == 0) {
+      std::vector<Real> omega(noise.begin(), noise.begin() + kN);
+      std::vector<Real> rest(noise.begin() + kN, noise.end());
+      VortexArraysSystem system(&thread, h.v0, h.sigma, h.rho, h.D_phi, h.rho_0, pbc_config, omega);
+      system.InjectNoise(rest);
+      StochasticRungeKuttaStepper stepper(&thread);
+      Real t = h.t0;
+      for (int k = 1; k <= h.nsteps; ++k) {
+        t += h.dt;
+        stepper.DoStep(system, state, t, h.dt);
+        pbc_config.ApplyPeriodicBoundaryConditions(state);
+        thread.SynchronizeVector(state);
+        if ((h.record_every > 0 && k % h.record_every == 0) || k == h.nsteps) dump(state.data(), n3);
+      }
+    } else if (h.family == 0) {
+      ChimeraSystem chimera_system(&thread, h.v0, h.sigma, h.rho, h.alpha, h.D_phi, h.rho_0, pbc_config);
+      if (h.mode == 1) {
+        chimera_system.EvaluateRhs(state, k_prev, k_next, h.k_coef, h.dt);
+        dump(k_next.data(), n3);
+      } else if (h.mode == 2) {
+        std::vector<Real> derivative(n3, 0.0);
+        std::vector<std::vector<Real>> additional(kN, std::vector<Real>(2, 0.0));
+        chimera_system.EvaluateRhs(state, derivative, additional, h.dt);
+        dump(derivative.data(), n3);
+        for (int i = 0; i < kN; ++i) dump(additional[i].data(), 2);
+      } else {
+        if (!noise.empty()) chimera_system.InjectNoise(noise);
+        StochasticEulerStepper euler(&thread);
+        StochasticRungeKuttaStepper srk(&thread);
+        RungeKutta4Stepper rk4(&thread);
+        Real t = h.t0;
+        for (int k = 1; k <= h.nsteps; ++k) {
+          t += h.dt;
+          if (h.stepper == 0)
+            euler.DoStep(chimera_system, state, t, h.dt);
+          else if (h.stepper == 1)
+            srk.DoStep(chimera_system, state, t, h.dt);
+          else
+            rk4.DoStep(chimera_system, state, t, h.dt);
+          pbc_config.ApplyPeriodicBoundaryConditions(state);
+          thread.SynchronizeVector(state);
+          if ((h.record_every > 0 && k % h.record_every == 0) || k == h.nsteps) dump(state.data(), n3);
+        }
+      }
+    } else {
+      std::fprintf(stderr, "spc_dropin_driver: unsupported family/stepper\n");
+      return 5;
+    }
+  } catch (const std::exception &e) {
+    std::fprintf(stderr, "%s\n", e.what());
+    return 3;
+  }
+  std::fclose(out);
+  return 0;
+}

@@ -1,0 +1,174 @@
+// Drop-in classes (spc_dropin.hpp) forwarding to the C-ABI.
+#include "spc_dropin.hpp"
+
+#include <cmath>
+#include <numeric>
+
+Thread::Thread(int, char **) : loop_indices_(kN) {
+  std::iota(loop_indices_.begin(), loop_indices_.end(), 0);
+}
+
+PeriodicBoundaryConditions::PeriodicBoundaryConditions(Thread *thread, Real x_size, Real y_size)
+    : thread_(thread), x_size_(x_size), y_size_(y_size), x_rsize_(1.0 / x_size),
+      y_rsize_(1.0 / y_size) {}
+
+void PeriodicBoundaryConditions::ClassAEffectiveParticleDistance(Real x_i, Real y_i, Real x_j,
+                                                                 Real y_j, Real &dx, Real &dy) {
+  dx = x_j - x_i;
+  dx -= static_cast<int>(dx * 2.0 * x_rsize_) * x_size_;
+  dy = y_j - y_i;
+  dy -= static_cast<int>(dy * 2.0 * y_rsize_) * y_size_;
+}
+
+void PeriodicBoundaryConditions::ApplyPeriodicBoundaryConditions(Real x, Real y, Real &x_pbc,
+                                                                 Real &y_pbc) {
+  x_pbc = x - std::floor(x * x_rsize_) * x_size_;
+  y_pbc = y - std::floor(y * y_rsize_) * y_size_;
+}
+
+void PeriodicBoundaryConditions::ApplyPeriodicBoundaryConditions(std::vector<Real> &s) {
+  ApplyPeriodicBoundaryConditions(s.data(), (long)s.size());
+}
+
+void PeriodicBoundaryConditions::ApplyPeriodicBoundaryConditions(Real *const s, long size) {
+  // The device already wrapped the state it returned, and the wrap is
+  // idempotent on [0, L), so this leaves a device-produced state unchanged.
+  for (long ii = 0; ii + 1 < size; ii += kS) {
+    s[ii] -= std::floor(s[ii] * x_rsize_) * x_size_;
+    s[ii + 1] -= std::floor(s[ii + 1] * y_rsize_) * y_size_;
+  }
+}
+
+// ---------------------------------------------------------------------------
+SpcSystemBase::SpcSystemBase(Thread *thread, int model, Real v_0, Real sigma, Real rho, Real alpha,
+                             Real D_phi, Real rho_0, PeriodicBoundaryConditions &pbc_config)
+    : thread_(thread), pbc_config_(pbc_config), model_(model), v_0_(v_0), sigma_(sigma),
+      rho_(rho), alpha_(alpha), D_phi_(D_phi), rho_0_(rho_0) {}
+
+SpcSystemBase::~SpcSystemBase() {
+  for (spc_handle *&h : handles_) {
+    spc_destroy(h);
+    h = nullptr;
+  }
+}
+
+void SpcSystemBase::Check(int rc, spc_handle *h) const {
+  if (rc != SPC_OK) throw std::runtime_error(std::string("spc: ") + spc_last_error(h));
+}
+
+spc_handle *SpcSystemBase::Handle(int stepper) {
+  if (!handles_[stepper]) {
+    spc_params p{};
+    p.model = model_;
+    p.stepper = stepper;
+    p.neighbour = neighbour_;
+    p.precision = precision_;
+    p.L = pbc_config_.GetXSize();
+    p.v0 = v_0_;
+    p.sigma = sigma_;
+    p.rho = rho_;
+    p.alpha = alpha_;
+    p.D_phi = D_phi_;
+    p.rho_0 = rho_0_;
+    p.skin = skin_;
+    p.seed = seed_;
+    spc_handle *h = nullptr;
+    Check(spc_create(&p, kN, &h), nullptr);
+    handles_[stepper] = h;
+    if (model_ == SPC_MODEL_VORTEX) Check(spc_upload_omega(h, frequencies_.data()), h);
+  }
+  return handles_[stepper];
+}
+
+void SpcSystemBase::Sync(spc_handle *h, const std::vector<Real> &state) {
+  int k = 0;
+  while (handles_[k] != h) ++k;
+  if (shadow_[k] != state) {
+    Check(spc_upload_state(h, state.data()), h);
+    shadow_[k] = state;
+  }
+}
+
+void SpcSystemBase::Advance(int stepper, std::vector<Real> &state, Real &t, Real dt, int nsteps) {
+  if ((int)state.size() != kS * kN) throw std::runtime_error("spc: state size is not 3N");
+  spc_handle *h = Handle(stepper);
+  Sync(h, state);
+  if (inject_pending_) {
+    Check(spc_inject_noise(h, injected_.data(), (int64_t)injected_.size()), h);
+    inject_pending_ = false;
+  }
+  double tt = t;
+  Check(spc_step(h, &tt, dt, nsteps), h);
+  Check(spc_download_state(h, state.data()), h);
+  int k = 0;
+  while (handles_[k] != h) ++k;
+  shadow_[k] = state;
+  t = tt;
+}
+
+// ---------------------------------------------------------------------------
+ChimeraSystem::ChimeraSystem(Thread *thread, Real v_0, Real sigma, Real rho, Real alpha,
+                             Real D_phi, Real rho_0, PeriodicBoundaryConditions &pbc_config)
+    : SpcSystemBase(thread, SPC_MODEL_CHIMERA, v_0, sigma, rho, alpha, D_phi, rho_0, pbc_config) {}
+
+void ChimeraSystem::EvaluateRhs(std::vector<Real> &system_state, const std::vector<Real> &k_prev,
+                                std::vector<Real> &k_next, Real k_coef, Real dt) {
+  spc_handle *h = Handle(SPC_STEPPER_RK4);
+  Sync(h, system_state);
+  Check(spc_rhs_rk(h, k_prev.data(), k_coef, dt, k_next.data()), h);
+}
+
+void ChimeraSystem::EvaluateRhs(std::vector<Real> &system_state, std::vector<Real> &derivative,
+                                std::vector<std::vector<Real>> &additional_derivative, Real dt) {
+  (void)dt;
+  spc_handle *h = Handle(SPC_STEPPER_RK4);
+  Sync(h, system_state);
+  std::vector<Real> d(kS * (size_t)kN), a(2 * (size_t)kN);
+  Check(spc_rhs_srk(h, d.data(), a.data()), h);
+  // the steppers pass zero-filled buffers (StochasticRungeKuttaStepper.hpp:36-39)
+  for (int i = 0; i < kN; ++i) {
+    derivative[kS * i] = d[kS * i];
+    derivative[kS * i + 1] = d[kS * i + 1];
+    derivative[kS * i + 2] += d[kS * i + 2];
+    additional_derivative[i][0] += a[2 * i];
+    additional_derivative[i][1] += a[2 * i + 1];
+  }
+}
+
+void ChimeraSystem::AddNoise(const std::vector<Real> &, std::vector<Real> &derivative, Real) {
+  spc_handle *h = Handle(SPC_STEPPER_EULER);
+  uint64_t step = 0;
+  Check(spc_get_step_counter(h, &step), h);
+  std::vector<Real> xi((size_t)kN);
+  Check(spc_export_noise(h, step, 1, xi.data()), h);
+  const Real intensity = std::sqrt(2.0 * D_phi_);
+  for (int i = 0; i < kN; ++i) derivative[kS * i + 2] = intensity * xi[i];
+}
+
+VortexArraysSystem::VortexArraysSystem(Thread *thread, Real v_0, Real sigma, Real rho, Real D_phi,
+                                       Real rho_0, PeriodicBoundaryConditions &pbc_config,
+                                       const std::vector<Real> &frequencies)
+    : SpcSystemBase(thread, SPC_MODEL_VORTEX, v_0, sigma, rho, 0.0, D_phi, rho_0, pbc_config) {
+  frequencies_ = frequencies;
+  if ((int)frequencies_.size() != kN) throw std::runtime_error("spc: need N frequencies");
+}
+
+void StochasticEulerStepper::DoStep(ChimeraSystem &chimera_system, std::vector<Real> &x, Real t,
+                                    Real dt) {
+  chimera_system.Advance(SPC_STEPPER_EULER, x, t, dt, 1);
+}
+
+void StochasticRungeKuttaStepper::DoStep(ChimeraSystem &system, std::vector<Real> &system_state,
+                                         Real t, Real dt) {
+  system.Advance(SPC_STEPPER_SRK, system_state, t, dt, 1);
+}
+
+void StochasticRungeKuttaStepper::DoStep(VortexArraysSystem &system,
+                                         std::vector<Real> &system_state, Real t, Real dt) {
+  system.Advance(SPC_STEPPER_SRK, system_state, t, dt, 1);
+}
+
+void RungeKutta4Stepper::DoStep(ChimeraSystem &chimera_system, std::vector<Real> &system_state,
+                                Real t, Real dt) {
+  chimera_system.Advance(SPC_STEPPER_RK4, system_state, t, dt, 1);
+}

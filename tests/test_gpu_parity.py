@@ -1,0 +1,258 @@
+"""GPU parity of the CUDA path (through the C-ABI) against the oracle and the
+reference's golden vectors.
+
+Tolerances (the plain FP64 form's contract):
+* neighbour sets: bit-exact, same indices in the same visiting order;
+* right-hand sides: |delta| <= 1e-12 * max(|value|, scale), where for a phase
+  rate scale = (sigma / n_i) sum_j |sin(phi_j - phi_i - alpha)| (a sum that
+  nearly cancels has no meaningful pure relative error; CUDA's and glibc's
+  sin/cos differ in the last ulp);
+* trajectories: |delta| <= 1e-9 after up to 100 steps (x, y by minimum image).
+"""
+import numpy as np
+import pytest
+
+from oracle import pyoracle as po
+from spc2_langevin_integration_gb300 import abi
+from tests._helpers import alignment_scale, golden_cases, init_state, load_golden, periodic_diff
+from tests.test_oracle import PHILOX_KAT
+
+pytestmark = pytest.mark.gpu
+
+RHS_TOL = 1e-12
+TRAJ_TOL = 1e-9
+PRM0 = dict(v0=0.01, sigma=1.0, rho=0.1, alpha=1.45, D_phi=0.005)
+
+
+def gpu(n, L, prm, stepper, model=abi.MODEL_CHIMERA, precision=abi.PRECISION_FP64,
+        neighbour=abi.NEIGHBOUR_CELL, flags=0, seed=0):
+    p = abi.make_params(L=L, stepper=stepper, model=model, precision=precision,
+                        neighbour=neighbour, flags=flags, seed=seed, **prm)
+    return abi.System(n, p)
+
+
+def golden_stepper(g):
+    fam, stp = int(g["family"]), int(g["stepper"])
+    if stp == 0:
+        return abi.STEPPER_EULER if fam == 0 else abi.STEPPER_EULER_PTR
+    return abi.STEPPER_SRK if stp == 1 else abi.STEPPER_RK4
+
+
+def golden_params(g):
+    return {k: float(g[k]) for k in ("v0", "sigma", "rho", "alpha", "D_phi")}
+
+
+@pytest.mark.parametrize("ctr,key,expect", PHILOX_KAT)
+def test_device_philox_known_answers(ctr, key, expect):
+    assert abi.philox4x32_10(ctr, key) == expect
+
+
+@pytest.mark.parametrize("name", golden_cases())
+def test_trajectory_matches_reference_golden(name):
+    g = load_golden(name)
+    n, L = int(g["n"]), float(g["L"])
+    model = abi.MODEL_VORTEX if "omega" in g else abi.MODEL_CHIMERA
+    with gpu(n, L, golden_params(g), golden_stepper(g), model=model) as s:
+        s.upload_state(g["state0"])
+        if "omega" in g:
+            s.upload_omega(g["omega"])
+        if s.noise_per_particle:
+            s.inject_noise(g["noise"])
+        every, nsteps = int(g["record_every"]), int(g["nsteps"])
+        frames, done = [], 0
+        while done < nsteps:
+            k = min(every - done % every, nsteps - done)
+            s.step(float(g["dt"]), k)
+            done += k
+            frames.append(s.download_state())
+    for got, ref in zip(frames, g["trajectory"]):
+        assert np.abs(periodic_diff(got, ref, L)).max() <= TRAJ_TOL
+
+
+def _phase_rate_ok(got, ref, scale, v0):
+    got, ref = got.reshape(-1, 3), ref.reshape(-1, 3)
+    assert np.all(np.abs(got[:, :2] - ref[:, :2]) <= RHS_TOL * abs(v0) + 1e-300)
+    tol = RHS_TOL * np.maximum(np.abs(ref[:, 2]), scale)
+    bad = np.abs(got[:, 2] - ref[:, 2]) > tol
+    assert not bad.any(), (np.flatnonzero(bad)[:5], got[bad][:3], ref[bad][:3])
+
+
+@pytest.mark.parametrize("name", golden_cases())
+def test_rhs_matches_reference_golden(name):
+    g = load_golden(name)
+    n, L = int(g["n"]), float(g["L"])
+    prm = golden_params(g)
+    o = po.OracleSystem(n, L, **prm)
+    with gpu(n, L, prm, abi.STEPPER_RK4) as s:
+        s.upload_state(g["state0"])
+        kn = s.rhs_rk(g["k_prev"], float(g["k_coef"]), float(g["dt"]), g["k_next_init"])
+        stage = g["state0"] + float(g["k_coef"]) * float(g["dt"]) * g["k_prev"]
+        off, idx = o.neighbour_lists(stage)
+        scale, counts = alignment_scale(stage, off, idx, prm["sigma"], prm["alpha"])
+        _phase_rate_ok(kn, g["rhs_rk"], scale, prm["v0"])
+        iso = counts == 0
+        assert np.array_equal(kn[2::3][iso], g["k_next_init"][2::3][iso])
+        d, a = s.rhs_srk()
+    off, idx = o.neighbour_lists(g["state0"])
+    scale, counts = alignment_scale(g["state0"], off, idx, prm["sigma"], prm["alpha"])
+    _phase_rate_ok(d, g["srk_derivative"], scale, prm["v0"])
+    a_ref = g["srk_additional"].reshape(-1, 2)
+    a = a.reshape(-1, 2)
+    d_ref = g["srk_derivative"][2::3]
+    # scales: sqrt(2D) sum|cos|/n and sum |d_j - d_i||cos|/n + 2D|d_i|
+    phi = g["state0"][2::3]
+    owner = np.repeat(np.arange(n), np.diff(off))
+    c = np.abs(np.cos(phi[idx] - phi[owner] - prm["alpha"]))
+    nn = np.maximum(counts, 1)
+    s0 = np.sqrt(2 * prm["D_phi"]) * np.bincount(owner, c, n) / nn
+    s1 = np.bincount(owner, np.abs(d_ref[idx] - d_ref[owner]) * c, n) / nn + \
+        2 * prm["D_phi"] * np.abs(d_ref)
+    assert np.all(np.abs(a[:, 0] - a_ref[:, 0]) <= RHS_TOL * np.maximum(np.abs(a_ref[:, 0]), s0) + 1e-300)
+    assert np.all(np.abs(a[:, 1] - a_ref[:, 1]) <= RHS_TOL * np.maximum(np.abs(a_ref[:, 1]), s1) + 1e-300)
+
+
+def _lattice_ties(L=4.0, rho=0.25, m=12):
+    # particles on a grid of pitch rho: every nearest pair sits exactly at dr^2 == rho^2
+    xs = (np.arange(m) + 0.5) * rho
+    X, Y = np.meshgrid(xs, xs)
+    n = m * m
+    st = np.zeros(3 * n)
+    st[0::3], st[1::3] = X.ravel(), Y.ravel()
+    st[2::3] = np.linspace(-3, 3, n)
+    return n, L, st
+
+
+def _neighbour_cases():
+    yield "golden_euler", load_golden("chimera_euler_n1024")["state0"], 1024, 1.0, 0.1
+    yield "random_n4096", init_state(4096, 2.0, 11), 4096, 2.0, 0.1
+    n, L, st = _lattice_ties()
+    yield "lattice_ties", st, n, L, 0.25
+    st = init_state(512, 1.0, 12)
+    st[0], st[3], st[4] = -1e-17, 1.0 - 2.0 ** -53, 1.0  # wraps to L, just below L, exactly L
+    yield "edges", st, 512, 1.0, 0.1
+    yield "allpairs", init_state(300, 0.5, 13), 300, 0.5, 0.2
+
+
+@pytest.mark.parametrize("case", list(_neighbour_cases()), ids=lambda c: c[0])
+def test_neighbour_sets_bit_exact(case):
+    _, st, n, L, rho = case
+    prm = dict(PRM0, rho=rho)
+    o = po.OracleSystem(n, L, **prm)
+    off_ref, idx_ref = o.neighbour_lists(st)
+    for flags in (0, abi.FLAG_EXACT_ALL):
+        for precision in (abi.PRECISION_FP64, abi.PRECISION_FP32C):
+            with gpu(n, L, prm, abi.STEPPER_EULER, flags=flags, precision=precision) as s:
+                s.upload_state(st)
+                off, idx = s.neighbours()
+            assert np.array_equal(off, off_ref)
+            assert np.array_equal(idx, idx_ref)
+
+
+def _oracle_run(n, L, prm, kind, state, dt, nsteps, noise=None, omega=None):
+    o = po.OracleSystem(n, L, **prm)
+    st = state.copy()
+    o.run(kind, st, 0.0, dt, nsteps, noise, omega)
+    return st
+
+
+@pytest.mark.parametrize("stepper,n,L,prm,nsteps,dt", [
+    (abi.STEPPER_EULER, 1024, 1.0, PRM0, 100, 0.01),
+    (abi.STEPPER_EULER_PTR, 1024, 1.0, PRM0, 100, 0.01),
+    (abi.STEPPER_SRK, 2048, 2.0, dict(v0=0.02, sigma=2.0, rho=0.25, alpha=0.0, D_phi=0.01), 100, 0.005),
+    (abi.STEPPER_RK4, 4096, 4.0, dict(v0=0.01, sigma=1.0, rho=0.25, alpha=1.45, D_phi=0.0), 100, 0.01),
+    (abi.STEPPER_EULER, 256, 0.5, dict(PRM0, rho=0.15), 100, 0.01),
+])
+def test_100_step_trajectory_with_philox_noise(stepper, n, L, prm, nsteps, dt):
+    st0 = init_state(n, L, 21)
+    vortex = stepper == abi.STEPPER_SRK
+    omega = np.random.default_rng(22).normal(0, 0.5, n) if vortex else None
+    with gpu(n, L, prm, stepper, model=abi.MODEL_VORTEX if vortex else abi.MODEL_CHIMERA,
+             seed=1234) as s:
+        s.upload_state(st0)
+        if vortex:
+            s.upload_omega(omega)
+        s.step(dt, nsteps)
+        got = s.download_state()
+        noise = s.export_noise(0, nsteps) if s.noise_per_particle else None
+    kind = {abi.STEPPER_EULER: po.EULER, abi.STEPPER_EULER_PTR: po.EULER_PTR,
+            abi.STEPPER_SRK: po.SRK, abi.STEPPER_RK4: po.RK4}[stepper]
+    ref = _oracle_run(n, L, prm, kind, st0, dt, nsteps, noise, omega)
+    assert np.abs(periodic_diff(got, ref, L)).max() <= TRAJ_TOL
+
+
+def test_graph_replay_and_resume_are_bitwise():
+    n, L = 1024, 1.0
+    st0 = init_state(n, L, 31)
+    with gpu(n, L, PRM0, abi.STEPPER_EULER, seed=7) as a, \
+            gpu(n, L, PRM0, abi.STEPPER_EULER, seed=7) as b, \
+            gpu(n, L, PRM0, abi.STEPPER_EULER, seed=7) as c:
+        a.upload_state(st0)
+        b.upload_state(st0)
+        a.step(0.01, 100)
+        for _ in range(4):
+            b.step(0.01, 25, graph=True)
+        ra, rb = a.download_state(), b.download_state()
+        assert np.array_equal(ra, rb)
+        # exact resume: state + step counter
+        a2 = gpu(n, L, PRM0, abi.STEPPER_EULER, seed=7)
+        a2.upload_state(st0)
+        a2.step(0.01, 50)
+        mid = a2.download_state()
+        c.upload_state(mid)
+        c.step_counter = 50
+        c.step(0.01, 50)
+        assert np.array_equal(c.download_state(), ra)
+        a2.close()
+
+
+def test_rk4_buffers_resume_bitwise():
+    n, L = 1024, 4.0
+    prm = dict(v0=0.01, sigma=1.0, rho=0.25, alpha=1.45, D_phi=0.0)
+    st0 = init_state(n, L, 32)
+    with gpu(n, L, prm, abi.STEPPER_RK4) as a, gpu(n, L, prm, abi.STEPPER_RK4) as b:
+        a.upload_state(st0)
+        a.step(0.01, 10)
+        b.upload_state(a.download_state())
+        b.upload_rk4_buffers(a.download_rk4_buffers())
+        a.step(0.01, 10)
+        b.step(0.01, 10)
+        assert np.array_equal(a.download_state(), b.download_state())
+
+
+def test_injected_noise_exhaustion_is_an_error():
+    n, L = 256, 1.0
+    with gpu(n, L, PRM0, abi.STEPPER_EULER) as s:
+        st0 = init_state(n, L, 33)
+        s.upload_state(st0)
+        s.inject_noise(np.zeros(n))
+        with pytest.raises(abi.SpcError) as e:
+            s.step(0.01, 2)
+        assert e.value.code == -5
+        assert np.array_equal(s.download_state(), st0)
+
+
+def test_order_parameters_match_oracle():
+    n, L = 2048, 2.0
+    st = init_state(n, L, 34)
+    st[2::3] = 0.3 * st[2::3]
+    o = po.OracleSystem(n, L, **PRM0)
+    ref = o.order_params(st)
+    with gpu(n, L, PRM0, abi.STEPPER_EULER) as s:
+        s.upload_state(st)
+        got = s.order_params()
+    for k in ("R", "psi", "R_local"):
+        assert abs(got[k] - ref[k]) <= 1e-12
+
+
+def test_fp32c_rhs_error_is_small():
+    g = load_golden("chimera_euler_n1024")
+    n, L = int(g["n"]), float(g["L"])
+    prm = golden_params(g)
+    o = po.OracleSystem(n, L, **prm)
+    off, idx = o.neighbour_lists(g["state0"])
+    scale, counts = alignment_scale(g["state0"], off, idx, prm["sigma"], prm["alpha"])
+    with gpu(n, L, prm, abi.STEPPER_SRK, precision=abi.PRECISION_FP32C) as s:
+        s.upload_state(g["state0"])
+        d, _ = s.rhs_srk()
+    err = np.abs(d[2::3] - g["srk_derivative"][2::3])
+    assert np.all(err <= 2e-6 * np.maximum(scale, 1e-3))
