@@ -124,7 +124,7 @@ __global__ void k_cell_bounds(const uint32_t *__restrict__ skeys, int n, int nce
   const int p = blockIdx.x * blockDim.x + threadIdx.x;
   if (p > n) return;
   const int lo = (p == 0) ? -1 : (int)skeys[p - 1];
-  const int hi = (p == n) ? ncell : (int)skeys[p];
+  const int hi = (p == n) ? ncell : min((int)skeys[p], ncell);
   for (int c = lo + 1; c <= hi; ++c) cell_start[c] = p;
 }
 
