@@ -215,7 +215,23 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--ncu-case", choices=["fp32c", "fp64"], default=None,
+                    help="run a few plain (ungraphed) steps of the workload for an ncu capture")
     args = ap.parse_args()
+    if args.ncu_case:
+        from spc2_langevin_integration_gb300 import abi
+        w = WORKLOAD
+        st, omega = init_inputs(w)
+        prec = abi.PRECISION_FP32C if args.ncu_case == "fp32c" else abi.PRECISION_FP64
+        p = abi.make_params(L=w["L"], v0=w["v0"], sigma=w["sigma"], rho=w["rho"],
+                            alpha=w["alpha"], D_phi=w["D_phi"], model=abi.MODEL_VORTEX,
+                            stepper=abi.STEPPER_SRK, precision=prec, seed=w["seed"])
+        with abi.System(w["n"], p) as s:
+            s.upload_state(st)
+            s.upload_omega(omega)
+            s.step(w["dt"], 3)
+            s.synchronize()
+        return
     w = WORKLOAD
     world, rank, local, dist = dist_setup(args)
     n_total = w["n"] * world
