@@ -180,6 +180,25 @@ void *spc_stream(spc_handle *h);
  * draw), for checking against the published known-answer vectors. */
 int spc_philox4x32_10(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]);
 
+/* SRK-form right-hand side (as spc_rhs_srk) computed without allocating
+ * any device memory.  No counterpart in the reference: it exists for callers
+ * that must not call cudaMalloc, such as code whose device memory is owned by
+ * another component's pool, latency-critical loops where an allocation would
+ * synchronise the device, or processes that fix their device footprint at
+ * start-up.  The caller passes device buffers: d_state (3N doubles, AoS),
+ * d_derivative (3N) and d_additional (2N); the work is enqueued on `stream`
+ * (a cudaStream_t, NULL for the default stream) and the call returns without
+ * waiting.  Intermediates live in one static device array of about 1.1 MB
+ * that every GPU loading the library keeps until the process exits; limits:
+ * n <= 8192 particles and int(L/rho)^2 <= 16384 cells, larger sizes return
+ * SPC_ERR_CAPACITY.  The first call on a device looks up that array's device
+ * address (once per device, with the device current), so make it before any
+ * stream capture.  All calls share the one array: calls whose work overlaps
+ * on the GPU (different streams, or different host threads) race and must be
+ * ordered by the caller. */
+int spc_rhs_srk_noalloc(const spc_params *p, int32_t n, const double *d_state,
+                        double *d_derivative, double *d_additional, void *stream);
+
 /* Page-locked host buffers for callers that stream state in and out. */
 int spc_alloc_pinned(size_t bytes, void **out);
 int spc_free_pinned(void *p);

@@ -796,3 +796,158 @@ int spc_free_pinned(void *p) {
 }
 
 }  // extern "C"
+
+// ===========================================================================
+// Allocation-free SRK right-hand side.
+//
+// Some callers cannot call cudaMalloc at the point where they need a
+// right-hand side: code that runs while another component owns every byte of
+// device memory through its own pool, latency-critical loops where a
+// cudaMalloc/cudaFree pair would synchronise the device, and hosts that must
+// not grow their device footprint after start-up.  spc_rhs_srk_noalloc serves
+// them: the caller passes device input and output buffers, and every
+// intermediate array (cell keys, the radix sort's buffers and histograms, the
+// cell table, the cell-order copies) lives in one file-scope __device__ array
+// of fixed size, resident on every GPU that loads this library until the
+// process exits.
+namespace {
+
+constexpr int kNoAllocMaxN = 8192;       // particles per call
+constexpr int kNoAllocMaxCells = 16384;  // cells (nc * nc) per call
+constexpr int kNoAllocMaxTiles = (kNoAllocMaxN + kSortTile - 1) / kSortTile;
+
+constexpr size_t na_round(size_t b) { return (b + 255) / 256 * 256; }
+constexpr size_t kNaD = na_round(8ull * kNoAllocMaxN);   // one double per particle
+constexpr size_t kNaF = na_round(4ull * kNoAllocMaxN);   // one 32-bit value per particle
+constexpr size_t kNaF2 = na_round(8ull * kNoAllocMaxN);  // one float2 per particle
+constexpr size_t kNaCells = na_round(4ull * (kNoAllocMaxCells + 1));
+constexpr size_t kNaHist = na_round(4ull * kRadix * kNoAllocMaxTiles);
+// x y phi | st_x st_y st_phi | sx sy sphi | dphi_s  (10 double arrays)
+// keys vals keys_alt vals_alt pidx cnt_s dphi_f    (7 32-bit arrays)
+// fxy cs (2 float2 arrays) | cell_start | hist | clamped counter
+constexpr size_t kNoAllocBytes = 10 * kNaD + 7 * kNaF + 2 * kNaF2 + kNaCells + kNaHist + 256;
+
+constexpr int kNoAllocMaxDevices = 64;
+std::mutex g_noalloc_mu;
+char *g_noalloc_base[kNoAllocMaxDevices] = {};
+
+}  // namespace
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];
+
+namespace {
+
+// Device address of g_noalloc_scratch on the current device.  In host code
+// the symbol name is only a stand-in, so the address is looked up once per
+// device with that device current and cached.
+int noalloc_scratch(char **out) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return fail(nullptr, SPC_ERR_CUDA, "cudaGetDevice: %s", cudaGetErrorString(e));
+  if (dev < 0 || dev >= kNoAllocMaxDevices) return fail(nullptr, SPC_ERR_INVALID, "device %d out of range", dev);
+  std::lock_guard<std::mutex> lk(g_noalloc_mu);
+  if (!g_noalloc_base[dev]) {
+    void *ptr = nullptr;
+    e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
+    if (e != cudaSuccess || !ptr)
+      return fail(nullptr, SPC_ERR_CUDA, "cudaGetSymbolAddress(scratch): %s", cudaGetErrorString(e));
+    g_noalloc_base[dev] = (char *)ptr;
+  }
+  *out = g_noalloc_base[dev];
+  return SPC_OK;
+}
+
+}  // namespace
+
+extern "C" int spc_rhs_srk_noalloc(const spc_params *p, int32_t n, const double *d_state,
+                                   double *d_derivative, double *d_additional, void *stream) {
+  int rc = validate(p, n, nullptr);
+  if (rc) return rc;
+  if (!d_state || !d_derivative || !d_additional)
+    return fail(nullptr, SPC_ERR_INVALID, "NULL device buffer");
+  if (n > kNoAllocMaxN)
+    return fail(nullptr, SPC_ERR_CAPACITY, "spc_rhs_srk_noalloc: n = %d exceeds its maximum of %d particles",
+                n, kNoAllocMaxN);
+  const bool allpairs = !(p->rho <= 0.25 * p->L);
+  const int nc = allpairs ? 1 : std::max(1, (int)(p->L / p->rho));
+  if ((long long)nc * nc > kNoAllocMaxCells)
+    return fail(nullptr, SPC_ERR_CAPACITY, "spc_rhs_srk_noalloc: %d x %d cells exceed its maximum of %d cells",
+                nc, nc, kNoAllocMaxCells);
+  char *base = nullptr;
+  rc = noalloc_scratch(&base);
+  if (rc) return rc;
+
+  spc_handle h;  // a view: every pointer below is inside the static scratch
+  h.p = *p;
+  h.n = n;
+  h.stream = (cudaStream_t)stream;
+  SysConst &sc = h.sc;
+  sc.n = n;
+  sc.L = p->L;
+  sc.rL = 1.0 / p->L;
+  sc.rho2 = p->rho * p->rho;
+  sc.v0 = p->v0;
+  sc.sigma = p->sigma;
+  sc.alpha = p->alpha;
+  sc.D = p->D_phi;
+  sc.allpairs = allpairs;
+  sc.nc = nc;
+  sc.ncell = nc * nc;
+  sc.cell = p->L / nc;
+  sc.cell_f = (float)sc.cell;
+  sc.lo2 = (float)(sc.rho2 * (1.0 - 3e-5));
+  sc.hi2 = (float)(sc.rho2 * (1.0 + 3e-5));
+  sc.exact_all = (p->flags & SPC_FLAG_EXACT_ALL) ? 1 : 0;
+
+  KArgs &a = h.a;
+  a.sc = sc;
+  char *cur = base;
+  auto take = [&](size_t bytes) {
+    char *r = cur;
+    cur += bytes;
+    return (void *)r;
+  };
+  a.x = (double *)take(kNaD);
+  a.y = (double *)take(kNaD);
+  a.phi = (double *)take(kNaD);
+  a.st_x = (double *)take(kNaD);
+  a.st_y = (double *)take(kNaD);
+  a.st_phi = (double *)take(kNaD);
+  a.sx = (double *)take(kNaD);
+  a.sy = (double *)take(kNaD);
+  a.sphi = (double *)take(kNaD);
+  a.dphi_s = (double *)take(kNaD);
+  a.keys = (uint32_t *)take(kNaF);
+  a.vals = (uint32_t *)take(kNaF);
+  h.keys_alt = (uint32_t *)take(kNaF);
+  h.vals_alt = (uint32_t *)take(kNaF);
+  a.pidx = (int *)take(kNaF);
+  a.cnt_s = (int *)take(kNaF);
+  a.dphi_f = (float *)take(kNaF);
+  a.fxy = (float2 *)take(kNaF2);
+  a.cs = (float2 *)take(kNaF2);
+  a.cell_start = (int *)take(kNaCells);
+  h.hist = (uint32_t *)take(kNaHist);
+  unsigned long long *clamped = (unsigned long long *)take(256);
+  a.clamped = clamped;
+  a.omega = nullptr;
+  a.out_d = d_derivative;
+  a.out_a = d_additional;
+  h.ntiles = (n + kSortTile - 1) / kSortTile;
+  int bits = 1;
+  while (bits < 31 && (1u << bits) < (unsigned)sc.ncell) ++bits;
+  h.sort_passes = (bits + kRadixBits - 1) / kRadixBits;
+
+  // the scratch keeps the previous call's contents: the clamp counter is the
+  // only array the kernels accumulate into, so it is cleared here
+  cudaError_t e = cudaMemsetAsync(clamped, 0, 8, h.stream);
+  if (e != cudaSuccess) return fail(nullptr, SPC_ERR_CUDA, "clear scratch: %s", cudaGetErrorString(e));
+  k_aos_to_soa<<<blocks_for(n, 256), 256, 0, h.stream>>>(d_state, n, a.x, a.y, a.phi);
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return fail(nullptr, SPC_ERR_CUDA, "launch: %s", cudaGetErrorString(e));
+  KArgs run = a;
+  rc = eval_stage(&h, run, 0, -1, 0.0);
+  if (rc == SPC_OK) rc = launch_pass(&h, run, kKindSin, kEpiSrk1);
+  if (rc == SPC_OK) rc = launch_pass(&h, run, kKindCos2, kEpiSrk2Out);
+  return rc;
+}
