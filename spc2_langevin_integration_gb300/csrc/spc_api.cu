@@ -16,6 +16,7 @@
 #include "../../include/spc_gb300.h"
 #include "spc_kernels.cuh"
 #include "spc_sort.cuh"
+#include "spc_tile.cuh"
 
 using namespace spc;
 
@@ -38,7 +39,7 @@ struct spc_handle {
   KArgs a{};
   // sort scratch
   uint32_t *keys_alt = nullptr, *vals_alt = nullptr, *hist = nullptr;
-  int ntiles = 0, sort_passes = 0;
+  int ntiles = 0, sort_passes = 0, radix_bits = 8;
   const uint32_t *sorted_keys = nullptr, *sorted_vals = nullptr;
   double *aos = nullptr;       // AoS staging, 3N (4 x 3N for RK4 buffers)
   double *order_part = nullptr;
@@ -93,6 +94,12 @@ int dalloc(spc_handle *h, T **ptr, size_t count) {
   return SPC_OK;
 }
 
+// A positive finite power of two (then x / L equals x * (1 / L) exactly).
+inline int is_pow2(double L) {
+  int e = 0;
+  return std::frexp(L, &e) == 0.5 ? 1 : 0;
+}
+
 inline int blocks_for(long long n, int threads) { return (int)((n + threads - 1) / threads); }
 
 int noise_m(const spc_params &p) {
@@ -101,6 +108,14 @@ int noise_m(const spc_params &p) {
     case SPC_STEPPER_RK4: return 0;
     default: return 1;
   }
+}
+
+// The 11-bit scatter needs more than the default 48 KB of dynamic shared
+// memory; the attribute is set with the device current (not a stream
+// operation, so never inside a capture).
+cudaError_t set_kernel_attributes() {
+  return cudaFuncSetAttribute(k_radix_scatter, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              (int)scatter_smem_bytes(11));
 }
 
 int set_device(spc_handle *h) {
@@ -117,7 +132,9 @@ void mark(spc_handle *h, int slot) {
 int eval_stage(spc_handle *h, KArgs &a, int rk_form, int kq, double kcdt) {
   const int n = h->n;
   cudaStream_t st = h->stream;
-  k_stage<<<blocks_for(n, 256), 256, 0, st>>>(a, rk_form, kq, kcdt);
+  const int bits = h->radix_bits;
+  k_stage<<<blocks_for(n, kStageThreads), kStageThreads, 0, st>>>(a, rk_form, kq, kcdt,
+                                                                   h->sc.allpairs ? 0 : bits, h->hist);
   SPC_LAUNCHED(h);
   mark(h, 1);
   if (h->sc.allpairs) {
@@ -131,13 +148,11 @@ int eval_stage(spc_handle *h, KArgs &a, int rk_form, int kq, double kcdt) {
   }
   uint32_t *kin = a.keys, *vin = a.vals, *kout = h->keys_alt, *vout = h->vals_alt;
   for (int pass = 0; pass < h->sort_passes; ++pass) {
-    const int shift = pass * kRadixBits;
-    k_radix_hist<<<h->ntiles, kSortThreads, 0, st>>>(kin, n, shift, h->ntiles, h->hist);
-    SPC_LAUNCHED(h);
-    k_scan_exclusive<<<1, kScanThreads, 0, st>>>(h->hist, kRadix * h->ntiles);
-    SPC_LAUNCHED(h);
-    k_radix_scatter<<<h->ntiles, kSortThreads, 0, st>>>(kin, vin, kout, vout, n, shift,
-                                                          h->ntiles, h->hist);
+    const int shift = pass * bits;
+    if (pass > 0) k_radix_hist<<<h->ntiles, kSortThreads, 0, st>>>(kin, n, shift, bits, h->hist);
+    k_scan_digits<<<1, kScanThreads, 0, st>>>(h->hist, h->ntiles, bits);
+    k_radix_scatter<<<h->ntiles, kSortThreads, scatter_smem_bytes(bits), st>>>(kin, vin, kout, vout, n,
+                                                                               shift, bits, h->hist);
     SPC_LAUNCHED(h);
     std::swap(kin, kout);
     std::swap(vin, vout);
@@ -145,12 +160,10 @@ int eval_stage(spc_handle *h, KArgs &a, int rk_form, int kq, double kcdt) {
   mark(h, 2);
   a.skeys = kin;
   a.svals = vin;
-  k_cell_bounds<<<blocks_for(n + 1, 256), 256, 0, st>>>(kin, n, h->sc.ncell, a.cell_start);
-  SPC_LAUNCHED(h);
   if (h->p.precision == SPC_PRECISION_FP32C)
-    k_gather<kPrecFP32C><<<blocks_for(n, 256), 256, 0, st>>>(a);
+    k_gather<kPrecFP32C><<<blocks_for(n + 1, 256), 256, 0, st>>>(a);
   else
-    k_gather<kPrecFP64><<<blocks_for(n, 256), 256, 0, st>>>(a);
+    k_gather<kPrecFP64><<<blocks_for(n + 1, 256), 256, 0, st>>>(a);
   SPC_LAUNCHED(h);
   mark(h, 3);
   return SPC_OK;
@@ -161,9 +174,13 @@ int launch_pass_t(spc_handle *h, const KArgs &a, int epi) {
   cudaStream_t st = h->stream;
   if (h->sc.allpairs) {
     k_allpairs_pass<PREC, KIND><<<blocks_for(h->n, kAllPairsThreads), kAllPairsThreads, 0, st>>>(a, epi);
-  } else {
+  } else if constexpr (KIND == kKindNb) {
     const int blocks = std::min(blocks_for(h->sc.ncell, kPassWarps), 152 * 64);
     k_cell_pass<PREC, KIND><<<blocks, kPassThreads, 0, st>>>(a, epi);
+  } else if constexpr (PREC == kPrecFP32C) {
+    k_tile_fp32c<KIND><<<std::min(h->sc.ncell, 152 * 256), kTileThreads32, 0, st>>>(a, epi);
+  } else {
+    k_tile_fp64<KIND><<<std::min(h->sc.ncell, 152 * 256), kTileThreads64, 0, st>>>(a, epi);
   }
   SPC_LAUNCHED(h);
   return SPC_OK;
@@ -309,6 +326,10 @@ int spc_create(const spc_params *p, int32_t n, spc_handle **out) {
     h->err = "no CUDA device";
     return bail(SPC_ERR_CUDA);
   }
+  if (set_kernel_attributes() != cudaSuccess) {
+    h->err = "cudaFuncSetAttribute failed";
+    return bail(SPC_ERR_CUDA);
+  }
   if (cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess) {
     h->err = "cudaStreamCreate failed";
     return bail(SPC_ERR_CUDA);
@@ -332,6 +353,7 @@ int spc_create(const spc_params *p, int32_t n, spc_handle **out) {
   sc.lo2 = (float)(sc.rho2 * (1.0 - 3e-5));
   sc.hi2 = (float)(sc.rho2 * (1.0 + 3e-5));
   sc.exact_all = (p->flags & SPC_FLAG_EXACT_ALL) ? 1 : 0;
+  sc.L_pow2 = is_pow2(p->L);
 
   KArgs &a = h->a;
   a.sc = sc;
@@ -359,10 +381,12 @@ int spc_create(const spc_params *p, int32_t n, spc_handle **out) {
   ALLOC(h->keys_alt, N);
   ALLOC(h->vals_alt, N);
   h->ntiles = (int)((N + kSortTile - 1) / kSortTile);
-  ALLOC(h->hist, (size_t)kRadix * h->ntiles);
   int bits = 1;
   while (bits < 31 && (1u << bits) < (unsigned)sc.ncell) ++bits;
-  h->sort_passes = (bits + kRadixBits - 1) / kRadixBits;
+  // one pass of exactly the key width when it is at most 11 bits, else 8-bit passes
+  h->radix_bits = (bits <= 11) ? bits : 8;
+  h->sort_passes = (bits + h->radix_bits - 1) / h->radix_bits;
+  ALLOC(h->hist, (size_t)(1 << h->radix_bits) * h->ntiles);
   ALLOC(a.cell_start, (size_t)sc.ncell + 1);
   ALLOC(a.sx, N);
   ALLOC(a.sy, N);
@@ -373,6 +397,7 @@ int spc_create(const spc_params *p, int32_t n, spc_handle **out) {
   ALLOC(a.dphi_s, N);
   ALLOC(a.dphi_f, N);
   ALLOC(a.cnt_s, N);
+  if (p->precision == SPC_PRECISION_FP32C && !sc.allpairs) ALLOC(a.nbmask, (size_t)kMaskWords * N);
   ALLOC(h->aos, 12 * N);
   h->order_blocks = std::min(blocks_for(n, 256), 1024);
   ALLOC(h->order_part, 2 * (size_t)h->order_blocks);
@@ -380,6 +405,8 @@ int spc_create(const spc_params *p, int32_t n, spc_handle **out) {
   ALLOC(h->d_clamped, 1);
 #undef ALLOC
   a.clamped = h->d_clamped;
+  a.hist = h->hist;
+  a.hist_len = (1 << h->radix_bits) * h->ntiles;
   a.step_base = h->d_step;
   a.seed = p->seed;
   a.system_id = p->system_id;
@@ -393,7 +420,8 @@ int spc_create(const spc_params *p, int32_t n, spc_handle **out) {
         cudaMemsetAsync(a.kphi[q], 0, N * 8, st))
       return bail(SPC_ERR_CUDA);
   }
-  if (cudaMemsetAsync(h->d_step, 0, 8, st) || cudaMemsetAsync(h->d_clamped, 0, 8, st) ||
+  if (cudaMemsetAsync(h->hist, 0, (size_t)a.hist_len * 4, st) ||
+      cudaMemsetAsync(h->d_step, 0, 8, st) || cudaMemsetAsync(h->d_clamped, 0, 8, st) ||
       cudaMemsetAsync(a.x, 0, N * 8, st) || cudaMemsetAsync(a.y, 0, N * 8, st) ||
       cudaMemsetAsync(a.phi, 0, N * 8, st))
     return bail(SPC_ERR_CUDA);
@@ -821,7 +849,7 @@ constexpr size_t kNaD = na_round(8ull * kNoAllocMaxN);   // one double per parti
 constexpr size_t kNaF = na_round(4ull * kNoAllocMaxN);   // one 32-bit value per particle
 constexpr size_t kNaF2 = na_round(8ull * kNoAllocMaxN);  // one float2 per particle
 constexpr size_t kNaCells = na_round(4ull * (kNoAllocMaxCells + 1));
-constexpr size_t kNaHist = na_round(4ull * kRadix * kNoAllocMaxTiles);
+constexpr size_t kNaHist = na_round(4ull * (1u << 11) * kNoAllocMaxTiles);
 // x y phi | st_x st_y st_phi | sx sy sphi | dphi_s  (10 double arrays)
 // keys vals keys_alt vals_alt pidx cnt_s dphi_f    (7 32-bit arrays)
 // fxy cs (2 float2 arrays) | cell_start | hist | clamped counter
@@ -898,6 +926,7 @@ extern "C" int spc_rhs_srk_noalloc(const spc_params *p, int32_t n, const double 
   sc.lo2 = (float)(sc.rho2 * (1.0 - 3e-5));
   sc.hi2 = (float)(sc.rho2 * (1.0 + 3e-5));
   sc.exact_all = (p->flags & SPC_FLAG_EXACT_ALL) ? 1 : 0;
+  sc.L_pow2 = is_pow2(p->L);
 
   KArgs &a = h.a;
   a.sc = sc;
@@ -936,11 +965,17 @@ extern "C" int spc_rhs_srk_noalloc(const spc_params *p, int32_t n, const double 
   h.ntiles = (n + kSortTile - 1) / kSortTile;
   int bits = 1;
   while (bits < 31 && (1u << bits) < (unsigned)sc.ncell) ++bits;
-  h.sort_passes = (bits + kRadixBits - 1) / kRadixBits;
+  h.radix_bits = (bits <= 11) ? bits : 8;
+  h.sort_passes = (bits + h.radix_bits - 1) / h.radix_bits;
+  a.hist = h.hist;
+  a.hist_len = (1 << h.radix_bits) * h.ntiles;
 
-  // the scratch keeps the previous call's contents: the clamp counter is the
-  // only array the kernels accumulate into, so it is cleared here
-  cudaError_t e = cudaMemsetAsync(clamped, 0, 8, h.stream);
+  cudaError_t e = set_kernel_attributes();
+  if (e != cudaSuccess) return fail(nullptr, SPC_ERR_CUDA, "kernel attributes: %s", cudaGetErrorString(e));
+  // the scratch keeps the previous call's contents: the clamp counter and the
+  // radix histogram table are accumulated into, so they are cleared here
+  e = cudaMemsetAsync(clamped, 0, 8, h.stream);
+  if (e == cudaSuccess) e = cudaMemsetAsync(h.hist, 0, (size_t)a.hist_len * 4, h.stream);
   if (e != cudaSuccess) return fail(nullptr, SPC_ERR_CUDA, "clear scratch: %s", cudaGetErrorString(e));
   k_aos_to_soa<<<blocks_for(n, 256), 256, 0, h.stream>>>(d_state, n, a.x, a.y, a.phi);
   e = cudaGetLastError();

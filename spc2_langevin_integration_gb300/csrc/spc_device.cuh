@@ -32,6 +32,7 @@ struct SysConst {
   float cell_f;
   float lo2, hi2; // prefilter: float dr^2 < lo2 => inside, > hi2 => outside, else decide in FP64
   int exact_all;  // decide every candidate in FP64
+  int L_pow2;     // L is a power of two: x / L == x * (1 / L) exactly
 };
 
 // PeriodicBoundaryConditions::ClassAEffectiveParticleDistance (PeriodicBoundaryConditions.cpp:22-35):
@@ -70,7 +71,9 @@ __device__ __forceinline__ void wrap_if_outside(const SysConst &sc, double &x, d
 // int(x / x_size_ * num_subcells_x_) (ChimeraSystem.cpp:304-305).  An index
 // outside [0, nc) (x within an ulp of L) is clamped; *clamped is set.
 __device__ __forceinline__ int cell_coord(const SysConst &sc, double x, int &clamped) {
-  int c = __double2int_rz(dmul(ddiv(x, sc.L), (double)sc.nc));
+  // for a power-of-two L the scaling by 1/L is exact, so it equals the division
+  const double q = sc.L_pow2 ? dmul(x, sc.rL) : ddiv(x, sc.L);
+  int c = __double2int_rz(dmul(q, (double)sc.nc));
   if (c < 0) {
     c = 0;
     clamped = 1;
@@ -119,6 +122,22 @@ __device__ __forceinline__ void philox_normal2(uint64_t seed, uint32_t system_id
   const double r = sqrt(-2.0 * log(u1));
   double s, c;
   sincospi(2.0 * u2, &s, &c);
+  z0 = r * c;
+  z1 = r * s;
+}
+
+// Float form of the same draw for the FP32-compensated path: the same Philox
+// words, 24-bit uniforms and single-precision Box-Muller (the double version's
+// log/sqrt/sincospi run on GB300's 1/64-rate FP64 pipe).
+__device__ __forceinline__ void philox_normal2_f(uint64_t seed, uint32_t system_id, uint64_t step,
+                                                 uint32_t i, float &z0, float &z1) {
+  const U4 o = philox4x32_10(U4{i, system_id, (uint32_t)step, (uint32_t)(step >> 32)},
+                             (uint32_t)seed, (uint32_t)(seed >> 32));
+  const float u1 = (float)((o.x >> 8) + 1u) * 0x1.0p-24f;
+  const float u2 = (float)(o.z >> 8) * 0x1.0p-24f;
+  const float r = sqrtf(-2.0f * logf(u1));
+  float s, c;
+  sincospif(2.0f * u2, &s, &c);
   z0 = r * c;
   z1 = r * s;
 }

@@ -14,6 +14,7 @@
 #pragma once
 
 #include "spc_device.cuh"
+#include "spc_sort.cuh"
 
 namespace spc {
 
@@ -71,6 +72,9 @@ struct KArgs {
   int step_off;                      // this step = *step_base + step_off
   int is_vortex;
   unsigned long long *clamped;
+  uint32_t *hist;                    // radix histogram table (zeroed by k_gather)
+  int hist_len;
+  uint32_t *nbmask;                  // FP32C: pass-1 neighbour bitmasks [word][n], or null
 };
 
 // ---------------------------------------------------------------------------
@@ -78,37 +82,60 @@ struct KArgs {
 // wrap and cell key (:295-308).  kq < 0 means k_prev is all zeros (the Euler
 // stepper's zero-filled buffer, StochasticEulerStepper.hpp:34); rk_form = 0 is
 // the SRK form, whose stage state is the state itself (:456-458).
-__global__ void k_stage(KArgs a, int rk_form, int kq, double kcdt) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+// With hist_bits > 0 the kernel also counts the first radix digit per sort
+// tile into hist (tile-major [tile][digit], zero on entry): a block-local
+// shared histogram, then one global atomic per non-empty bin.
+constexpr int kStageThreads = 256;
+constexpr int kMaxHistBits = 11;
+
+__global__ void __launch_bounds__(kStageThreads)
+    k_stage(KArgs a, int rk_form, int kq, double kcdt, int hist_bits, uint32_t *hist) {
+  __shared__ uint32_t h[1 << kMaxHistBits];
   const SysConst &sc = a.sc;
-  if (i >= sc.n) return;
-  double x = a.x[i], y = a.y[i], ph = a.phi[i];
-  if (rk_form) {
-    const double kx = kq >= 0 ? a.kx[kq][i] : 0.0;
-    const double ky = kq >= 0 ? a.ky[kq][i] : 0.0;
-    const double kp = kq >= 0 ? a.kphi[kq][i] : 0.0;
-    x = dadd(x, dmul(kcdt, kx));
-    y = dadd(y, dmul(kcdt, ky));
-    ph = dadd(ph, dmul(kcdt, kp));
+  const int R = 1 << hist_bits;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (hist_bits > 0) {
+    for (int d = threadIdx.x; d < R; d += blockDim.x) h[d] = 0;
+    __syncthreads();
   }
-  if (sc.allpairs) {
-    // all pairs use the unwrapped stage positions (ChimeraSystem.cpp:135-153)
-    a.sx[i] = x;
-    a.sy[i] = y;
-    a.sphi[i] = ph;
-    a.pidx[i] = i;
-    return;
+  if (i < sc.n) {
+    double x = a.x[i], y = a.y[i], ph = a.phi[i];
+    if (rk_form) {
+      const double kx = kq >= 0 ? a.kx[kq][i] : 0.0;
+      const double ky = kq >= 0 ? a.ky[kq][i] : 0.0;
+      const double kp = kq >= 0 ? a.kphi[kq][i] : 0.0;
+      x = dadd(x, dmul(kcdt, kx));
+      y = dadd(y, dmul(kcdt, ky));
+      ph = dadd(ph, dmul(kcdt, kp));
+    }
+    if (sc.allpairs) {
+      // all pairs use the unwrapped stage positions (ChimeraSystem.cpp:135-153)
+      a.sx[i] = x;
+      a.sy[i] = y;
+      a.sphi[i] = ph;
+      a.pidx[i] = i;
+    } else {
+      wrap_if_outside(sc, x, y);
+      int clamped = 0;
+      const int cx = cell_coord(sc, x, clamped);
+      const int cy = cell_coord(sc, y, clamped);
+      if (clamped) atomicAdd(a.clamped, 1ull);
+      a.st_x[i] = x;
+      a.st_y[i] = y;
+      a.st_phi[i] = ph;
+      const uint32_t key = (uint32_t)(cy * sc.nc + cx);
+      a.keys[i] = key;
+      a.vals[i] = (uint32_t)i;
+      if (hist_bits > 0) atomicAdd(&h[key & (R - 1)], 1u);
+    }
   }
-  wrap_if_outside(sc, x, y);
-  int clamped = 0;
-  const int cx = cell_coord(sc, x, clamped);
-  const int cy = cell_coord(sc, y, clamped);
-  if (clamped) atomicAdd(a.clamped, 1ull);
-  a.st_x[i] = x;
-  a.st_y[i] = y;
-  a.st_phi[i] = ph;
-  a.keys[i] = (uint32_t)(cy * sc.nc + cx);
-  a.vals[i] = (uint32_t)i;
+  if (hist_bits > 0) {
+    __syncthreads();
+    // a block of 256 lies inside one sort tile of 2048
+    uint32_t *row = hist + (size_t)(blockIdx.x * blockDim.x / kSortTile) * R;
+    for (int d = threadIdx.x; d < R; d += blockDim.x)
+      if (h[d]) atomicAdd(&row[d], h[d]);
+  }
 }
 
 // Phase reduced to about [-pi, pi] in double, then float (FP32C trig input).
@@ -122,7 +149,12 @@ template <int PREC>
 __global__ void k_gather(KArgs a) {
   const int p = blockIdx.x * blockDim.x + threadIdx.x;
   const SysConst &sc = a.sc;
-  if (p >= sc.n) return;
+  if (p > sc.n) return;
+  // the cell start table of the sorted keys (one thread per slot and one past the end)
+  cell_bounds_at(a.skeys, sc.n, sc.ncell, a.cell_start, p);
+  // leave the first-digit histogram table zero for the next stage kernel
+  for (int k = p; k < a.hist_len; k += sc.n + 1) a.hist[k] = 0u;
+  if (p == sc.n) return;
   const int i = (int)a.svals[p];
   const int key = (int)a.skeys[p];
   const int cx = key % sc.nc, cy = key / sc.nc;
@@ -243,11 +275,12 @@ __device__ void epilogue(const KArgs &a, int epi, const ILane &il, Acc<PREC> &ac
     return;
   }
   double z0 = 0.0, z1 = 0.0;
-  if ((epi == kEpiEuler || epi == kEpiEulerPtr || epi == kEpiSrk2) && !a.noise)
-    philox_normal2(a.seed, a.system_id, *a.step_base + (unsigned long long)a.step_off, (uint32_t)i,
-                   z0, z1);
+  const bool draws = (epi == kEpiEuler || epi == kEpiEulerPtr || epi == kEpiSrk2) && !a.noise;
   const double dt = a.dt;
   if constexpr (PREC == kPrecFP64) {
+    if (draws)
+      philox_normal2(a.seed, a.system_id, *a.step_base + (unsigned long long)a.step_off,
+                     (uint32_t)i, z0, z1);
     const double cph = cos(il.phi), sph = sin(il.phi);
     const double d0 = dmul(sc.v0, cph), d1 = dmul(sc.v0, sph);  // v_0_ * cos(phi_i) (:419-420)
     if constexpr (KIND == kKindSin) {
@@ -327,6 +360,13 @@ __device__ void epilogue(const KArgs &a, int epi, const ILane &il, Acc<PREC> &ac
   } else {
     // FP32C: right-hand sides and increments in float, accumulated into the
     // double positions and phase.
+    if (draws) {
+      float f0, f1;
+      philox_normal2_f(a.seed, a.system_id, *a.step_base + (unsigned long long)a.step_off,
+                       (uint32_t)i, f0, f1);
+      z0 = f0;
+      z1 = f1;
+    }
     const float ph_r = reduced_phase_f(il.phi);
     float sph, cph;
     sincosf(ph_r, &sph, &cph);

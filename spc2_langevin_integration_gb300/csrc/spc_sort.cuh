@@ -7,10 +7,12 @@
 // every cell's members in ascending index order, which is the reference's
 // visiting order inside a cell.
 //
-// Per 8-bit digit pass: (1) per-tile digit histograms, (2) one exclusive scan
-// over the digit-major histogram table, (3) a stable scatter where each warp
-// ranks its keys with __match_any_sync in element order and warps are ordered
-// by a per-digit prefix in shared memory.
+// Digit width is 11 bits when every key fits one digit (up to 2048 cells, one
+// pass) and 8 bits otherwise.  Per pass: (1) per-tile digit histograms (the
+// first pass's histogram is fused into the stage kernel), (2) one exclusive
+// scan over the digit-major histogram table, (3) a stable scatter where each
+// warp ranks its keys with __match_any_sync in element order and warps are
+// ordered by a per-digit prefix in shared memory.
 #pragma once
 
 #include "spc_device.cuh"
@@ -21,59 +23,93 @@ constexpr int kSortThreads = 256;
 constexpr int kSortWarps = kSortThreads / kWarp;
 constexpr int kSortItems = 8;
 constexpr int kSortTile = kSortThreads * kSortItems;  // keys per tile
-constexpr int kRadixBits = 8;
-constexpr int kRadix = 1 << kRadixBits;
 constexpr int kScanThreads = 1024;
 
+// Tile-major digit histogram of keys[tile*2048 ...] for the digit at `shift`.
 __global__ void __launch_bounds__(kSortThreads)
-    k_radix_hist(const uint32_t *__restrict__ keys, int n, int shift, int ntiles,
+    k_radix_hist(const uint32_t *__restrict__ keys, int n, int shift, int bits,
                  uint32_t *__restrict__ hist) {
-  __shared__ uint32_t h[kRadix];
-  for (int d = threadIdx.x; d < kRadix; d += blockDim.x) h[d] = 0;
+  __shared__ uint32_t h[1 << 11];
+  const int R = 1 << bits;
+  for (int d = threadIdx.x; d < R; d += blockDim.x) h[d] = 0;
   __syncthreads();
   const int base = blockIdx.x * kSortTile;
   for (int k = threadIdx.x; k < kSortTile; k += blockDim.x) {
     const int idx = base + k;
-    if (idx < n) atomicAdd(&h[(keys[idx] >> shift) & (kRadix - 1)], 1u);
+    if (idx < n) atomicAdd(&h[(keys[idx] >> shift) & (R - 1)], 1u);
   }
   __syncthreads();
-  for (int d = threadIdx.x; d < kRadix; d += blockDim.x) hist[(size_t)d * ntiles + blockIdx.x] = h[d];
+  for (int d = threadIdx.x; d < R; d += blockDim.x) hist[(size_t)blockIdx.x * R + d] = h[d];
 }
 
-// Exclusive scan of data[0..m) in place, one block of kScanThreads threads.
-__global__ void __launch_bounds__(kScanThreads) k_scan_exclusive(uint32_t *__restrict__ data, int m) {
-  __shared__ uint32_t sums[kScanThreads];
-  const int t = threadIdx.x;
-  const int per = (m + kScanThreads - 1) / kScanThreads;
-  const int a = min(t * per, m), b = min(a + per, m);
-  uint32_t s = 0;
-  for (int i = a; i < b; ++i) s += data[i];
-  sums[t] = s;
+// In-place exclusive scan of the tile-major table hist[tile][digit] in
+// digit-major order (all tiles of digit 0, then of digit 1, ...), which gives
+// each (tile, digit) its first output position.  One block: each thread owns
+// digits d = t, t + 1024; it sums its digits over the tiles (independent,
+// coalesced loads), the block scans the digit totals with warp shuffles, and
+// the thread writes its digits' running prefixes back.
+__global__ void __launch_bounds__(kScanThreads)
+    k_scan_digits(uint32_t *__restrict__ hist, int ntiles, int bits) {
+  __shared__ uint32_t wsum[kScanThreads / kWarp];
+  const int R = 1 << bits;
+  const int t = threadIdx.x, lane = t % kWarp, w = t / kWarp;
+  constexpr int kPer = 2;  // up to 2048 digits
+  uint32_t tot[kPer];
+#pragma unroll
+  for (int k = 0; k < kPer; ++k) {
+    const int d = t * kPer + k;
+    uint32_t s = 0;
+    if (d < R)
+      for (int tile = 0; tile < ntiles; ++tile) s += hist[(size_t)tile * R + d];
+    tot[k] = s;
+  }
+  const uint32_t mine = tot[0] + tot[1];
+  uint32_t incl = mine;
+#pragma unroll
+  for (int off = 1; off < kWarp; off <<= 1) {
+    const uint32_t y = __shfl_up_sync(0xffffffffu, incl, off);
+    if (lane >= off) incl += y;
+  }
+  if (lane == kWarp - 1) wsum[w] = incl;
   __syncthreads();
-  for (int off = 1; off < kScanThreads; off <<= 1) {
-    const uint32_t v = t >= off ? sums[t - off] : 0u;
-    __syncthreads();
-    sums[t] += v;
-    __syncthreads();
+  if (w == 0) {
+    const uint32_t s = wsum[lane];
+    uint32_t si = s;
+#pragma unroll
+    for (int off = 1; off < kWarp; off <<= 1) {
+      const uint32_t y = __shfl_up_sync(0xffffffffu, si, off);
+      if (lane >= off) si += y;
+    }
+    wsum[lane] = si - s;
   }
-  uint32_t run = t ? sums[t - 1] : 0u;
-  for (int i = a; i < b; ++i) {
-    const uint32_t v = data[i];
-    data[i] = run;
-    run += v;
+  __syncthreads();
+  uint32_t run = wsum[w] + (incl - mine);
+#pragma unroll
+  for (int k = 0; k < kPer; ++k) {
+    const int d = t * kPer + k;
+    if (d < R)
+      for (int tile = 0; tile < ntiles; ++tile) {
+        const size_t at = (size_t)tile * R + d;
+        const uint32_t v = hist[at];
+        hist[at] = run;
+        run += v;
+      }
   }
 }
 
+// Stable scatter of one digit pass; hist_scanned is the output of k_scan_digits.
 __global__ void __launch_bounds__(kSortThreads)
     k_radix_scatter(const uint32_t *__restrict__ keys_in, const uint32_t *__restrict__ vals_in,
                     uint32_t *__restrict__ keys_out, uint32_t *__restrict__ vals_out, int n,
-                    int shift, int ntiles, const uint32_t *__restrict__ hist_scanned) {
-  __shared__ uint32_t wcount[kSortWarps][kRadix];
-  __shared__ uint32_t tile_base_of_digit[kRadix];
+                    int shift, int bits, const uint32_t *__restrict__ hist_scanned) {
+  extern __shared__ uint32_t smem_sort[];
+  const int R = 1 << bits;
+  uint32_t *wcount = smem_sort;                      // [kSortWarps][R]
+  uint32_t *tile_base_of_digit = smem_sort + kSortWarps * R;
   const int warp = threadIdx.x / kWarp, lane = threadIdx.x % kWarp;
-  for (int d = threadIdx.x; d < kSortWarps * kRadix; d += blockDim.x) (&wcount[0][0])[d] = 0;
-  for (int d = threadIdx.x; d < kRadix; d += blockDim.x)
-    tile_base_of_digit[d] = hist_scanned[(size_t)d * ntiles + blockIdx.x];
+  for (int d = threadIdx.x; d < kSortWarps * R; d += blockDim.x) smem_sort[d] = 0;
+  for (int d = threadIdx.x; d < R; d += blockDim.x)
+    tile_base_of_digit[d] = hist_scanned[(size_t)blockIdx.x * R + d];
   __syncthreads();
 
   const int base = blockIdx.x * kSortTile + warp * (kSortItems * kWarp);
@@ -86,23 +122,23 @@ __global__ void __launch_bounds__(kSortThreads)
     key[it] = valid ? keys_in[idx] : 0u;
     val[it] = valid ? vals_in[idx] : 0u;
     // invalid lanes get a digit no valid key has, so they never share a group
-    const uint32_t d = valid ? ((key[it] >> shift) & (kRadix - 1)) : (uint32_t)kRadix;
+    const uint32_t d = valid ? ((key[it] >> shift) & (R - 1)) : (uint32_t)R;
     const unsigned peers = __match_any_sync(0xffffffffu, d);
     uint32_t r = 0xffffffffu;
-    if (valid) r = wcount[warp][d] + __popc(peers & lanes_below);
+    if (valid) r = wcount[warp * R + d] + __popc(peers & lanes_below);
     __syncwarp();
-    if (valid && (31 - __clz(peers)) == lane) wcount[warp][d] += __popc(peers);
+    if (valid && (31 - __clz(peers)) == lane) wcount[warp * R + d] += __popc(peers);
     __syncwarp();
     rank[it] = r;
   }
   __syncthreads();
   // warps are consecutive runs of elements: order them per digit
-  for (int d = threadIdx.x; d < kRadix; d += blockDim.x) {
+  for (int d = threadIdx.x; d < R; d += blockDim.x) {
     uint32_t run = 0;
 #pragma unroll
     for (int w = 0; w < kSortWarps; ++w) {
-      const uint32_t c = wcount[w][d];
-      wcount[w][d] = run;
+      const uint32_t c = wcount[w * R + d];
+      wcount[w * R + d] = run;
       run += c;
     }
   }
@@ -110,19 +146,21 @@ __global__ void __launch_bounds__(kSortThreads)
 #pragma unroll
   for (int it = 0; it < kSortItems; ++it) {
     if (rank[it] == 0xffffffffu) continue;
-    const uint32_t d = (key[it] >> shift) & (kRadix - 1);
-    const uint32_t pos = tile_base_of_digit[d] + wcount[warp][d] + rank[it];
+    const uint32_t d = (key[it] >> shift) & (R - 1);
+    const uint32_t pos = tile_base_of_digit[d] + wcount[warp * R + d] + rank[it];
     keys_out[pos] = key[it];
     vals_out[pos] = val[it];
   }
 }
 
+inline size_t scatter_smem_bytes(int bits) {
+  return (size_t)(kSortWarps + 1) * (1u << bits) * sizeof(uint32_t);
+}
+
 // cell_start[c] = first sorted position with key >= c, for c in [0, ncell];
 // every entry is written exactly once.
-__global__ void k_cell_bounds(const uint32_t *__restrict__ skeys, int n, int ncell,
-                              int *__restrict__ cell_start) {
-  const int p = blockIdx.x * blockDim.x + threadIdx.x;
-  if (p > n) return;
+__device__ __forceinline__ void cell_bounds_at(const uint32_t *__restrict__ skeys, int n, int ncell,
+                                               int *__restrict__ cell_start, int p) {
   const int lo = (p == 0) ? -1 : (int)skeys[p - 1];
   const int hi = (p == n) ? ncell : min((int)skeys[p], ncell);
   for (int c = lo + 1; c <= hi; ++c) cell_start[c] = p;

@@ -1,0 +1,412 @@
+// Cell-tile neighbour passes: one CTA per cell.
+//
+// The CTA stages the candidates of the cell's 3x3 stencil (in the reference's
+// visiting order, ChimeraSystem.cpp:39-44; ascending index inside a cell) into
+// shared memory once, with each stencil cell's periodic shift already added to
+// the float prefilter coordinates, and then every thread of the CTA works on
+// one particle of the cell against that list: no global load in the inner
+// loop, and every candidate read is a shared-memory broadcast.
+//
+// FP32C (k_tile_fp32c): the candidate list is split among up to four warps per
+// 32-particle chunk to keep ~27 warps resident per SM; each part sums blocks of
+// 32 terms in float and adds each block sum with Kahan compensation; the parts
+// are combined in a fixed order, so results are deterministic.
+//
+// FP64 (k_tile_fp64): one thread per particle walks the whole list in order,
+// so each particle's sum keeps the reference's order term for term.  Accepted
+// candidates go into a per-thread FIFO in shared memory and the warp drains
+// the common minimum of its queues after every block of 32 candidates, so the
+// FP64 sin/cos (1/64-rate pipe on GB300) runs on full warps instead of on the
+// few lanes that happen to accept a given candidate.
+//
+// Both decide every pair exactly as the reference: float prefilter on
+// cell-relative coordinates, the reference's FP64 test for pairs within a
+// relative 3e-5 of rho^2 (warp-uniform branch, rare).
+#pragma once
+
+#include "spc_kernels.cuh"
+
+namespace spc {
+
+constexpr int kTileCap = 1024;      // FP32C: candidates staged per round
+constexpr int kTileCap64 = 768;     // FP64: candidates staged per round (7 CTAs/SM fit)
+constexpr int kTileThreads32 = 128; // FP32C CTA: 4 warps
+constexpr int kTileThreads64 = 64;  // FP64 CTA: 2 warps
+constexpr int kQCap = 64;           // FP64 per-thread queue (power of two)
+
+struct Stencil {
+  int start[9];    // cell-order start of each stencil cell
+  int prefix[10];  // offsets of each stencil cell in the staged list
+  float shx[9], shy[9];
+};
+
+__device__ __forceinline__ void stencil_of(const KArgs &a, int c, Stencil &s) {
+  const SysConst &sc = a.sc;
+  const int nc = sc.nc, cx = c % nc, cy = c / nc;
+  s.prefix[0] = 0;
+#pragma unroll
+  for (int q = 0; q < 9; ++q) {
+    const int ox = (q % 3) - 1, oy = (q / 3) - 1;
+    const int cj = adjust_cell(cy + oy, nc) * nc + adjust_cell(cx + ox, nc);
+    const int ja = a.cell_start[cj], jb = a.cell_start[cj + 1];
+    s.start[q] = ja;
+    s.prefix[q + 1] = s.prefix[q] + (jb - ja);
+    s.shx[q] = (float)ox * sc.cell_f;
+    s.shy[q] = (float)oy * sc.cell_f;
+  }
+}
+
+// cell-order slot of staged candidate g (0 <= g < prefix[9])
+__device__ __forceinline__ int slot_of(const Stencil &s, int g, int &q_out) {
+  int q = 0;
+#pragma unroll
+  for (int k = 1; k < 9; ++k) q += (g >= s.prefix[k]) ? 1 : 0;
+  q_out = q;
+  return s.start[q] + (g - s.prefix[q]);
+}
+
+// ---------------------------------------------------------------------------
+// FP32C passes.  Pass 1 (KIND == kKindSin) also records, for cells whose
+// candidate list fits one staging round, each particle's neighbour set as a
+// bitmask over that list (word w of particle p at nbmask[w * n + p]); pass 2
+// (kKindCos2) then walks only the set bits instead of re-testing every
+// candidate.  Cells with more candidates run the filter in pass 2 as well.
+constexpr int kMaskWords = kTileCap / 32;
+
+struct TileRed {
+  float s[4][kTileThreads32], c[4][kTileThreads32], s1[4][kTileThreads32], c1[4][kTileThreads32];
+  int n[4][kTileThreads32];
+};
+
+__device__ __forceinline__ int split_point(int rcnt, int part, int S) {
+  // part boundaries on multiples of 32 so that mask words are not shared
+  return part >= S ? rcnt : ((rcnt * part / S) & ~31);
+}
+
+// One block of 32 staged candidates against one particle (FP32C).  The block
+// is fully unrolled: bit t of *bits is candidate j0 + t.  SELF: the block may
+// contain the particle itself (staged index `self`).  Pairs the float test
+// cannot decide (within the band around rho^2) are left out here and reported
+// through *mn (the smallest |d2 - mid| seen).
+template <int KIND, bool SELF>
+__device__ __forceinline__ void block32(const float4 *__restrict__ s_c4, const float *__restrict__ s_d,
+                                        int j0, int self, float fxi, float fyi, float ca, float sa,
+                                        float di, float lo2, float mid, float &b0, float &b1,
+                                        uint32_t &bits, float &mn) {
+#pragma unroll
+  for (int t = 0; t < kWarp; ++t) {
+    const float4 cj = s_c4[j0 + t];
+    const float dx = cj.x - fxi, dy = cj.y - fyi;
+    const float d2 = fmaf(dx, dx, dy * dy);
+    bool in = d2 < lo2;
+    float off = fabsf(d2 - mid);
+    if (SELF) {
+      in = in && (j0 + t != self);
+      off = (j0 + t != self) ? off : 3.0e38f;
+    }
+    mn = fminf(mn, off);
+    if constexpr (KIND == kKindSin) {
+      const float tv = fmaf(cj.w, ca, -cj.z * sa);
+      if (in) {
+        b0 += tv;
+        bits |= 1u << t;
+      }
+    } else {
+      const float tv = fmaf(cj.z, ca, cj.w * sa);
+      if (in) {
+        b0 += tv;
+        b1 = fmaf(s_d[j0 + t] - di, tv, b1);
+        bits |= 1u << t;
+      }
+    }
+  }
+}
+
+template <int KIND>
+__global__ void __launch_bounds__(kTileThreads32) k_tile_fp32c(KArgs a, int epi) {
+  __shared__ float4 s_c4[kTileCap];   // x+shift, y+shift, cos phi, sin phi (padded to 32)
+  __shared__ float s_d[KIND == kKindCos2 ? kTileCap : 1];  // pass 2: phase rate (float)
+  __shared__ int s_p[kTileCap];       // cell-order slot (exact fallback)
+  __shared__ TileRed red;
+  __shared__ float t_s[kTileThreads32], t_c[kTileThreads32], t_s1[kTileThreads32],
+      t_c1[kTileThreads32];
+  __shared__ int t_n[kTileThreads32];
+  const SysConst &sc = a.sc;
+  const int n_all = sc.n;
+  const int tid = threadIdx.x, w = tid / kWarp, lane = tid % kWarp;
+  const float lo2 = sc.lo2, hi2 = sc.hi2;
+  const float band = 0.5f * (hi2 - lo2), mid = 0.5f * (hi2 + lo2);
+  const bool exact_all = sc.exact_all != 0;
+  for (int c = blockIdx.x; c < sc.ncell; c += gridDim.x) {
+    const int cb = a.cell_start[c], ce = a.cell_start[c + 1];
+    if (cb == ce) continue;
+    Stencil st;
+    stencil_of(a, c, st);
+    const int total = st.prefix[9];
+    const int rounds = (total + kTileCap - 1) / kTileCap;
+    const bool masked = rounds == 1 && a.nbmask != nullptr && !exact_all;
+    for (int ig = cb; ig < ce; ig += kTileThreads32) {
+      const int gi = min(kTileThreads32, ce - ig);
+      if (tid < gi) {
+        t_s[tid] = t_c[tid] = t_s1[tid] = t_c1[tid] = 0.0f;
+        t_n[tid] = 0;
+      }
+      for (int r = 0; r < rounds; ++r) {
+        const int rlo = r * kTileCap, rcnt = min(kTileCap, total - rlo);
+        const int rpad = (rcnt + kWarp - 1) & ~(kWarp - 1);
+        if (rounds > 1 || ig == cb) {
+          __syncthreads();
+          for (int k = tid; k < rpad; k += blockDim.x) {
+            if (k < rcnt) {
+              int q;
+              const int pj = slot_of(st, rlo + k, q);
+              const float2 f = a.fxy[pj];
+              const float2 cs = a.cs[pj];
+              s_c4[k] = make_float4(f.x + st.shx[q], f.y + st.shy[q], cs.x, cs.y);
+              s_p[k] = pj;
+              if constexpr (KIND == kKindCos2) s_d[k] = a.dphi_f[pj];
+            } else {  // padding: far away, never a neighbour, never near the cutoff
+              s_c4[k] = make_float4(3.0e18f, 3.0e18f, 0.0f, 0.0f);
+              s_p[k] = 0;
+              if constexpr (KIND == kKindCos2) s_d[k] = 0.0f;
+            }
+          }
+          __syncthreads();
+        }
+        // work items: (chunk of 32 particles, part of the candidate list)
+        const int chunks = (gi + kWarp - 1) / kWarp;
+        const int S = chunks >= 4 ? 1 : (chunks == 1 ? 4 : 2);
+        const int items = chunks * S;
+        for (int item = w; item < items; item += kTileThreads32 / kWarp) {
+          const int chunk = item / S, part = item % S;
+          const int li = chunk * kWarp + lane;  // particle within the group
+          const bool valid = li < gi;
+          const int p = ig + li;
+          float fxi = 3.0e30f, fyi = 3.0e30f, ca = 0.0f, sa = 0.0f, di = 0.0f;
+          double xi = 0.0, yi = 0.0;
+          if (valid) {
+            const float2 f = a.fxy[p];
+            fxi = f.x;
+            fyi = f.y;
+            float sn, cn;
+            sincosf(reduced_phase_f(a.sphi[p]) + (float)sc.alpha, &sn, &cn);
+            ca = cn;
+            sa = sn;
+            if constexpr (KIND == kKindCos2) di = a.dphi_f[p];
+            xi = a.sx[p];
+            yi = a.sy[p];
+          }
+          // staged index of i itself (the own cell is stencil entry 4); its block
+          const int self = st.prefix[4] + (p - cb) - rlo;
+          const int jlo = split_point(rpad, part, S), jhi = split_point(rpad, part + 1, S);
+          float S0 = 0.0f, C0 = 0.0f, S1 = 0.0f, C1 = 0.0f;
+          int n = 0;
+          if (KIND == kKindCos2 && masked) {
+            // pass 2 over the neighbour bitmask of pass 1 (same staged list)
+            uint32_t next = (valid && jlo < jhi) ? a.nbmask[(size_t)(jlo / kWarp) * n_all + p] : 0u;
+            for (int j0 = jlo; j0 < jhi; j0 += kWarp) {
+              const uint32_t bits = next;
+              if (j0 + kWarp < jhi)
+                next = valid ? a.nbmask[(size_t)((j0 + kWarp) / kWarp) * n_all + p] : 0u;
+              float b0 = 0.0f, b1 = 0.0f;
+#pragma unroll
+              for (int t = 0; t < kWarp; ++t) {
+                if ((bits >> t) & 1u) {
+                  const float4 cj = s_c4[j0 + t];
+                  const float tv = fmaf(cj.z, ca, cj.w * sa);
+                  b0 += tv;
+                  b1 = fmaf(s_d[j0 + t] - di, tv, b1);
+                }
+              }
+              n += __popc(bits);
+              kahan_add(S0, C0, b0);
+              kahan_add(S1, C1, b1);
+            }
+          } else {
+            for (int j0 = jlo; j0 < jhi; j0 += kWarp) {
+              float b0 = 0.0f, b1 = 0.0f, mn = 3.0e38f;
+              uint32_t bits = 0u;
+              const bool self_block = (unsigned)(self - j0) < (unsigned)kWarp;
+              if (!exact_all) {
+                if (__any_sync(0xffffffffu, self_block))
+                  block32<KIND, true>(s_c4, s_d, j0, self, fxi, fyi, ca, sa, di, lo2, mid, b0, b1, bits, mn);
+                else
+                  block32<KIND, false>(s_c4, s_d, j0, self, fxi, fyi, ca, sa, di, lo2, mid, b0, b1, bits, mn);
+              }
+              // pairs the float test cannot decide: the reference's FP64 test
+              const bool amb = valid && (exact_all || mn <= band);
+              if (__any_sync(0xffffffffu, amb)) {
+                if (amb) {
+                  for (int t = 0; t < kWarp; ++t) {
+                    const int j = j0 + t;
+                    if (j == self || j >= rcnt) continue;
+                    const float4 cj = s_c4[j];
+                    const float dx = cj.x - fxi, dy = cj.y - fyi;
+                    const float d2 = fmaf(dx, dx, dy * dy);
+                    if (!(exact_all || fabsf(d2 - mid) <= band)) continue;
+                    if (!exact_within(sc, xi, yi, a.sx[s_p[j]], a.sy[s_p[j]])) continue;
+                    if constexpr (KIND == kKindSin) {
+                      b0 += fmaf(cj.w, ca, -cj.z * sa);
+                    } else {
+                      const float tv = fmaf(cj.z, ca, cj.w * sa);
+                      b0 += tv;
+                      b1 = fmaf(s_d[j] - di, tv, b1);
+                    }
+                    bits |= 1u << t;
+                  }
+                }
+              }
+              n += __popc(bits);
+              kahan_add(S0, C0, b0);
+              if constexpr (KIND == kKindCos2) kahan_add(S1, C1, b1);
+              if (KIND == kKindSin && masked && valid)
+                a.nbmask[(size_t)(j0 / kWarp) * n_all + p] = bits;
+            }
+          }
+          if (valid) {
+            red.s[part][li] = S0;
+            red.c[part][li] = C0;
+            red.s1[part][li] = S1;
+            red.c1[part][li] = C1;
+            red.n[part][li] = n;
+          }
+        }
+        __syncthreads();
+        if (tid < gi) {
+          float ts = t_s[tid], tc = t_c[tid], ts1 = t_s1[tid], tc1 = t_c1[tid];
+          int tn = t_n[tid];
+          for (int part = 0; part < S; ++part) {
+            kahan_add(ts, tc, red.s[part][tid]);
+            kahan_add(ts, tc, -red.c[part][tid]);
+            if constexpr (KIND == kKindCos2) {
+              kahan_add(ts1, tc1, red.s1[part][tid]);
+              kahan_add(ts1, tc1, -red.c1[part][tid]);
+            }
+            tn += red.n[part][tid];
+          }
+          t_s[tid] = ts;
+          t_c[tid] = tc;
+          t_s1[tid] = ts1;
+          t_c1[tid] = tc1;
+          t_n[tid] = tn;
+        }
+      }
+      if (tid < gi) {
+        const int p = ig + tid;
+        ILane il;
+        load_i<kPrecFP32C, KIND>(a, il, p, true);
+        Acc<kPrecFP32C> acc;
+        acc.init();
+        acc.s0 = t_s[tid] - t_c[tid];
+        acc.s1 = t_s1[tid] - t_c1[tid];
+        acc.n = t_n[tid];
+        epilogue<kPrecFP32C, KIND>(a, epi, il, acc, a.pidx[p]);
+      }
+      __syncthreads();
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+template <int KIND>
+__global__ void __launch_bounds__(kTileThreads64) k_tile_fp64(KArgs a, int epi) {
+  __shared__ float2 s_xy[kTileCap64];   // x+shift, y+shift (prefilter)
+  __shared__ double s_phi[kTileCap64];  // stage phase
+  __shared__ double s_d[KIND == kKindCos2 ? kTileCap64 : 1];  // pass 2: phase rate
+  __shared__ int s_p[kTileCap64];
+  __shared__ uint16_t s_q[kQCap][kTileThreads64];
+  const SysConst &sc = a.sc;
+  const int tid = threadIdx.x;
+  const float lo2 = sc.lo2, hi2 = sc.hi2;
+  const float band = 0.5f * (hi2 - lo2), mid = 0.5f * (hi2 + lo2);
+  const bool exact_all = sc.exact_all != 0;
+  for (int c = blockIdx.x; c < sc.ncell; c += gridDim.x) {
+    const int cb = a.cell_start[c], ce = a.cell_start[c + 1];
+    if (cb == ce) continue;
+    Stencil st;
+    stencil_of(a, c, st);
+    const int total = st.prefix[9];
+    const int rounds = (total + kTileCap64 - 1) / kTileCap64;
+    for (int ig = cb; ig < ce; ig += kTileThreads64) {
+      const int gi = min(kTileThreads64, ce - ig);
+      const bool valid = tid < gi;
+      const int p = ig + tid;
+      ILane il;
+      load_i<kPrecFP64, KIND>(a, il, p, valid);
+      if (!valid) {
+        il.fx = il.fy = 3.0e30f;
+        il.x = il.y = il.phi = il.dphi = 0.0;
+        il.card = 1.0;
+      }
+      Acc<kPrecFP64> acc;
+      acc.init();
+      for (int r = 0; r < rounds; ++r) {
+        const int rlo = r * kTileCap64, rcnt = min(kTileCap64, total - rlo);
+        if (rounds > 1 || ig == cb) {
+          __syncthreads();
+          for (int k = tid; k < rcnt; k += blockDim.x) {
+            int q;
+            const int pj = slot_of(st, rlo + k, q);
+            const float2 f = a.fxy[pj];
+            s_xy[k] = make_float2(f.x + st.shx[q], f.y + st.shy[q]);
+            s_phi[k] = a.sphi[pj];
+            s_p[k] = pj;
+            if constexpr (KIND == kKindCos2) s_d[k] = a.dphi_s[pj];
+          }
+          __syncthreads();
+        }
+        const int self = st.prefix[4] + (p - cb) - rlo;
+        int qn = 0, qh = 0;
+        auto eval = [&](int j) {
+          const double dphi_ = dsub(dsub(s_phi[j], il.phi), sc.alpha);
+          if constexpr (KIND == kKindSin) {
+            acc.s0 = dadd(acc.s0, sin(dphi_));  // ChimeraSystem.cpp:412
+          } else {
+            const double cc = cos(dphi_);      // ChimeraSystem.cpp:634-637
+            acc.s0 = dadd(acc.s0, ddiv(cc, il.card));
+            acc.s1 = dadd(acc.s1, ddiv(dmul(dsub(s_d[j], il.dphi), cc), il.card));
+          }
+        };
+        for (int j0 = 0; j0 < rcnt; j0 += kWarp) {
+          const int je = min(j0 + kWarp, rcnt);
+          for (int j = j0; j < je; ++j) {
+            const float2 cj = s_xy[j];
+            const float dx = cj.x - il.fx, dy = cj.y - il.fy;
+            const float d2 = fmaf(dx, dx, dy * dy);
+            bool in = !exact_all && (d2 < lo2) && (j != self);
+            const bool amb = (exact_all || fabsf(d2 - mid) <= band) && (j != self) && valid;
+            if (__any_sync(0xffffffffu, amb)) {
+              if (amb) in = exact_within(sc, il.x, il.y, a.sx[s_p[j]], a.sy[s_p[j]]);
+            }
+            if (in) {
+              s_q[qn & (kQCap - 1)][tid] = (uint16_t)j;
+              ++qn;
+            }
+          }
+          // drain the warp's common backlog on full warps, in FIFO order (lanes
+          // past the end of the cell hold no queue and do not bound it)
+          int m = __reduce_min_sync(0xffffffffu, valid ? qn - qh : 0x7fffffff);
+          if (m == 0x7fffffff) m = 0;
+          if (valid) {
+            for (int k = 0; k < m; ++k) eval(s_q[(qh + k) & (kQCap - 1)][tid]);
+            qh += m;
+          }
+          // keep room for the next block of 32
+          while (qn - qh > kQCap - kWarp) {
+            eval(s_q[qh & (kQCap - 1)][tid]);
+            ++qh;
+          }
+        }
+        while (qh < qn) {  // tail of this round
+          eval(s_q[qh & (kQCap - 1)][tid]);
+          ++qh;
+        }
+        acc.n += qn;
+      }
+      if (valid) epilogue<kPrecFP64, KIND>(a, epi, il, acc, a.pidx[p]);
+      __syncthreads();
+    }
+  }
+}
+
+}  // namespace spc
