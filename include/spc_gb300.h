@@ -180,6 +180,55 @@ void *spc_stream(spc_handle *h);
  * draw), for checking against the published known-answer vectors. */
 int spc_philox4x32_10(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]);
 
+/* ---------------------------------------------------------------------------
+ * Batches: many independent systems (each with its own N, box and
+ * parameters) resident in one pool of device memory and advanced together,
+ * one kernel launch per phase for all of them.  The reference runs one system
+ * per process (its parameter scan gives each MPI rank one system,
+ * main.cpp:15-18); here a batch replaces that, and a serving loop admits and
+ * releases systems between calls.  All systems of a batch share the stepper
+ * and precision; dt is per call.  A system admitted with a step budget is
+ * frozen once it has taken that many steps (later steps leave it unchanged),
+ * so requests of different lengths finish exactly.  A system's trajectory is
+ * the same alone or in a batch: its noise is keyed by (seed, system_id,
+ * step, particle) and its neighbour sums never see another system.
+ * ------------------------------------------------------------------------- */
+typedef struct spc_batch spc_batch;
+
+typedef struct spc_batch_config {
+  int32_t stepper;       /* SPC_STEPPER_* of every system */
+  int32_t precision;     /* SPC_PRECISION_* of every system */
+  int32_t max_systems;   /* system slots */
+  int32_t pad;
+  int64_t max_particles; /* pool capacity (sum of N) */
+  int64_t max_cells;     /* sum over systems of int(L/rho)^2 (1 per all-pairs system) */
+} spc_batch_config;
+
+/* Device bytes a batch reserves per pool particle and per cell, for
+ * admission control by memory footprint. */
+int spc_batch_footprint(int32_t stepper, int32_t precision, int64_t *bytes_per_particle,
+                        int64_t *bytes_per_cell);
+int spc_batch_create(const spc_batch_config *cfg, spc_batch **out);
+int spc_batch_destroy(spc_batch *b);
+const char *spc_batch_last_error(const spc_batch *b);
+/* Admit a system (the engine's ctor + state upload, SimulationEngine.cpp:31-50):
+ * aos3n is its initial state, omega its natural frequencies (vortex model,
+ * else NULL), steps its step budget (-1: unlimited).  SPC_ERR_CAPACITY when
+ * the pool has no contiguous room for n particles, or no free cells or slot. */
+int spc_batch_admit(spc_batch *b, const spc_params *p, int32_t n, const double *aos3n,
+                    const double *omega, int64_t steps, int32_t *slot);
+int spc_batch_release(spc_batch *b, int32_t slot);
+/* nsteps steps of every admitted system (DoStep + wrap each, as spc_step). */
+int spc_batch_step(spc_batch *b, double dt, int32_t nsteps);
+int spc_batch_step_graph(spc_batch *b, double dt, int32_t nsteps);
+int spc_batch_download(spc_batch *b, int32_t slot, double *aos3n);
+int spc_batch_upload(spc_batch *b, int32_t slot, const double *aos3n);
+int spc_batch_status(spc_batch *b, int32_t slot, uint64_t *steps_done, int64_t *remaining);
+int spc_batch_usage(spc_batch *b, int64_t *particles, int64_t *cells, int32_t *systems);
+int spc_batch_order_params(spc_batch *b, int32_t slot, double *R, double *psi);
+int spc_batch_synchronize(spc_batch *b);
+void *spc_batch_stream(spc_batch *b);
+
 /* SRK-form right-hand side (as spc_rhs_srk) computed without allocating
  * any device memory.  No counterpart in the reference: it exists for callers
  * that must not call cudaMalloc, such as code whose device memory is owned by

@@ -38,7 +38,7 @@ def lib() -> C.CDLL:
         L.orc_wrap_state.argtypes = [P, dp]
         L.orc_rhs_rk.argtypes = [P, dp, dp, dp, D, D, C.c_void_p]
         L.orc_rhs_srk.argtypes = [P, dp, dp, dp, C.c_void_p]
-        L.orc_step_euler.argtypes = [P, dp, D, D, dp]
+        L.orc_step_euler.argtypes = [P, dp, D, D, dp, C.c_void_p]
         L.orc_step_euler_ptr.argtypes = [P, dp, D, D, dp]
         L.orc_step_srk.argtypes = [P, dp, D, D, dp, C.c_void_p]
         L.orc_step_rk4.argtypes = [P, dp, D, D]

@@ -302,7 +302,7 @@ void orc_rhs_srk(orc_system *s, const double *state, double *derivative,
 /* StochasticEulerStepper::DoStep (StochasticEulerStepper.hpp:31-47) with
  * ChimeraSystem::AddNoise (ChimeraSystem.cpp:924-932). */
 void orc_step_euler(orc_system *s, double *state, double t, double dt,
-                    const double *noise) {
+                    const double *noise, const double *omega) {
   (void)t;
   const int n = s->n;
   memset(s->det, 0, (size_t)3 * n * sizeof(double));
@@ -313,7 +313,10 @@ void orc_step_euler(orc_system *s, double *state, double t, double dt,
   for (int i = 0; i < n; ++i) {
     state[3 * i] += dt * s->det[3 * i] + sqrt(dt) * s->sto[3 * i];
     state[3 * i + 1] += dt * s->det[3 * i + 1] + sqrt(dt) * s->sto[3 * i + 1];
-    state[3 * i + 2] += dt * s->det[3 * i + 2] + sqrt(dt) * s->sto[3 * i + 2];
+    if (omega) /* frequencies in the drift, as StochasticRungeKuttaStepperPtr.hpp:65 */
+      state[3 * i + 2] += dt * (omega[i] + s->det[3 * i + 2]) + sqrt(dt) * s->sto[3 * i + 2];
+    else
+      state[3 * i + 2] += dt * s->det[3 * i + 2] + sqrt(dt) * s->sto[3 * i + 2];
   }
 }
 
@@ -392,7 +395,7 @@ double orc_run(orc_system *s, int stepper, double *state, double t0, double dt,
     t += dt;
     switch (stepper) {
       case ORC_EULER:
-        orc_step_euler(s, state, t, dt, noise + (size_t)k * n);
+        orc_step_euler(s, state, t, dt, noise + (size_t)k * n, omega);
         break;
       case ORC_EULER_PTR:
         orc_step_euler_ptr(s, state, t, dt, noise + (size_t)k * n);

@@ -69,9 +69,11 @@ void orc_rhs_srk(orc_system *s, const double *state, double *derivative,
 /* Steppers.  noise holds the normals of one step in the reference's draw
  * order: Euler one per particle (ChimeraSystem.cpp:924-932), SRK U1 then U2
  * per particle (StochasticRungeKuttaStepper.hpp:44-45).  omega (may be NULL)
- * are the natural frequencies of StochasticRungeKuttaStepperPtr (:65). */
+ * are the natural frequencies of StochasticRungeKuttaStepperPtr (:65); the
+ * Euler stepper, which has no frequency form in the reference, adds them to
+ * its phase drift the same way (an extension for vortex systems). */
 void orc_step_euler(orc_system *s, double *state, double t, double dt,
-                    const double *noise);
+                    const double *noise, const double *omega);
 void orc_step_euler_ptr(orc_system *s, double *state, double t, double dt,
                         const double *noise);
 void orc_step_srk(orc_system *s, double *state, double t, double dt,

@@ -43,6 +43,13 @@ class Params(C.Structure):
     ]
 
 
+class BatchConfig(C.Structure):
+    _fields_ = [
+        ("stepper", C.c_int32), ("precision", C.c_int32), ("max_systems", C.c_int32),
+        ("pad", C.c_int32), ("max_particles", C.c_int64), ("max_cells", C.c_int64),
+    ]
+
+
 _lib = None
 
 
@@ -94,6 +101,26 @@ def lib() -> C.CDLL:
     L.spc_philox4x32_10.argtypes = [C.POINTER(C.c_uint32), C.POINTER(C.c_uint32),
                                     C.POINTER(C.c_uint32)]
     L.spc_profile_steps.argtypes = [H, C.c_double, C.c_int32, dp, C.c_int32]
+    L.spc_batch_footprint.argtypes = [C.c_int32, C.c_int32, C.POINTER(C.c_int64),
+                                      C.POINTER(C.c_int64)]
+    L.spc_batch_create.argtypes = [C.POINTER(BatchConfig), C.POINTER(H)]
+    L.spc_batch_destroy.argtypes = [H]
+    L.spc_batch_last_error.restype = C.c_char_p
+    L.spc_batch_last_error.argtypes = [H]
+    L.spc_batch_admit.argtypes = [H, C.POINTER(Params), C.c_int32, C.c_void_p, C.c_void_p,
+                                  C.c_int64, C.POINTER(C.c_int32)]
+    L.spc_batch_release.argtypes = [H, C.c_int32]
+    L.spc_batch_step.argtypes = [H, C.c_double, C.c_int32]
+    L.spc_batch_step_graph.argtypes = [H, C.c_double, C.c_int32]
+    L.spc_batch_download.argtypes = [H, C.c_int32, C.c_void_p]
+    L.spc_batch_upload.argtypes = [H, C.c_int32, C.c_void_p]
+    L.spc_batch_status.argtypes = [H, C.c_int32, C.POINTER(C.c_uint64), C.POINTER(C.c_int64)]
+    L.spc_batch_usage.argtypes = [H, C.POINTER(C.c_int64), C.POINTER(C.c_int64),
+                                  C.POINTER(C.c_int32)]
+    L.spc_batch_order_params.argtypes = [H, C.c_int32, dp, dp]
+    L.spc_batch_synchronize.argtypes = [H]
+    L.spc_batch_stream.restype = C.c_void_p
+    L.spc_batch_stream.argtypes = [H]
     L.spc_alloc_pinned.argtypes = [C.c_size_t, C.POINTER(C.c_void_p)]
     L.spc_free_pinned.argtypes = [C.c_void_p]
     _lib = L
@@ -278,3 +305,102 @@ def header_functions() -> list[str]:
     path = os.path.join(_build.ROOT, "include", "spc_gb300.h")
     text = open(path).read()
     return sorted(set(re.findall(r"^\s*(?:int|void \*|const char \*)\s*(spc_\w+)\(", text, re.M)))
+
+
+def footprint(stepper: int, precision: int):
+    """(bytes per pool particle, bytes per cell) a batch reserves."""
+    bp, bc = C.c_int64(), C.c_int64()
+    lib().spc_batch_footprint(stepper, precision, C.byref(bp), C.byref(bc))
+    return bp.value, bc.value
+
+
+def cells_of(L: float, rho: float) -> int:
+    """Cells a system occupies in a batch: int(L/rho)^2, or 1 when rho > L/4."""
+    return 1 if not (rho <= 0.25 * L) else int(L / rho) ** 2
+
+
+class Batch:
+    """Many systems advanced together (the C-ABI's spc_batch)."""
+
+    def __init__(self, stepper: int, precision: int, max_systems: int, max_particles: int,
+                 max_cells: int):
+        self._L = lib()
+        self.stepper, self.precision = stepper, precision
+        cfg = BatchConfig(stepper, precision, int(max_systems), 0, int(max_particles),
+                          int(max_cells))
+        h = C.c_void_p()
+        rc = self._L.spc_batch_create(C.byref(cfg), C.byref(h))
+        if rc != SPC_OK:
+            raise SpcError(rc, (self._L.spc_batch_last_error(None) or b"").decode())
+        self.h = h
+        self.n = {}
+
+    def _check(self, rc: int):
+        if rc != SPC_OK:
+            raise SpcError(rc, (self._L.spc_batch_last_error(self.h) or b"").decode())
+
+    def close(self):
+        if getattr(self, "h", None):
+            self._L.spc_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def admit(self, n: int, params: Params, state, omega=None, steps: int = -1) -> int:
+        st = _f64(state, 3 * n)
+        om = None if omega is None else _f64(omega, n)
+        slot = C.c_int32()
+        self._check(self._L.spc_batch_admit(self.h, C.byref(params), int(n), _ptr(st),
+                                            None if om is None else _ptr(om), int(steps),
+                                            C.byref(slot)))
+        self.n[slot.value] = int(n)
+        return slot.value
+
+    def release(self, slot: int):
+        self._check(self._L.spc_batch_release(self.h, int(slot)))
+        self.n.pop(slot, None)
+
+    def step(self, dt: float, nsteps: int, graph: bool = False):
+        f = self._L.spc_batch_step_graph if graph else self._L.spc_batch_step
+        self._check(f(self.h, dt, int(nsteps)))
+
+    def download(self, slot: int, out=None) -> np.ndarray:
+        out = np.empty(3 * self.n[slot]) if out is None else out
+        self._check(self._L.spc_batch_download(self.h, int(slot), _ptr(out)))
+        return out
+
+    def upload(self, slot: int, state):
+        st = _f64(state, 3 * self.n[slot])
+        self._check(self._L.spc_batch_upload(self.h, int(slot), _ptr(st)))
+
+    def status(self, slot: int):
+        done, rem = C.c_uint64(), C.c_int64()
+        self._check(self._L.spc_batch_status(self.h, int(slot), C.byref(done), C.byref(rem)))
+        return done.value, rem.value
+
+    def usage(self):
+        p, c, s = C.c_int64(), C.c_int64(), C.c_int32()
+        self._check(self._L.spc_batch_usage(self.h, C.byref(p), C.byref(c), C.byref(s)))
+        return {"particles": p.value, "cells": c.value, "systems": s.value}
+
+    def order_params(self, slot: int):
+        R, psi = C.c_double(), C.c_double()
+        self._check(self._L.spc_batch_order_params(self.h, int(slot), C.byref(R), C.byref(psi)))
+        return {"R": R.value, "psi": psi.value}
+
+    def synchronize(self):
+        self._check(self._L.spc_batch_synchronize(self.h))
+
+    @property
+    def stream(self) -> int:
+        return self._L.spc_batch_stream(self.h)

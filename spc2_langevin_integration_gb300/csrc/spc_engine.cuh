@@ -1,0 +1,702 @@
+// Host-side engine behind both C-ABI object kinds (a single-system handle is
+// an engine holding one system; a batch holds many).
+//
+// An engine owns, on one CUDA stream:
+//  * a particle pool for the state of every admitted system (x, y, phi,
+//    omega, and RK4's persistent stage rates), first-fit allocated per system;
+//  * per-evaluation scratch sized to the pool (stage arrays, sort buffers,
+//    cell-order copies, float prefilter data, FP32C neighbour bitmasks) and to
+//    the cell capacity (cell table, cell -> system map);
+//  * the device table of active systems (SysDesc) and its host mirror.
+// Admitting or releasing a system changes the layout (dense order of the
+// active systems' particles and their global cell ranges); the next step
+// rebuilds the device tables and drops any cached CUDA graph.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../include/spc_gb300.h"
+#include "spc_kernels.cuh"
+#include "spc_sort.cuh"
+#include "spc_tile.cuh"
+
+namespace spc {
+
+inline std::mutex &err_mutex() {
+  static std::mutex m;
+  return m;
+}
+inline std::string &global_error() {
+  static std::string s;
+  return s;
+}
+
+// A positive finite power of two (then x / L equals x * (1 / L) exactly).
+inline int is_pow2(double L) {
+  int e = 0;
+  return std::frexp(L, &e) == 0.5 ? 1 : 0;
+}
+
+inline int blocks_for(long long n, int threads) { return (int)((n + threads - 1) / threads); }
+
+inline int noise_per_particle(int stepper) {
+  switch (stepper) {
+    case SPC_STEPPER_SRK: return 2;
+    case SPC_STEPPER_RK4: return 0;
+    default: return 1;
+  }
+}
+
+// Per-system constants from the public parameters (ChimeraSystem.cpp:19-33).
+inline SysConst make_sysconst(const spc_params &p, int n) {
+  SysConst sc{};
+  sc.n = n;
+  sc.L = p.L;
+  sc.rL = 1.0 / p.L;
+  sc.rho2 = p.rho * p.rho;
+  sc.v0 = p.v0;
+  sc.sigma = p.sigma;
+  sc.alpha = p.alpha;
+  sc.D = p.D_phi;
+  sc.allpairs = !(p.rho <= 0.25 * p.L);
+  sc.nc = sc.allpairs ? 1 : std::max(1, (int)(p.L / p.rho));
+  sc.ncell = sc.nc * sc.nc;
+  sc.cell = p.L / sc.nc;
+  sc.cell_f = (float)sc.cell;
+  // prefilter band: a relative 3e-5 of rho^2 on each side, far wider than the
+  // float error of the cell-relative dr^2 (about 3e-6 rho^2 for cells <= 4/3 rho)
+  sc.lo2 = (float)(sc.rho2 * (1.0 - 3e-5));
+  sc.hi2 = (float)(sc.rho2 * (1.0 + 3e-5));
+  sc.exact_all = (p.flags & SPC_FLAG_EXACT_ALL) ? 1 : 0;
+  sc.L_pow2 = is_pow2(p.L);
+  return sc;
+}
+
+inline int validate_params(const spc_params *p, int n, std::string &why) {
+  char buf[256];
+  auto bad = [&](const char *m) {
+    why = m;
+    return SPC_ERR_INVALID;
+  };
+  if (!p) return bad("params is NULL");
+  if (n <= 0) {
+    snprintf(buf, sizeof(buf), "n must be positive (got %d)", n);
+    return bad(buf);
+  }
+  if (!(p->L > 0.0) || !std::isfinite(p->L)) return bad("L must be positive");
+  if (!(p->rho > 0.0) || !std::isfinite(p->rho)) return bad("rho must be positive");
+  if (!(p->D_phi >= 0.0) || !std::isfinite(p->D_phi)) return bad("D_phi must be >= 0");
+  if (!std::isfinite(p->v0) || !std::isfinite(p->sigma) || !std::isfinite(p->alpha))
+    return bad("v0, sigma, alpha must be finite");
+  if (p->model != SPC_MODEL_CHIMERA && p->model != SPC_MODEL_VORTEX) return bad("unknown model");
+  if (p->stepper < SPC_STEPPER_EULER || p->stepper > SPC_STEPPER_EULER_PTR) return bad("unknown stepper");
+  if (p->model == SPC_MODEL_VORTEX && p->stepper != SPC_STEPPER_SRK && p->stepper != SPC_STEPPER_EULER)
+    return bad("the vortex model's natural frequencies enter the Euler and stochastic Runge-Kutta drifts only");
+  if (p->neighbour != SPC_NEIGHBOUR_CELL && p->neighbour != SPC_NEIGHBOUR_VERLET)
+    return bad("unknown neighbour search");
+  if (p->precision != SPC_PRECISION_FP64 && p->precision != SPC_PRECISION_FP32C)
+    return bad("unknown precision");
+  if (p->neighbour == SPC_NEIGHBOUR_VERLET && !(p->skin > 0.0)) return bad("Verlet skin must be positive");
+  if (p->rho <= 0.25 * p->L && std::floor(p->L / p->rho) > 46340.0) return bad("too many cells");
+  return SPC_OK;
+}
+
+struct SysHost {
+  bool used = false;
+  spc_params p{};
+  int n = 0;
+  int pool_p0 = 0;
+  int ncell = 0;  // cells it occupies in the global cell list (1 for all pairs)
+  SysConst sc{};
+  unsigned long long step = 0;
+  long long remaining = 0;
+  bool omega_set = false;
+};
+
+struct Engine {
+  int stepper = 0, precision = 0, device = 0;
+  cudaStream_t stream = nullptr;
+  std::vector<void *> allocs;
+  std::string err;
+  // capacities
+  int pool_cap = 0, sys_cap = 0, cell_cap = 0, tile_cap = 0;
+  KArgs a{};
+  SysDesc *d_sys = nullptr;
+  int *d_ap = nullptr;
+  unsigned long long *d_clamped = nullptr;
+  uint32_t *keys_alt = nullptr, *vals_alt = nullptr, *hist = nullptr, *part = nullptr;
+  double *aos = nullptr;  // AoS staging (12 x pool_cap doubles)
+  double *order_part = nullptr;
+  int order_blocks = 0;
+  // host mirror
+  std::vector<SysHost> slots;
+  std::vector<int> order;  // active slots in layout order
+  std::vector<std::pair<int, int>> free_ranges;  // (start, length), sorted by start
+  int cells_used = 0;
+  bool dirty = true;
+  // current layout
+  int nsys = 0, n_active = 0, ncell_total = 0, ntiles = 0, radix_bits = 1, sort_passes = 1;
+  bool has_cells = false;
+  std::vector<int> slot_layout;  // slot -> layout index (-1 if inactive)
+  // noise injection (single-system handles)
+  double *d_noise = nullptr;
+  long long noise_count = 0, noise_cursor = 0;
+  bool injecting = false;
+  bool scratch_k = false;
+  // graph cache
+  cudaGraphExec_t graph = nullptr;
+  int graph_steps = 0;
+  double graph_dt = 0.0;
+  // profiling marks
+  cudaEvent_t prof_ev[8] = {};
+  bool profiling = false;
+  // an engine that is a view over caller-provided memory owns nothing
+  bool view = false;
+};
+
+inline int fail(Engine *e, int code, const char *fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  if (e) e->err = buf;
+  std::lock_guard<std::mutex> lk(err_mutex());
+  global_error() = buf;
+  return code;
+}
+
+#define SPC_CUDA(e, call)                                                                    \
+  do {                                                                                       \
+    cudaError_t e_ = (call);                                                                 \
+    if (e_ != cudaSuccess)                                                                   \
+      return ::spc::fail((e), e_ == cudaErrorMemoryAllocation ? SPC_ERR_NOMEM : SPC_ERR_CUDA, \
+                         "%s: %s (%s:%d)", #call, cudaGetErrorString(e_), __FILE__, __LINE__); \
+  } while (0)
+
+#define SPC_LAUNCHED(e) SPC_CUDA(e, cudaGetLastError())
+
+#define SPC_TRY(expr)              \
+  do {                             \
+    int rc_ = (expr);              \
+    if (rc_ != SPC_OK) return rc_; \
+  } while (0)
+
+template <class T>
+int dalloc(Engine *e, T **ptr, size_t count) {
+  void *p = nullptr;
+  cudaError_t ce = cudaMalloc(&p, std::max<size_t>(count, 1) * sizeof(T));
+  if (ce != cudaSuccess)
+    return fail(e, SPC_ERR_NOMEM, "cudaMalloc(%zu bytes): %s", count * sizeof(T), cudaGetErrorString(ce));
+  e->allocs.push_back(p);
+  *ptr = (T *)p;
+  return SPC_OK;
+}
+
+// The 11-bit scatter needs more than the default 48 KB of dynamic shared
+// memory; the attribute is set with the device current (not a stream
+// operation, so never inside a capture).
+inline cudaError_t set_kernel_attributes() {
+  return cudaFuncSetAttribute(k_radix_scatter, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              (int)scatter_smem_bytes(11));
+}
+
+inline int engine_set_device(Engine *e) {
+  SPC_CUDA(e, cudaSetDevice(e->device));
+  return SPC_OK;
+}
+
+// Bytes of device memory per pool particle and per cell for a stepper/precision.
+inline void engine_footprint(int stepper, int precision, long long *per_particle, long long *per_cell) {
+  long long b = 4 * 8;                       // x, y, phi, omega
+  if (stepper == SPC_STEPPER_RK4) b += 12 * 8;  // k1..k4
+  b += 3 * 8 + 4 * 4 + 3 * 8 + 8 + 4 + 8 + 4 + 4 + 4;  // stage, sort, cell order, fxy, pidx, dphi, cnt, sys_of_p
+  if (precision == SPC_PRECISION_FP32C) b += 8 + 4 + (long long)kMaskWords * 4;  // cs, dphi_f, masks
+  b += 12 * 8 + 4 + 4;                       // AoS staging, histogram share
+  *per_particle = b;
+  *per_cell = 4 + 4;                         // cell_start, sys_of_c
+}
+
+inline int engine_init(Engine *e, int stepper, int precision, int pool_cap, int sys_cap, int cell_cap) {
+  e->stepper = stepper;
+  e->precision = precision;
+  e->pool_cap = pool_cap;
+  e->sys_cap = sys_cap;
+  e->cell_cap = cell_cap;
+  if (cudaGetDevice(&e->device) != cudaSuccess) return fail(e, SPC_ERR_CUDA, "no CUDA device");
+  if (set_kernel_attributes() != cudaSuccess) return fail(e, SPC_ERR_CUDA, "cudaFuncSetAttribute failed");
+  SPC_CUDA(e, cudaStreamCreateWithFlags(&e->stream, cudaStreamNonBlocking));
+  const size_t N = (size_t)pool_cap;
+  KArgs &a = e->a;
+  e->tile_cap = (int)((N + kSortTile - 1) / kSortTile);
+  SPC_TRY(dalloc(e, &a.x, N));
+  SPC_TRY(dalloc(e, &a.y, N));
+  SPC_TRY(dalloc(e, &a.phi, N));
+  double *omega = nullptr;
+  SPC_TRY(dalloc(e, &omega, N));
+  a.omega = omega;
+  if (stepper == SPC_STEPPER_RK4)
+    for (int q = 0; q < 4; ++q) {
+      SPC_TRY(dalloc(e, &a.kx[q], N));
+      SPC_TRY(dalloc(e, &a.ky[q], N));
+      SPC_TRY(dalloc(e, &a.kphi[q], N));
+    }
+  SPC_TRY(dalloc(e, &a.st_x, N));
+  SPC_TRY(dalloc(e, &a.st_y, N));
+  SPC_TRY(dalloc(e, &a.st_phi, N));
+  SPC_TRY(dalloc(e, &a.keys, N));
+  SPC_TRY(dalloc(e, &a.vals, N));
+  SPC_TRY(dalloc(e, &e->keys_alt, N));
+  SPC_TRY(dalloc(e, &e->vals_alt, N));
+  SPC_TRY(dalloc(e, &a.sx, N));
+  SPC_TRY(dalloc(e, &a.sy, N));
+  SPC_TRY(dalloc(e, &a.sphi, N));
+  SPC_TRY(dalloc(e, &a.fxy, N));
+  SPC_TRY(dalloc(e, &a.pidx, N));
+  SPC_TRY(dalloc(e, &a.dphi_s, N));
+  SPC_TRY(dalloc(e, &a.cnt_s, N));
+  int *sys_of_p = nullptr, *sys_of_c = nullptr;
+  SPC_TRY(dalloc(e, &sys_of_p, N));
+  a.sys_of_p = sys_of_p;
+  if (precision == SPC_PRECISION_FP32C) {
+    SPC_TRY(dalloc(e, &a.cs, N));
+    SPC_TRY(dalloc(e, &a.dphi_f, N));
+    SPC_TRY(dalloc(e, &a.nbmask, (size_t)kMaskWords * N));
+  }
+  SPC_TRY(dalloc(e, &a.cell_start, (size_t)cell_cap + 1));
+  SPC_TRY(dalloc(e, &sys_of_c, (size_t)cell_cap));
+  a.sys_of_c = sys_of_c;
+  // radix histogram table: up to 2^11 digits per tile, plus group partials
+  SPC_TRY(dalloc(e, &e->hist, (size_t)(1 << 11) * e->tile_cap));
+  SPC_TRY(dalloc(e, &e->part, (size_t)(1 << 11) * ((e->tile_cap + kScanGroup - 1) / kScanGroup)));
+  SPC_TRY(dalloc(e, &e->d_sys, (size_t)sys_cap));
+  SPC_TRY(dalloc(e, &e->d_ap, (size_t)sys_cap));
+  SPC_TRY(dalloc(e, &e->d_clamped, 1));
+  SPC_TRY(dalloc(e, &e->aos, 12 * N));
+  e->order_blocks = std::min(blocks_for((long long)N, 256), 1024);
+  SPC_TRY(dalloc(e, &e->order_part, 2 * (size_t)e->order_blocks));
+  a.sys = e->d_sys;
+  a.ap_cells = e->d_ap;
+  a.clamped = e->d_clamped;
+  a.hist = e->hist;
+  cudaStream_t st = e->stream;
+  SPC_CUDA(e, cudaMemsetAsync(omega, 0, N * 8, st));
+  SPC_CUDA(e, cudaMemsetAsync(e->hist, 0, (size_t)(1 << 11) * e->tile_cap * 4, st));
+  SPC_CUDA(e, cudaMemsetAsync(e->d_clamped, 0, 8, st));
+  if (stepper == SPC_STEPPER_RK4)
+    for (int q = 0; q < 4; ++q) {
+      SPC_CUDA(e, cudaMemsetAsync(a.kx[q], 0, N * 8, st));
+      SPC_CUDA(e, cudaMemsetAsync(a.ky[q], 0, N * 8, st));
+      SPC_CUDA(e, cudaMemsetAsync(a.kphi[q], 0, N * 8, st));
+    }
+  SPC_CUDA(e, cudaStreamSynchronize(st));
+  e->slots.assign(sys_cap, SysHost());
+  e->slot_layout.assign(sys_cap, -1);
+  e->free_ranges.clear();
+  e->free_ranges.push_back({0, pool_cap});
+  return SPC_OK;
+}
+
+inline void engine_free(Engine *e) {
+  if (!e || e->view) return;
+  cudaSetDevice(e->device);
+  if (e->stream) cudaStreamSynchronize(e->stream);
+  if (e->graph) cudaGraphExecDestroy(e->graph);
+  for (cudaEvent_t ev : e->prof_ev)
+    if (ev) cudaEventDestroy(ev);
+  for (void *p : e->allocs) cudaFree(p);
+  e->allocs.clear();
+  if (e->stream) cudaStreamDestroy(e->stream);
+  e->stream = nullptr;
+}
+
+// ---------------------------------------------------------------------------
+// pool allocator (first fit, coalescing)
+inline int pool_take(Engine *e, int n) {
+  for (size_t k = 0; k < e->free_ranges.size(); ++k) {
+    auto &r = e->free_ranges[k];
+    if (r.second >= n) {
+      const int at = r.first;
+      r.first += n;
+      r.second -= n;
+      if (r.second == 0) e->free_ranges.erase(e->free_ranges.begin() + k);
+      return at;
+    }
+  }
+  return -1;
+}
+
+inline void pool_give(Engine *e, int at, int n) {
+  auto &fr = e->free_ranges;
+  fr.push_back({at, n});
+  std::sort(fr.begin(), fr.end());
+  std::vector<std::pair<int, int>> merged;
+  for (auto &r : fr) {
+    if (!merged.empty() && merged.back().first + merged.back().second == r.first)
+      merged.back().second += r.second;
+    else
+      merged.push_back(r);
+  }
+  fr.swap(merged);
+}
+
+inline void drop_graph(Engine *e) {
+  if (e->graph) {
+    cudaGraphExecDestroy(e->graph);
+    e->graph = nullptr;
+  }
+}
+
+// Admit a system: its state goes to a pool range; returns the slot.
+inline int engine_admit(Engine *e, const spc_params &p, int n, long long steps, int *slot_out) {
+  std::string why;
+  int rc = validate_params(&p, n, why);
+  if (rc) return fail(e, rc, "%s", why.c_str());
+  if (p.stepper != e->stepper) return fail(e, SPC_ERR_INVALID, "stepper differs from the batch's");
+  if (p.precision != e->precision) return fail(e, SPC_ERR_INVALID, "precision differs from the batch's");
+  SysConst sc = make_sysconst(p, n);
+  const int ncell = sc.allpairs ? 1 : sc.ncell;
+  int slot = -1;
+  for (int s = 0; s < e->sys_cap; ++s)
+    if (!e->slots[s].used) {
+      slot = s;
+      break;
+    }
+  if (slot < 0) return fail(e, SPC_ERR_CAPACITY, "no free system slot (capacity %d)", e->sys_cap);
+  if (e->cells_used + ncell > e->cell_cap)
+    return fail(e, SPC_ERR_CAPACITY, "cells: %d used + %d needed > %d", e->cells_used, ncell, e->cell_cap);
+  const int at = pool_take(e, n);
+  if (at < 0) return fail(e, SPC_ERR_CAPACITY, "no contiguous pool range of %d particles", n);
+  SysHost &h = e->slots[slot];
+  h = SysHost();
+  h.used = true;
+  h.p = p;
+  h.n = n;
+  h.pool_p0 = at;
+  h.ncell = ncell;
+  h.sc = sc;
+  h.step = 0;
+  h.remaining = steps < 0 ? (1ll << 62) : steps;
+  e->cells_used += ncell;
+  e->order.push_back(slot);
+  e->dirty = true;
+  *slot_out = slot;
+  return SPC_OK;
+}
+
+inline int engine_release(Engine *e, int slot) {
+  if (slot < 0 || slot >= e->sys_cap || !e->slots[slot].used)
+    return fail(e, SPC_ERR_INVALID, "no system in slot %d", slot);
+  SysHost &h = e->slots[slot];
+  pool_give(e, h.pool_p0, h.n);
+  e->cells_used -= h.ncell;
+  h.used = false;
+  e->order.erase(std::find(e->order.begin(), e->order.end(), slot));
+  e->dirty = true;
+  return SPC_OK;
+}
+
+inline SysDesc desc_of(const SysHost &h, int dense_p0, int c0) {
+  SysDesc d{};
+  d.sc = h.sc;
+  d.pool_p0 = h.pool_p0;
+  d.dense_p0 = dense_p0;
+  d.c0 = c0;
+  d.is_vortex = h.p.model == SPC_MODEL_VORTEX;
+  d.system_id = h.p.system_id;
+  d.seed = h.p.seed;
+  d.step = h.step;
+  d.remaining = h.remaining;
+  d.budget = 0;
+  return d;
+}
+
+// Rebuild the device layout tables from the host mirror.
+inline int engine_layout(Engine *e) {
+  if (!e->dirty) return SPC_OK;
+  drop_graph(e);
+  std::vector<SysDesc> table;
+  std::vector<int> ap;
+  int dense = 0, cells = 0;
+  std::fill(e->slot_layout.begin(), e->slot_layout.end(), -1);
+  for (int slot : e->order) {
+    const SysHost &h = e->slots[slot];
+    e->slot_layout[slot] = (int)table.size();
+    table.push_back(desc_of(h, dense, cells));
+    if (h.sc.allpairs) ap.push_back(cells);
+    dense += h.n;
+    cells += h.ncell;
+  }
+  e->nsys = (int)table.size();
+  e->n_active = dense;
+  e->ncell_total = cells;
+  e->ntiles = std::max(1, (dense + kSortTile - 1) / kSortTile);
+  int bits = 1;
+  while (bits < 31 && (1u << bits) < (unsigned)std::max(cells, 2)) ++bits;
+  e->sort_passes = (bits + 10) / 11;
+  e->radix_bits = (bits + e->sort_passes - 1) / e->sort_passes;
+  e->has_cells = cells > (int)ap.size();
+  KArgs &a = e->a;
+  a.nsys = e->nsys;
+  a.n_active = e->n_active;
+  a.ncell_total = e->ncell_total;
+  a.n_ap = (int)ap.size();
+  a.hist_len = (1 << e->radix_bits) * e->ntiles;
+  if (e->nsys > 0) {
+    SPC_CUDA(e, cudaMemcpyAsync(e->d_sys, table.data(), table.size() * sizeof(SysDesc),
+                                cudaMemcpyHostToDevice, e->stream));
+    if (!ap.empty())
+      SPC_CUDA(e, cudaMemcpyAsync(e->d_ap, ap.data(), ap.size() * sizeof(int), cudaMemcpyHostToDevice,
+                                  e->stream));
+    const int g = std::max(e->n_active, e->ncell_total);
+    k_layout_maps<<<blocks_for(g, 256), 256, 0, e->stream>>>(e->d_sys, e->nsys, e->n_active, e->ncell_total,
+                                                             (int *)a.sys_of_p, (int *)a.sys_of_c);
+    SPC_LAUNCHED(e);
+    // the histogram table must be zero before the next stage kernel
+    SPC_CUDA(e, cudaMemsetAsync(e->hist, 0, (size_t)(1 << 11) * e->tile_cap * 4, e->stream));
+    // host-side copies above read pageable memory: finish before `table` dies
+    SPC_CUDA(e, cudaStreamSynchronize(e->stream));
+  }
+  e->dirty = false;
+  return SPC_OK;
+}
+
+inline void mark(Engine *e, int slot) {
+  if (e->profiling) cudaEventRecord(e->prof_ev[slot], e->stream);
+}
+
+// One evaluation's binning: stage, sort, cell bounds, cell-order gather.
+inline int eval_stage(Engine *e, KArgs &a, int rk_form, int kq, double kcdt) {
+  const int n = e->n_active;
+  cudaStream_t st = e->stream;
+  const int bits = e->radix_bits;
+  k_stage<<<blocks_for(n, kStageThreads), kStageThreads, 0, st>>>(a, rk_form, kq, kcdt, bits, e->hist);
+  SPC_LAUNCHED(e);
+  mark(e, 1);
+  uint32_t *kin = a.keys, *vin = a.vals, *kout = e->keys_alt, *vout = e->vals_alt;
+  for (int pass = 0; pass < e->sort_passes; ++pass) {
+    const int shift = pass * bits;
+    if (pass > 0) k_radix_hist<<<e->ntiles, kSortThreads, 0, st>>>(kin, n, shift, bits, e->hist);
+    if (e->ntiles <= kScanGroup) {
+      k_scan_digits<<<1, kScanThreads, 0, st>>>(e->hist, e->ntiles, bits);
+    } else {
+      const int ng = (e->ntiles + kScanGroup - 1) / kScanGroup;
+      const dim3 grid(ng, blocks_for(1 << bits, 256));
+      k_scan_group_sums<<<grid, 256, 0, st>>>(e->hist, e->ntiles, bits, e->part);
+      k_scan_digits<<<1, kScanThreads, 0, st>>>(e->part, ng, bits);
+      k_scan_group_apply<<<grid, 256, 0, st>>>(e->hist, e->ntiles, bits, e->part);
+    }
+    k_radix_scatter<<<e->ntiles, kSortThreads, scatter_smem_bytes(bits), st>>>(kin, vin, kout, vout, n,
+                                                                               shift, bits, e->hist);
+    SPC_LAUNCHED(e);
+    std::swap(kin, kout);
+    std::swap(vin, vout);
+  }
+  mark(e, 2);
+  a.skeys = kin;
+  a.svals = vin;
+  if (e->precision == SPC_PRECISION_FP32C)
+    k_gather<kPrecFP32C><<<blocks_for(n + 1, 256), 256, 0, st>>>(a);
+  else
+    k_gather<kPrecFP64><<<blocks_for(n + 1, 256), 256, 0, st>>>(a);
+  SPC_LAUNCHED(e);
+  mark(e, 3);
+  return SPC_OK;
+}
+
+template <int PREC, int KIND>
+int launch_pass_t(Engine *e, const KArgs &a, int epi) {
+  cudaStream_t st = e->stream;
+  if (a.n_ap > 0) {
+    k_allpairs_pass<PREC, KIND><<<std::min(a.n_ap, 152 * 16), kAllPairsThreads, 0, st>>>(a, epi);
+    SPC_LAUNCHED(e);
+  }
+  if (e->has_cells) {
+    const int grid = std::min(e->ncell_total, 152 * 256);
+    if constexpr (KIND == kKindNb) {
+      k_cell_pass<PREC, KIND><<<std::min(blocks_for(e->ncell_total, kPassWarps), 152 * 64), kPassThreads, 0,
+                                st>>>(a, epi);
+    } else if constexpr (PREC == kPrecFP32C) {
+      k_tile_fp32c<KIND><<<grid, kTileThreads32, 0, st>>>(a, epi);
+    } else {
+      k_tile_fp64<KIND><<<grid, kTileThreads64, 0, st>>>(a, epi);
+    }
+    SPC_LAUNCHED(e);
+  }
+  return SPC_OK;
+}
+
+inline int launch_pass(Engine *e, const KArgs &a, int kind, int epi) {
+  const bool fp32 = e->precision == SPC_PRECISION_FP32C;
+  if (kind == kKindSin)
+    return fp32 ? launch_pass_t<kPrecFP32C, kKindSin>(e, a, epi) : launch_pass_t<kPrecFP64, kKindSin>(e, a, epi);
+  if (kind == kKindCos2)
+    return fp32 ? launch_pass_t<kPrecFP32C, kKindCos2>(e, a, epi) : launch_pass_t<kPrecFP64, kKindCos2>(e, a, epi);
+  return launch_pass_t<kPrecFP64, kKindNb>(e, a, epi);
+}
+
+// Enqueue one DoStep + wrap of every active system.  noise: pool-indexed
+// device normals of this step, or null for Philox.
+inline int enqueue_step(Engine *e, double dt, int step_off, const double *noise) {
+  KArgs a = e->a;
+  a.dt = dt;
+  a.noise = noise;
+  a.noise_m = noise_per_particle(e->stepper);
+  a.step_off = step_off;
+  switch (e->stepper) {
+    case SPC_STEPPER_EULER:
+      // EvaluateRhs(x, det, det, 0.0, dt) on the zero-filled det (StochasticEulerStepper.hpp:34-37)
+      SPC_TRY(eval_stage(e, a, 1, -1, 0.0 * dt));
+      SPC_TRY(launch_pass(e, a, kKindSin, kEpiEuler));
+      mark(e, 4);
+      break;
+    case SPC_STEPPER_EULER_PTR:
+      SPC_TRY(eval_stage(e, a, 0, -1, 0.0));
+      SPC_TRY(launch_pass(e, a, kKindSin, kEpiEulerPtr));
+      mark(e, 4);
+      break;
+    case SPC_STEPPER_SRK:
+      SPC_TRY(eval_stage(e, a, 0, -1, 0.0));
+      SPC_TRY(launch_pass(e, a, kKindSin, kEpiSrk1));
+      mark(e, 4);
+      SPC_TRY(launch_pass(e, a, kKindCos2, kEpiSrk2));
+      break;
+    case SPC_STEPPER_RK4: {
+      // RungeKutta4Stepper.cpp:31-45: k_coef 0, 1/2, 1/2, 1 on k1, k1, k2, k3
+      const double coef[4] = {0.0, 0.5, 0.5, 1.0};
+      const int kprev[4] = {0, 0, 1, 2};
+      for (int s = 0; s < 4; ++s) {
+        if (s > 0) e->profiling = false;  // phases are timed on the first stage
+        SPC_TRY(eval_stage(e, a, 1, kprev[s], coef[s] * dt));
+        a.kq_out = s;
+        SPC_TRY(launch_pass(e, a, kKindSin, s == 3 ? kEpiRk4Combine : kEpiRkK));
+        if (s == 0) mark(e, 4);
+      }
+      break;
+    }
+    default:
+      return fail(e, SPC_ERR_INVALID, "unknown stepper %d", e->stepper);
+  }
+  return SPC_OK;
+}
+
+// Host mirror of the per-call step bookkeeping (k_begin_call / k_end_call).
+inline void mirror_call(Engine *e, int nsteps) {
+  for (int slot : e->order) {
+    SysHost &h = e->slots[slot];
+    const long long b = std::max(0ll, std::min<long long>(nsteps, h.remaining));
+    h.step += (unsigned long long)b;
+    h.remaining -= b;
+  }
+}
+
+// nsteps steps of every active system (eagerly launched or as a replayed
+// CUDA graph).  noise (single-system injection) is consumed per step.
+inline int engine_steps(Engine *e, double dt, int nsteps, bool use_graph, const double *noise_base,
+                        long long noise_per_step) {
+  SPC_TRY(engine_set_device(e));
+  SPC_TRY(engine_layout(e));
+  if (e->nsys == 0 || nsteps == 0) return SPC_OK;
+  const int sb = blocks_for(e->nsys, 128);
+  if (!use_graph) {
+    k_begin_call<<<sb, 128, 0, e->stream>>>(e->d_sys, e->nsys, nsteps);
+    SPC_LAUNCHED(e);
+    for (int s = 0; s < nsteps; ++s)
+      SPC_TRY(enqueue_step(e, dt, s, noise_base ? noise_base + (long long)s * noise_per_step : nullptr));
+    k_end_call<<<sb, 128, 0, e->stream>>>(e->d_sys, e->nsys);
+    SPC_LAUNCHED(e);
+  } else {
+    if (!e->graph || e->graph_steps != nsteps || e->graph_dt != dt) {
+      drop_graph(e);
+      cudaGraph_t g = nullptr;
+      SPC_CUDA(e, cudaStreamBeginCapture(e->stream, cudaStreamCaptureModeThreadLocal));
+      int rc = SPC_OK;
+      k_begin_call<<<sb, 128, 0, e->stream>>>(e->d_sys, e->nsys, nsteps);
+      for (int s = 0; s < nsteps && rc == SPC_OK; ++s) rc = enqueue_step(e, dt, s, nullptr);
+      k_end_call<<<sb, 128, 0, e->stream>>>(e->d_sys, e->nsys);
+      cudaError_t ce = cudaStreamEndCapture(e->stream, &g);
+      if (rc != SPC_OK) {
+        if (g) cudaGraphDestroy(g);
+        return rc;
+      }
+      if (ce != cudaSuccess) return fail(e, SPC_ERR_CUDA, "graph capture: %s", cudaGetErrorString(ce));
+      ce = cudaGraphInstantiate(&e->graph, g, 0);
+      cudaGraphDestroy(g);
+      if (ce != cudaSuccess) {
+        e->graph = nullptr;
+        return fail(e, SPC_ERR_CUDA, "graph instantiate: %s", cudaGetErrorString(ce));
+      }
+      e->graph_steps = nsteps;
+      e->graph_dt = dt;
+    }
+    SPC_CUDA(e, cudaGraphLaunch(e->graph, e->stream));
+  }
+  mirror_call(e, nsteps);
+  return SPC_OK;
+}
+
+// Per-system overwrite of the device table's step counter (the layout copy
+// is rebuilt from the host mirror, so this only marks the layout dirty).
+inline void engine_set_step(Engine *e, int slot, unsigned long long step) {
+  e->slots[slot].step = step;
+  e->dirty = true;
+}
+
+// AoS <-> pool range of one system
+inline int engine_upload(Engine *e, int slot, const double *aos3n) {
+  const SysHost &h = e->slots[slot];
+  SPC_CUDA(e, cudaMemcpyAsync(e->aos, aos3n, 3 * (size_t)h.n * 8, cudaMemcpyHostToDevice, e->stream));
+  k_aos_to_soa<<<blocks_for(h.n, 256), 256, 0, e->stream>>>(e->aos, h.n, e->a.x + h.pool_p0,
+                                                            e->a.y + h.pool_p0, e->a.phi + h.pool_p0);
+  SPC_LAUNCHED(e);
+  return SPC_OK;
+}
+
+inline int engine_download(Engine *e, int slot, double *aos3n) {
+  const SysHost &h = e->slots[slot];
+  k_soa_to_aos<<<blocks_for(h.n, 256), 256, 0, e->stream>>>(e->a.x + h.pool_p0, e->a.y + h.pool_p0,
+                                                            e->a.phi + h.pool_p0, h.n, e->aos);
+  SPC_LAUNCHED(e);
+  SPC_CUDA(e, cudaMemcpyAsync(aos3n, e->aos, 3 * (size_t)h.n * 8, cudaMemcpyDeviceToHost, e->stream));
+  SPC_CUDA(e, cudaStreamSynchronize(e->stream));
+  return SPC_OK;
+}
+
+inline int engine_upload_omega(Engine *e, int slot, const double *omega) {
+  SysHost &h = e->slots[slot];
+  SPC_CUDA(e, cudaMemcpyAsync((double *)e->a.omega + h.pool_p0, omega, (size_t)h.n * 8,
+                              cudaMemcpyHostToDevice, e->stream));
+  SPC_CUDA(e, cudaStreamSynchronize(e->stream));
+  h.omega_set = true;
+  return SPC_OK;
+}
+
+inline int engine_order_global(Engine *e, int slot, double *R, double *psi) {
+  const SysHost &h = e->slots[slot];
+  const int blocks = std::min(blocks_for(h.n, 256), e->order_blocks);
+  k_order_sum<<<blocks, 256, 0, e->stream>>>(e->a.phi + h.pool_p0, h.n, e->order_part);
+  SPC_LAUNCHED(e);
+  std::vector<double> part(2 * (size_t)blocks);
+  SPC_CUDA(e, cudaMemcpyAsync(part.data(), e->order_part, part.size() * 8, cudaMemcpyDeviceToHost, e->stream));
+  SPC_CUDA(e, cudaStreamSynchronize(e->stream));
+  double re = 0.0, im = 0.0;
+  for (int b = 0; b < blocks; ++b) {
+    re += part[2 * b];
+    im += part[2 * b + 1];
+  }
+  re /= (double)h.n;
+  im /= (double)h.n;
+  if (R) *R = std::hypot(re, im);
+  if (psi) *psi = std::atan2(im, re);
+  return SPC_OK;
+}
+
+}  // namespace spc

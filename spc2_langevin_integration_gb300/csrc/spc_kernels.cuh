@@ -1,16 +1,27 @@
-// Kernels of one right-hand-side evaluation and the fused stepper updates.
+// Kernels of one right-hand-side evaluation and the fused stepper updates,
+// for a batch of independent systems in one launch per phase.
 //
 // One evaluation (the reference's EvaluateInteractionsWithLinkedList,
 // ChimeraSystem.cpp:258-426 / :429-645) runs as:
 //   k_stage   stage state s + k_coef*dt*k_prev, copy-wrap, cell key  (ChimeraSystem.cpp:270-309)
-//   sort      stable radix sort of (key, index)                       (:335-338)
+//   sort      stable radix sort of (global cell key, index)           (:335-338)
 //   k_gather  particles into cell order + float prefilter coordinates
-//   k_cell_pass<...>  one warp per cell tile: the 3x3 stencil in the
+//   k_tile_*  (spc_tile.cuh) one CTA per cell: the 3x3 stencil in the
 //             reference's order, the exact FP64 cutoff, the alignment sums,
 //             then a fused epilogue (k_next, or the whole stepper update with
 //             noise and the engine's periodic wrap).
 // When rho > L/4 the reference switches to all pairs (ChimeraSystem.cpp:90-98)
-// on unwrapped stage positions; k_allpairs_pass does the same.
+// on unwrapped stage positions; such a system is one "cell" here and
+// k_allpairs_pass handles it.
+//
+// Indexing.  State (x, y, phi, omega, RK4 rates) lives in a particle pool:
+// system s owns pool slots [pool_p0, pool_p0 + n).  Each evaluation works on
+// the dense list of the active systems' particles, d in [0, n_active) with
+// system s at [dense_p0, dense_p0 + n); after the sort, slot p in
+// [0, n_active) is cell order.  Cells are global: system s owns cells
+// [c0, c0 + nc^2) (one cell for an all-pairs system).  Per-system constants
+// come from the SysDesc table, so a single system and a batch of hundreds run
+// the same kernels.
 #pragma once
 
 #include "spc_device.cuh"
@@ -37,26 +48,50 @@ enum Epilogue {
 
 constexpr int kKSlots = 6;  // RK4 k1..k4 (persistent) + two scratch slots for spc_rhs_rk
 
-struct KArgs {
+// One system of a batch.
+struct SysDesc {
   SysConst sc;
-  // state, structure of arrays, original index order
+  int pool_p0;            // first pool slot
+  int dense_p0;           // first dense index in the current layout
+  int c0;                 // first global cell in the current layout
+  int is_vortex;          // natural frequencies in the phase drift
+  uint32_t system_id;     // Philox counter word
+  uint64_t seed;          // Philox key
+  unsigned long long step;     // steps taken before the current call (Philox counter)
+  long long remaining;    // steps the system may still take (serving budget)
+  int budget;             // steps of the current call it takes; later steps leave it frozen
+};
+
+struct KArgs {
+  const SysDesc *sys;
+  int nsys;
+  int n_active;                      // dense particles
+  int ncell_total;
+  const int *sys_of_p;               // dense index -> system
+  const int *sys_of_c;               // global cell -> system
+  // state pool (structure of arrays)
   double *x, *y, *phi;
   const double *omega;
   double *kx[kKSlots], *ky[kKSlots], *kphi[kKSlots];
-  // stage (original order)
+  // stage (dense order)
   double *st_x, *st_y, *st_phi;
-  uint32_t *keys, *vals;             // unsorted (key, index)
+  uint32_t *keys, *vals;             // unsorted (global cell key, dense index)
   const uint32_t *skeys, *svals;     // sorted
   int *cell_start;
   // cell order
   double *sx, *sy, *sphi;
   float2 *fxy;                       // prefilter coordinates relative to the cell origin
   float2 *cs;                        // FP32C: (cos phi, sin phi)
-  int *pidx;                         // original index of cell-order slot p
+  int *pidx;                         // pool slot of cell-order slot p
   double *dphi_s;                    // SRK pass 1 phase rate, cell order
   float *dphi_f;                     // same, float (FP32C)
   int *cnt_s;                        // n_i, cell order
-  // parity outputs (original order)
+  uint32_t *nbmask;                  // FP32C: pass-1 neighbour bitmasks [word][n_active], or null
+  uint32_t *hist;                    // radix histogram table (zeroed by k_gather)
+  int hist_len;
+  const int *ap_cells;               // global cells of the all-pairs systems
+  int n_ap;
+  // parity / diagnostics outputs, indexed by pool slot
   double *out_d, *out_a, *out_r;
   int *out_cnt;
   const long long *list_off;
@@ -64,17 +99,10 @@ struct KArgs {
   // stepping
   double dt;
   int kq_out;                        // k slot written by kEpiRkK / kEpiRk4Combine (k4)
-  const double *noise;               // injected normals of this step, or null for Philox
+  const double *noise;               // injected normals of this step (pool-indexed), or null
   int noise_m;                       // normals per particle
-  uint64_t seed;
-  uint32_t system_id;
-  const unsigned long long *step_base;  // device step counter
-  int step_off;                      // this step = *step_base + step_off
-  int is_vortex;
+  int step_off;                      // this step = sys.step + step_off
   unsigned long long *clamped;
-  uint32_t *hist;                    // radix histogram table (zeroed by k_gather)
-  int hist_len;
-  uint32_t *nbmask;                  // FP32C: pass-1 neighbour bitmasks [word][n], or null
 };
 
 // ---------------------------------------------------------------------------
@@ -91,50 +119,50 @@ constexpr int kMaxHistBits = 11;
 __global__ void __launch_bounds__(kStageThreads)
     k_stage(KArgs a, int rk_form, int kq, double kcdt, int hist_bits, uint32_t *hist) {
   __shared__ uint32_t h[1 << kMaxHistBits];
-  const SysConst &sc = a.sc;
   const int R = 1 << hist_bits;
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int d = blockIdx.x * blockDim.x + threadIdx.x;
   if (hist_bits > 0) {
-    for (int d = threadIdx.x; d < R; d += blockDim.x) h[d] = 0;
+    for (int k = threadIdx.x; k < R; k += blockDim.x) h[k] = 0;
     __syncthreads();
   }
-  if (i < sc.n) {
-    double x = a.x[i], y = a.y[i], ph = a.phi[i];
+  if (d < a.n_active) {
+    const SysDesc &sd = a.sys[a.sys_of_p[d]];
+    const SysConst &sc = sd.sc;
+    const int q = sd.pool_p0 + (d - sd.dense_p0);
+    double x = a.x[q], y = a.y[q], ph = a.phi[q];
     if (rk_form) {
-      const double kx = kq >= 0 ? a.kx[kq][i] : 0.0;
-      const double ky = kq >= 0 ? a.ky[kq][i] : 0.0;
-      const double kp = kq >= 0 ? a.kphi[kq][i] : 0.0;
+      const double kx = kq >= 0 ? a.kx[kq][q] : 0.0;
+      const double ky = kq >= 0 ? a.ky[kq][q] : 0.0;
+      const double kp = kq >= 0 ? a.kphi[kq][q] : 0.0;
       x = dadd(x, dmul(kcdt, kx));
       y = dadd(y, dmul(kcdt, ky));
       ph = dadd(ph, dmul(kcdt, kp));
     }
+    uint32_t key;
     if (sc.allpairs) {
       // all pairs use the unwrapped stage positions (ChimeraSystem.cpp:135-153)
-      a.sx[i] = x;
-      a.sy[i] = y;
-      a.sphi[i] = ph;
-      a.pidx[i] = i;
+      key = (uint32_t)sd.c0;
     } else {
       wrap_if_outside(sc, x, y);
       int clamped = 0;
       const int cx = cell_coord(sc, x, clamped);
       const int cy = cell_coord(sc, y, clamped);
       if (clamped) atomicAdd(a.clamped, 1ull);
-      a.st_x[i] = x;
-      a.st_y[i] = y;
-      a.st_phi[i] = ph;
-      const uint32_t key = (uint32_t)(cy * sc.nc + cx);
-      a.keys[i] = key;
-      a.vals[i] = (uint32_t)i;
-      if (hist_bits > 0) atomicAdd(&h[key & (R - 1)], 1u);
+      key = (uint32_t)(sd.c0 + cy * sc.nc + cx);
     }
+    a.st_x[d] = x;
+    a.st_y[d] = y;
+    a.st_phi[d] = ph;
+    a.keys[d] = key;
+    a.vals[d] = (uint32_t)d;
+    if (hist_bits > 0) atomicAdd(&h[key & (R - 1)], 1u);
   }
   if (hist_bits > 0) {
     __syncthreads();
     // a block of 256 lies inside one sort tile of 2048
     uint32_t *row = hist + (size_t)(blockIdx.x * blockDim.x / kSortTile) * R;
-    for (int d = threadIdx.x; d < R; d += blockDim.x)
-      if (h[d]) atomicAdd(&row[d], h[d]);
+    for (int k = threadIdx.x; k < R; k += blockDim.x)
+      if (h[k]) atomicAdd(&row[k], h[k]);
   }
 }
 
@@ -148,36 +176,31 @@ __device__ __forceinline__ float reduced_phase_f(double ph) {
 template <int PREC>
 __global__ void k_gather(KArgs a) {
   const int p = blockIdx.x * blockDim.x + threadIdx.x;
-  const SysConst &sc = a.sc;
-  if (p > sc.n) return;
+  const int n = a.n_active;
+  if (p > n) return;
   // the cell start table of the sorted keys (one thread per slot and one past the end)
-  cell_bounds_at(a.skeys, sc.n, sc.ncell, a.cell_start, p);
+  cell_bounds_at(a.skeys, n, a.ncell_total, a.cell_start, p);
   // leave the first-digit histogram table zero for the next stage kernel
-  for (int k = p; k < a.hist_len; k += sc.n + 1) a.hist[k] = 0u;
-  if (p == sc.n) return;
-  const int i = (int)a.svals[p];
-  const int key = (int)a.skeys[p];
-  const int cx = key % sc.nc, cy = key / sc.nc;
-  const double x = a.st_x[i], y = a.st_y[i], ph = a.st_phi[i];
+  for (int k = p; k < a.hist_len; k += n + 1) a.hist[k] = 0u;
+  if (p == n) return;
+  const int d = (int)a.svals[p];
+  const SysDesc &sd = a.sys[a.sys_of_p[d]];
+  const SysConst &sc = sd.sc;
+  const double x = a.st_x[d], y = a.st_y[d], ph = a.st_phi[d];
   a.sx[p] = x;
   a.sy[p] = y;
   a.sphi[p] = ph;
-  a.pidx[p] = i;
-  a.fxy[p] = make_float2((float)(x - (double)cx * sc.cell), (float)(y - (double)cy * sc.cell));
+  a.pidx[p] = sd.pool_p0 + (d - sd.dense_p0);
+  if (!sc.allpairs) {
+    const int key = (int)a.skeys[p] - sd.c0;
+    const int cx = key % sc.nc, cy = key / sc.nc;
+    a.fxy[p] = make_float2((float)(x - (double)cx * sc.cell), (float)(y - (double)cy * sc.cell));
+  }
   if constexpr (PREC == kPrecFP32C) {
     float s, c;
     sincosf(reduced_phase_f(ph), &s, &c);
     a.cs[p] = make_float2(c, s);
   }
-}
-
-// FP32C: in the all-pairs layout the slot is the particle itself.
-__global__ void k_fill_cs(KArgs a) {
-  const int p = blockIdx.x * blockDim.x + threadIdx.x;
-  if (p >= a.sc.n) return;
-  float s, c;
-  sincosf(reduced_phase_f(a.sphi[p]), &s, &c);
-  a.cs[p] = make_float2(c, s);
 }
 
 // ---------------------------------------------------------------------------
@@ -220,9 +243,10 @@ struct ILane {
 };
 
 template <int PREC, int KIND>
-__device__ __forceinline__ void accept_pair(const KArgs &a, const ILane &il, Acc<PREC> &acc, int pj,
-                                            float cjc, float cjs, float dphij_f, long long &wpos) {
-  const SysConst &sc = a.sc;
+__device__ __forceinline__ void accept_pair(const KArgs &a, const SysDesc &sd, const ILane &il,
+                                            Acc<PREC> &acc, int pj, float cjc, float cjs,
+                                            float dphij_f, long long &wpos) {
+  const SysConst &sc = sd.sc;
   if constexpr (KIND == kKindSin) {
     if constexpr (PREC == kPrecFP64) {
       // alignment_force_[i] += sin(phi_j - phi_i - alpha_) (ChimeraSystem.cpp:412)
@@ -245,7 +269,7 @@ __device__ __forceinline__ void accept_pair(const KArgs &a, const ILane &il, Acc
     }
     acc.n++;
   } else {
-    if (a.list_idx) a.list_idx[wpos++] = a.pidx[pj];
+    if (a.list_idx) a.list_idx[wpos++] = a.pidx[pj] - sd.pool_p0;
     if constexpr (PREC == kPrecFP64) {
       if (a.out_r) {
         acc.s0 += cos(a.sphi[pj]);
@@ -256,31 +280,34 @@ __device__ __forceinline__ void accept_pair(const KArgs &a, const ILane &il, Acc
   }
 }
 
-__device__ __forceinline__ double noise_at(const KArgs &a, int i, int k, double z0, double z1) {
-  if (a.noise) return a.noise[(size_t)i * a.noise_m + k];
+__device__ __forceinline__ double noise_at(const KArgs &a, int q, int k, double z0, double z1) {
+  if (a.noise) return a.noise[(size_t)q * a.noise_m + k];
   return k == 0 ? z0 : z1;
 }
 
-// Fused epilogue for particle i (original index) at cell-order slot p.
+// Fused epilogue for the particle in pool slot q (system sd) at cell-order slot p.
 template <int PREC, int KIND>
-__device__ void epilogue(const KArgs &a, int epi, const ILane &il, Acc<PREC> &acc, int i) {
-  const SysConst &sc = a.sc;
+__device__ void epilogue(const KArgs &a, int epi, const SysDesc &sd, const ILane &il,
+                         Acc<PREC> &acc, int q) {
+  const SysConst &sc = sd.sc;
   const int p = il.p;
   if constexpr (KIND == kKindNb) {
-    if (epi == kEpiCount) a.out_cnt[i] = acc.n;
+    if (epi == kEpiCount) a.out_cnt[q] = acc.n;
     if (epi == kEpiLocalOrder) {
       const double re = acc.s0 + cos(il.phi), im = acc.s1 + sin(il.phi);
-      a.out_r[i] = sqrt(re * re + im * im) / (double)(acc.n + 1);
+      a.out_r[q] = sqrt(re * re + im * im) / (double)(acc.n + 1);
     }
     return;
   }
+  // past its step budget a system is frozen: no persistent state changes
+  const bool live = a.step_off < sd.budget;
+  const int i = q - sd.pool_p0;  // index within the system (Philox counter)
+  const unsigned long long step = sd.step + (unsigned long long)a.step_off;
   double z0 = 0.0, z1 = 0.0;
-  const bool draws = (epi == kEpiEuler || epi == kEpiEulerPtr || epi == kEpiSrk2) && !a.noise;
+  const bool draws = (epi == kEpiEuler || epi == kEpiEulerPtr || epi == kEpiSrk2) && !a.noise && live;
   const double dt = a.dt;
   if constexpr (PREC == kPrecFP64) {
-    if (draws)
-      philox_normal2(a.seed, a.system_id, *a.step_base + (unsigned long long)a.step_off,
-                     (uint32_t)i, z0, z1);
+    if (draws) philox_normal2(sd.seed, sd.system_id, step, (uint32_t)i, z0, z1);
     const double cph = cos(il.phi), sph = sin(il.phi);
     const double d0 = dmul(sc.v0, cph), d1 = dmul(sc.v0, sph);  // v_0_ * cos(phi_i) (:419-420)
     if constexpr (KIND == kKindSin) {
@@ -288,41 +315,47 @@ __device__ void epilogue(const KArgs &a, int epi, const ILane &il, Acc<PREC> &ac
       const bool has = acc.n != 0;
       const double rate = has ? ddiv(dmul(sc.sigma, acc.s0), (double)acc.n) : 0.0;
       if (epi == kEpiRkK || epi == kEpiRk4Combine) {
-        const int q = a.kq_out;
-        a.kx[q][i] = d0;
-        a.ky[q][i] = d1;
-        if (has) a.kphi[q][i] = rate;  // otherwise k_next keeps its value (H5)
+        if (!live) return;
+        const int k = a.kq_out;
+        a.kx[k][q] = d0;
+        a.ky[k][q] = d1;
+        if (has) a.kphi[k][q] = rate;  // otherwise k_next keeps its value (H5)
         if (epi == kEpiRk4Combine) {
           // RungeKutta4Stepper.cpp:52-54
-          const double k4p = a.kphi[q][i];
-          double xs = a.x[i], ys = a.y[i], ps = a.phi[i];
-          const double sx_ = dadd(dadd(dadd(a.kx[0][i], dmul(2.0, a.kx[1][i])), dmul(2.0, a.kx[2][i])), d0);
-          const double sy_ = dadd(dadd(dadd(a.ky[0][i], dmul(2.0, a.ky[1][i])), dmul(2.0, a.ky[2][i])), d1);
-          const double sp_ = dadd(dadd(dadd(a.kphi[0][i], dmul(2.0, a.kphi[1][i])), dmul(2.0, a.kphi[2][i])), k4p);
+          const double k4p = a.kphi[k][q];
+          double xs = a.x[q], ys = a.y[q], ps = a.phi[q];
+          const double sx_ = dadd(dadd(dadd(a.kx[0][q], dmul(2.0, a.kx[1][q])), dmul(2.0, a.kx[2][q])), d0);
+          const double sy_ = dadd(dadd(dadd(a.ky[0][q], dmul(2.0, a.ky[1][q])), dmul(2.0, a.ky[2][q])), d1);
+          const double sp_ = dadd(dadd(dadd(a.kphi[0][q], dmul(2.0, a.kphi[1][q])), dmul(2.0, a.kphi[2][q])), k4p);
           xs = dadd(xs, ddiv(dmul(sx_, dt), 6.0));
           ys = dadd(ys, ddiv(dmul(sy_, dt), 6.0));
           ps = dadd(ps, dmul(ddiv(sp_, 6.0), dt));
-          a.x[i] = wrap_1d(xs, sc.rL, sc.L);  // SimulationEngine.cpp:154
-          a.y[i] = wrap_1d(ys, sc.rL, sc.L);
-          a.phi[i] = ps;
+          a.x[q] = wrap_1d(xs, sc.rL, sc.L);  // SimulationEngine.cpp:154
+          a.y[q] = wrap_1d(ys, sc.rL, sc.L);
+          a.phi[q] = ps;
         }
       } else if (epi == kEpiEuler) {
-        // StochasticEulerStepper.hpp:43-45 with AddNoise (ChimeraSystem.cpp:927-930)
+        if (!live) return;
+        // StochasticEulerStepper.hpp:43-45 with AddNoise (ChimeraSystem.cpp:927-930);
+        // a vortex system adds its frequency to the phase drift as the
+        // SRK-Ptr stepper does (StochasticRungeKuttaStepperPtr.hpp:65)
         const double sdt = dsqrt(dt);
-        const double sto = dmul(dsqrt(dmul(2.0, sc.D)), noise_at(a, i, 0, z0, z1));
-        const double xs = dadd(a.x[i], dadd(dmul(dt, d0), dmul(sdt, 0.0)));
-        const double ys = dadd(a.y[i], dadd(dmul(dt, d1), dmul(sdt, 0.0)));
-        a.phi[i] = dadd(a.phi[i], dadd(dmul(dt, rate), dmul(sdt, sto)));
-        a.x[i] = wrap_1d(xs, sc.rL, sc.L);
-        a.y[i] = wrap_1d(ys, sc.rL, sc.L);
+        const double sto = dmul(dsqrt(dmul(2.0, sc.D)), noise_at(a, q, 0, z0, z1));
+        const double xs = dadd(a.x[q], dadd(dmul(dt, d0), dmul(sdt, 0.0)));
+        const double ys = dadd(a.y[q], dadd(dmul(dt, d1), dmul(sdt, 0.0)));
+        const double drift = sd.is_vortex ? dadd(a.omega[q], rate) : rate;
+        a.phi[q] = dadd(a.phi[q], dadd(dmul(dt, drift), dmul(sdt, sto)));
+        a.x[q] = wrap_1d(xs, sc.rL, sc.L);
+        a.y[q] = wrap_1d(ys, sc.rL, sc.L);
       } else if (epi == kEpiEulerPtr) {
+        if (!live) return;
         // StochasticEulerStepperPtr.hpp:44-51
-        const double dW = dmul(dsqrt(dt), noise_at(a, i, 0, z0, z1));
-        const double xs = dadd(a.x[i], dmul(d0, dt));
-        const double ys = dadd(a.y[i], dmul(d1, dt));
-        a.phi[i] = dadd(a.phi[i], dadd(dmul(rate, dt), dmul(dsqrt(dmul(2.0, sc.D)), dW)));
-        a.x[i] = wrap_1d(xs, sc.rL, sc.L);
-        a.y[i] = wrap_1d(ys, sc.rL, sc.L);
+        const double dW = dmul(dsqrt(dt), noise_at(a, q, 0, z0, z1));
+        const double xs = dadd(a.x[q], dmul(d0, dt));
+        const double ys = dadd(a.y[q], dmul(d1, dt));
+        a.phi[q] = dadd(a.phi[q], dadd(dmul(rate, dt), dmul(dsqrt(dmul(2.0, sc.D)), dW)));
+        a.x[q] = wrap_1d(xs, sc.rL, sc.L);
+        a.y[q] = wrap_1d(ys, sc.rL, sc.L);
       } else if (epi == kEpiSrk1) {
         a.dphi_s[p] = rate;  // derivative is zero-filled each step: 0 when isolated
         a.cnt_s[p] = acc.n;
@@ -332,29 +365,30 @@ __device__ void epilogue(const KArgs &a, int epi, const ILane &il, Acc<PREC> &ac
       const double A1 = dadd(acc.s1, dmul(dmul(-2.0, sc.D), il.dphi));
       const double d2 = il.dphi;
       if (epi == kEpiSrk2Out) {
-        a.out_d[3 * (size_t)i] = d0;
-        a.out_d[3 * (size_t)i + 1] = d1;
-        a.out_d[3 * (size_t)i + 2] = d2;
-        a.out_a[2 * (size_t)i] = A0;
-        a.out_a[2 * (size_t)i + 1] = A1;
+        a.out_d[3 * (size_t)q] = d0;
+        a.out_d[3 * (size_t)q + 1] = d1;
+        a.out_d[3 * (size_t)q + 2] = d2;
+        a.out_a[2 * (size_t)q] = A0;
+        a.out_a[2 * (size_t)q + 1] = A1;
       } else {
+        if (!live) return;
         // StochasticRungeKuttaStepper.hpp:44-55 (+ omega: StochasticRungeKuttaStepperPtr.hpp:65)
-        const double U1 = noise_at(a, i, 0, z0, z1), U2 = noise_at(a, i, 1, z0, z1);
+        const double U1 = noise_at(a, q, 0, z0, z1), U2 = noise_at(a, q, 1, z0, z1);
         const double sdt = dsqrt(dt);
         const double dW = dmul(U1, sdt);
         const double dZ = dmul(dmul(dmul(0.5, dt), sdt), dadd(U1, ddiv(U2, dsqrt(3.0))));
         const double D = sc.D;
         const double s2D = dsqrt(dmul(2.0, D));
         const double dtdt_x = dmul(dmul(dmul(0.5, dadd(dmul(d2, d1), dmul(D, d0))), dt), dt);
-        const double xs = dadd(a.x[i], dsub(dsub(dmul(d0, dt), dmul(dmul(s2D, d1), dZ)), dtdt_x));
+        const double xs = dadd(a.x[q], dsub(dsub(dmul(d0, dt), dmul(dmul(s2D, d1), dZ)), dtdt_x));
         const double dtdt_y = dmul(dmul(dmul(0.5, dsub(dmul(d2, d0), dmul(D, d1))), dt), dt);
-        const double ys = dadd(a.y[i], dadd(dadd(dmul(d1, dt), dmul(dmul(s2D, d0), dZ)), dtdt_y));
-        const double drift = a.is_vortex ? dmul(dadd(a.omega[i], d2), dt) : dmul(d2, dt);
-        const double ps = dadd(a.phi[i], dadd(dadd(dadd(drift, dmul(s2D, dW)), dmul(A0, dZ)),
+        const double ys = dadd(a.y[q], dadd(dadd(dmul(d1, dt), dmul(dmul(s2D, d0), dZ)), dtdt_y));
+        const double drift = sd.is_vortex ? dmul(dadd(a.omega[q], d2), dt) : dmul(d2, dt);
+        const double ps = dadd(a.phi[q], dadd(dadd(dadd(drift, dmul(s2D, dW)), dmul(A0, dZ)),
                                               dmul(dmul(dmul(0.5, A1), dt), dt)));
-        a.x[i] = wrap_1d(xs, sc.rL, sc.L);
-        a.y[i] = wrap_1d(ys, sc.rL, sc.L);
-        a.phi[i] = ps;
+        a.x[q] = wrap_1d(xs, sc.rL, sc.L);
+        a.y[q] = wrap_1d(ys, sc.rL, sc.L);
+        a.phi[q] = ps;
       }
     }
   } else {
@@ -362,8 +396,7 @@ __device__ void epilogue(const KArgs &a, int epi, const ILane &il, Acc<PREC> &ac
     // double positions and phase.
     if (draws) {
       float f0, f1;
-      philox_normal2_f(a.seed, a.system_id, *a.step_base + (unsigned long long)a.step_off,
-                       (uint32_t)i, f0, f1);
+      philox_normal2_f(sd.seed, sd.system_id, step, (uint32_t)i, f0, f1);
       z0 = f0;
       z1 = f1;
     }
@@ -376,27 +409,30 @@ __device__ void epilogue(const KArgs &a, int epi, const ILane &il, Acc<PREC> &ac
       const bool has = acc.n != 0;
       const float rate = has ? (float)sc.sigma * acc.s0 / (float)acc.n : 0.0f;
       if (epi == kEpiRkK || epi == kEpiRk4Combine) {
-        const int q = a.kq_out;
-        a.kx[q][i] = (double)d0;
-        a.ky[q][i] = (double)d1;
-        if (has) a.kphi[q][i] = (double)rate;
+        if (!live) return;
+        const int k = a.kq_out;
+        a.kx[k][q] = (double)d0;
+        a.ky[k][q] = (double)d1;
+        if (has) a.kphi[k][q] = (double)rate;
         if (epi == kEpiRk4Combine) {
-          const float k4p = (float)a.kphi[q][i];
-          const float sx_ = (float)a.kx[0][i] + 2.0f * (float)a.kx[1][i] + 2.0f * (float)a.kx[2][i] + d0;
-          const float sy_ = (float)a.ky[0][i] + 2.0f * (float)a.ky[1][i] + 2.0f * (float)a.ky[2][i] + d1;
-          const float sp_ = (float)a.kphi[0][i] + 2.0f * (float)a.kphi[1][i] + 2.0f * (float)a.kphi[2][i] + k4p;
+          const float k4p = (float)a.kphi[k][q];
+          const float sx_ = (float)a.kx[0][q] + 2.0f * (float)a.kx[1][q] + 2.0f * (float)a.kx[2][q] + d0;
+          const float sy_ = (float)a.ky[0][q] + 2.0f * (float)a.ky[1][q] + 2.0f * (float)a.ky[2][q] + d1;
+          const float sp_ = (float)a.kphi[0][q] + 2.0f * (float)a.kphi[1][q] + 2.0f * (float)a.kphi[2][q] + k4p;
           const float sixth = dtf / 6.0f;
-          a.x[i] = wrap_1d(a.x[i] + (double)(sx_ * sixth), sc.rL, sc.L);
-          a.y[i] = wrap_1d(a.y[i] + (double)(sy_ * sixth), sc.rL, sc.L);
-          a.phi[i] = a.phi[i] + (double)(sp_ * sixth);
+          a.x[q] = wrap_1d(a.x[q] + (double)(sx_ * sixth), sc.rL, sc.L);
+          a.y[q] = wrap_1d(a.y[q] + (double)(sy_ * sixth), sc.rL, sc.L);
+          a.phi[q] = a.phi[q] + (double)(sp_ * sixth);
         }
       } else if (epi == kEpiEuler || epi == kEpiEulerPtr) {
-        const float xi = (float)noise_at(a, i, 0, z0, z1);
+        if (!live) return;
+        const float xi = (float)noise_at(a, q, 0, z0, z1);
         const float sdt = sqrtf(dtf);
         const float s2D = sqrtf(2.0f * D);
-        a.x[i] = wrap_1d(a.x[i] + (double)(dtf * d0), sc.rL, sc.L);
-        a.y[i] = wrap_1d(a.y[i] + (double)(dtf * d1), sc.rL, sc.L);
-        a.phi[i] = a.phi[i] + (double)(dtf * rate + sdt * s2D * xi);
+        const float drift = (epi == kEpiEuler && sd.is_vortex) ? (float)a.omega[q] + rate : rate;
+        a.x[q] = wrap_1d(a.x[q] + (double)(dtf * d0), sc.rL, sc.L);
+        a.y[q] = wrap_1d(a.y[q] + (double)(dtf * d1), sc.rL, sc.L);
+        a.phi[q] = a.phi[q] + (double)(dtf * drift + sdt * s2D * xi);
       } else if (epi == kEpiSrk1) {
         a.dphi_s[p] = (double)rate;
         a.dphi_f[p] = rate;
@@ -409,44 +445,45 @@ __device__ void epilogue(const KArgs &a, int epi, const ILane &il, Acc<PREC> &ac
       const float A1 = acc.s1 * inv_n + (-2.0f * D) * il.dphif;
       const float d2 = il.dphif;
       if (epi == kEpiSrk2Out) {
-        a.out_d[3 * (size_t)i] = (double)d0;
-        a.out_d[3 * (size_t)i + 1] = (double)d1;
-        a.out_d[3 * (size_t)i + 2] = (double)d2;
-        a.out_a[2 * (size_t)i] = (double)A0;
-        a.out_a[2 * (size_t)i + 1] = (double)A1;
+        a.out_d[3 * (size_t)q] = (double)d0;
+        a.out_d[3 * (size_t)q + 1] = (double)d1;
+        a.out_d[3 * (size_t)q + 2] = (double)d2;
+        a.out_a[2 * (size_t)q] = (double)A0;
+        a.out_a[2 * (size_t)q + 1] = (double)A1;
       } else {
-        const float U1 = (float)noise_at(a, i, 0, z0, z1), U2 = (float)noise_at(a, i, 1, z0, z1);
+        if (!live) return;
+        const float U1 = (float)noise_at(a, q, 0, z0, z1), U2 = (float)noise_at(a, q, 1, z0, z1);
         const float sdt = sqrtf(dtf);
         const float dW = U1 * sdt;
         const float dZ = 0.5f * dtf * sdt * (U1 + U2 * 0.57735026918962576f);
         const float dx = d0 * dtf - s2D * d1 * dZ - 0.5f * (d2 * d1 + D * d0) * dtf * dtf;
         const float dy = d1 * dtf + s2D * d0 * dZ + 0.5f * (d2 * d0 - D * d1) * dtf * dtf;
-        const float drift = (a.is_vortex ? (float)a.omega[i] + d2 : d2) * dtf;
+        const float drift = (sd.is_vortex ? (float)a.omega[q] + d2 : d2) * dtf;
         const float dp = drift + s2D * dW + A0 * dZ + 0.5f * A1 * dtf * dtf;
-        a.x[i] = wrap_1d(a.x[i] + (double)dx, sc.rL, sc.L);
-        a.y[i] = wrap_1d(a.y[i] + (double)dy, sc.rL, sc.L);
-        a.phi[i] = a.phi[i] + (double)dp;
+        a.x[q] = wrap_1d(a.x[q] + (double)dx, sc.rL, sc.L);
+        a.y[q] = wrap_1d(a.y[q] + (double)dy, sc.rL, sc.L);
+        a.phi[q] = a.phi[q] + (double)dp;
       }
     }
   }
 }
 
 template <int PREC, int KIND>
-__device__ __forceinline__ void load_i(const KArgs &a, ILane &il, int p, bool valid) {
+__device__ __forceinline__ void load_i(const KArgs &a, const SysConst &sc, ILane &il, int p, bool valid) {
   il.p = p;
   il.valid = valid;
   if (!valid) return;
   il.x = a.sx[p];
   il.y = a.sy[p];
   il.phi = a.sphi[p];
-  if (!a.sc.allpairs) {
+  if (!sc.allpairs) {
     const float2 f = a.fxy[p];
     il.fx = f.x;
     il.fy = f.y;
   }
   if constexpr (PREC == kPrecFP32C) {
     float s, c;
-    sincosf(reduced_phase_f(il.phi) + (float)a.sc.alpha, &s, &c);
+    sincosf(reduced_phase_f(il.phi) + (float)sc.alpha, &s, &c);
     il.ca = c;
     il.sa = s;
   }
@@ -464,26 +501,26 @@ constexpr int kPassWarps = 4;
 constexpr int kPassThreads = kPassWarps * kWarp;
 constexpr int kIPL = 2;  // i particles per lane: a warp covers a 64-particle cell tile
 
-// One warp per cell tile: up to 64 particles of cell c, two per lane; the
-// warp walks the 9 stencil cells in the reference's order
-// (ChimeraSystem.cpp:39-44) and, within each, the members in ascending index
-// (cell order), staging 32 candidates at a time in shared memory.  The float
-// prefilter decides pairs far from the cutoff; pairs within a relative 3e-5 of
-// rho^2 are decided by the reference's own FP64 test, so neighbour sets are
-// exactly the reference's.
+// Neighbour diagnostics (counts, lists in visiting order, local order
+// parameter): one warp per cell tile, two particles per lane, the 9 stencil
+// cells in the reference's order (ChimeraSystem.cpp:39-44) and within each the
+// members in ascending index, 32 candidates at a time through shared memory.
+// Decisions as everywhere: float prefilter, the reference's FP64 test near the
+// cutoff.
 template <int PREC, int KIND>
 __global__ void __launch_bounds__(kPassThreads) k_cell_pass(KArgs a, int epi) {
   __shared__ float4 stage[kPassWarps][kWarp];
-  __shared__ float stage_d[kPassWarps][kWarp];
   const int w = threadIdx.x / kWarp, lane = threadIdx.x % kWarp;
   const int gwarp = blockIdx.x * kPassWarps + w;
   const int nwarps = gridDim.x * kPassWarps;
-  const SysConst &sc = a.sc;
-  const int nc = sc.nc;
-  const bool exact_all = sc.exact_all != 0;
-  for (int c = gwarp; c < sc.ncell; c += nwarps) {
+  for (int c = gwarp; c < a.ncell_total; c += nwarps) {
+    const SysDesc &sd = a.sys[a.sys_of_c[c]];
+    const SysConst &sc = sd.sc;
+    if (sc.allpairs) continue;
+    const int nc = sc.nc;
+    const bool exact_all = sc.exact_all != 0;
     const int cb = a.cell_start[c], ce = a.cell_start[c + 1];
-    const int cx = c % nc, cy = c / nc;
+    const int cl = c - sd.c0, cx = cl % nc, cy = cl / nc;
     for (int base = cb; base < ce; base += kIPL * kWarp) {
       ILane il[kIPL];
       Acc<PREC> acc[kIPL];
@@ -491,14 +528,13 @@ __global__ void __launch_bounds__(kPassThreads) k_cell_pass(KArgs a, int epi) {
 #pragma unroll
       for (int k = 0; k < kIPL; ++k) {
         const int p = base + k * kWarp + lane;
-        load_i<PREC, KIND>(a, il[k], p, p < ce);
+        load_i<PREC, KIND>(a, sc, il[k], p, p < ce);
         acc[k].init();
-        wpos[k] = (KIND == kKindNb && a.list_idx && il[k].valid) ? a.list_off[a.pidx[p]] : 0;
+        wpos[k] = (a.list_idx && il[k].valid) ? a.list_off[a.pidx[p]] : 0;
       }
       for (int q = 0; q < 9; ++q) {
         const int ox = (q % 3) - 1, oy = (q / 3) - 1;  // {-1,-1},{0,-1},{1,-1},{-1,0},...
-        const int jx = adjust_cell(cx + ox, nc), jy = adjust_cell(cy + oy, nc);
-        const int cj = jy * nc + jx;
+        const int cj = sd.c0 + adjust_cell(cy + oy, nc) * nc + adjust_cell(cx + ox, nc);
         const int ja = a.cell_start[cj], jb = a.cell_start[cj + 1];
         const float shx = (float)ox * sc.cell_f, shy = (float)oy * sc.cell_f;
         for (int jbase = ja; jbase < jb; jbase += kWarp) {
@@ -506,20 +542,12 @@ __global__ void __launch_bounds__(kPassThreads) k_cell_pass(KArgs a, int epi) {
           __syncwarp();
           if (pl < jb) {
             const float2 f = a.fxy[pl];
-            float cc = 0.0f, ss = 0.0f;
-            if constexpr (PREC == kPrecFP32C) {
-              const float2 t = a.cs[pl];
-              cc = t.x;
-              ss = t.y;
-              if constexpr (KIND == kKindCos2) stage_d[w][lane] = a.dphi_f[pl];
-            }
-            stage[w][lane] = make_float4(f.x + shx, f.y + shy, cc, ss);
+            stage[w][lane] = make_float4(f.x + shx, f.y + shy, 0.0f, 0.0f);
           }
           __syncwarp();
           const int cnt = min(kWarp, jb - jbase);
           for (int t = 0; t < cnt; ++t) {
             const float4 cj4 = stage[w][t];
-            const float dj = (PREC == kPrecFP32C && KIND == kKindCos2) ? stage_d[w][t] : 0.0f;
             const int pj = jbase + t;
 #pragma unroll
             for (int k = 0; k < kIPL; ++k) {
@@ -529,7 +557,7 @@ __global__ void __launch_bounds__(kPassThreads) k_cell_pass(KArgs a, int epi) {
               if (exact_all || d2 <= sc.hi2) {
                 const bool in = (!exact_all && d2 < sc.lo2) ||
                                 exact_within(sc, il[k].x, il[k].y, a.sx[pj], a.sy[pj]);
-                if (in) accept_pair<PREC, KIND>(a, il[k], acc[k], pj, cj4.z, cj4.w, dj, wpos[k]);
+                if (in) accept_pair<PREC, KIND>(a, sd, il[k], acc[k], pj, 0.0f, 0.0f, 0.0f, wpos[k]);
               }
             }
           }
@@ -537,13 +565,14 @@ __global__ void __launch_bounds__(kPassThreads) k_cell_pass(KArgs a, int epi) {
       }
 #pragma unroll
       for (int k = 0; k < kIPL; ++k)
-        if (il[k].valid) epilogue<PREC, KIND>(a, epi, il[k], acc[k], a.pidx[il[k].p]);
+        if (il[k].valid) epilogue<PREC, KIND>(a, epi, sd, il[k], acc[k], a.pidx[il[k].p]);
     }
   }
 }
 
-// All pairs (rho > L/4): ChimeraSystem.cpp:117-255.  One thread per i in
-// index order, j ascending, exact FP64 test on unwrapped stage positions.
+// All pairs (rho > L/4): ChimeraSystem.cpp:117-255.  One CTA per all-pairs
+// system (its particles form one cell, in index order); one thread per i,
+// j ascending, exact FP64 test on unwrapped stage positions.
 constexpr int kAllPairsThreads = 128;
 
 template <int PREC, int KIND>
@@ -551,45 +580,92 @@ __global__ void __launch_bounds__(kAllPairsThreads) k_allpairs_pass(KArgs a, int
   __shared__ double tx[kAllPairsThreads], ty[kAllPairsThreads];
   __shared__ float2 tcs[kAllPairsThreads];
   __shared__ float td[kAllPairsThreads];
-  const SysConst &sc = a.sc;
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  ILane il;
-  Acc<PREC> acc;
-  load_i<PREC, KIND>(a, il, i, i < sc.n);
-  acc.init();
-  long long wpos = (KIND == kKindNb && a.list_idx && il.valid) ? a.list_off[i] : 0;
-  for (int jt = 0; jt < sc.n; jt += kAllPairsThreads) {
-    const int jl = jt + threadIdx.x;
-    __syncthreads();
-    if (jl < sc.n) {
-      tx[threadIdx.x] = a.sx[jl];
-      ty[threadIdx.x] = a.sy[jl];
-      if constexpr (PREC == kPrecFP32C) {
-        tcs[threadIdx.x] = a.cs[jl];
-        if constexpr (KIND == kKindCos2) td[threadIdx.x] = a.dphi_f[jl];
-      }
-    }
-    __syncthreads();
-    const int cnt = min(kAllPairsThreads, sc.n - jt);
-    if (!il.valid) continue;
-    for (int t = 0; t < cnt; ++t) {
-      const int j = jt + t;
-      if (j == i) continue;
-      if (exact_within(sc, il.x, il.y, tx[t], ty[t])) {
-        float cc = 0.0f, ss = 0.0f, dj = 0.0f;
-        if constexpr (PREC == kPrecFP32C) {
-          cc = tcs[t].x;
-          ss = tcs[t].y;
-          if constexpr (KIND == kKindCos2) dj = td[t];
+  for (int w = blockIdx.x; w < a.n_ap; w += gridDim.x) {
+    const int c = a.ap_cells[w];
+    const SysDesc &sd = a.sys[a.sys_of_c[c]];
+    const SysConst &sc = sd.sc;
+    const int cb = a.cell_start[c], ce = a.cell_start[c + 1];
+    for (int ib = cb; ib < ce; ib += kAllPairsThreads) {
+      const int i = ib + threadIdx.x;
+      ILane il;
+      Acc<PREC> acc;
+      load_i<PREC, KIND>(a, sc, il, i, i < ce);
+      acc.init();
+      long long wpos = (a.list_idx && il.valid) ? a.list_off[a.pidx[i]] : 0;
+      for (int jt = cb; jt < ce; jt += kAllPairsThreads) {
+        const int jl = jt + threadIdx.x;
+        __syncthreads();
+        if (jl < ce) {
+          tx[threadIdx.x] = a.sx[jl];
+          ty[threadIdx.x] = a.sy[jl];
+          if constexpr (PREC == kPrecFP32C) {
+            tcs[threadIdx.x] = a.cs[jl];
+            if constexpr (KIND == kKindCos2) td[threadIdx.x] = a.dphi_f[jl];
+          }
         }
-        accept_pair<PREC, KIND>(a, il, acc, j, cc, ss, dj, wpos);
+        __syncthreads();
+        const int cnt = min(kAllPairsThreads, ce - jt);
+        if (!il.valid) continue;
+        for (int t = 0; t < cnt; ++t) {
+          const int j = jt + t;
+          if (j == i) continue;
+          if (exact_within(sc, il.x, il.y, tx[t], ty[t])) {
+            float cc = 0.0f, ss = 0.0f, dj = 0.0f;
+            if constexpr (PREC == kPrecFP32C) {
+              cc = tcs[t].x;
+              ss = tcs[t].y;
+              if constexpr (KIND == kKindCos2) dj = td[t];
+            }
+            accept_pair<PREC, KIND>(a, sd, il, acc, j, cc, ss, dj, wpos);
+          }
+        }
       }
+      if (il.valid) epilogue<PREC, KIND>(a, epi, sd, il, acc, a.pidx[i]);
+      __syncthreads();
     }
   }
-  if (il.valid) epilogue<PREC, KIND>(a, epi, il, acc, i);
 }
 
 // ---------------------------------------------------------------------------
+// Per-call step bookkeeping of every system: the call takes
+// budget = min(nsteps, remaining) steps, after which the system is frozen.
+__global__ void k_begin_call(SysDesc *sys, int nsys, int nsteps) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= nsys) return;
+  const long long r = sys[s].remaining;
+  sys[s].budget = (int)(r < (long long)nsteps ? (r > 0 ? r : 0) : nsteps);
+}
+
+__global__ void k_end_call(SysDesc *sys, int nsys) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= nsys) return;
+  sys[s].step += (unsigned long long)sys[s].budget;
+  sys[s].remaining -= sys[s].budget;
+  sys[s].budget = 0;
+}
+
+// dense index -> system, and global cell -> system, from the layout tables
+__global__ void k_layout_maps(const SysDesc *sys, int nsys, int n_active, int ncell_total,
+                              int *sys_of_p, int *sys_of_c) {
+  const int g = blockIdx.x * blockDim.x + threadIdx.x;
+  if (g < n_active) {
+    int lo = 0, hi = nsys - 1;  // last system with dense_p0 <= g
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) / 2;
+      if (sys[mid].dense_p0 <= g) lo = mid; else hi = mid - 1;
+    }
+    sys_of_p[g] = lo;
+  }
+  if (g < ncell_total) {
+    int lo = 0, hi = nsys - 1;
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) / 2;
+      if (sys[mid].c0 <= g) lo = mid; else hi = mid - 1;
+    }
+    sys_of_c[g] = lo;
+  }
+}
+
 __global__ void k_aos_to_soa(const double *__restrict__ aos, int n, double *x, double *y,
                              double *phi) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -607,8 +683,6 @@ __global__ void k_soa_to_aos(const double *x, const double *y, const double *phi
   aos[3 * (size_t)i + 1] = y[i];
   aos[3 * (size_t)i + 2] = phi[i];
 }
-
-__global__ void k_add_u64(unsigned long long *p, unsigned long long v) { *p += v; }
 
 // Philox normals of steps [first, first + nsteps) in the injection layout.
 __global__ void k_export_noise(uint64_t seed, uint32_t system_id, uint64_t first, int nsteps,
@@ -631,7 +705,7 @@ __global__ void k_philox_kat(U4 c, uint32_t k0, uint32_t k1, uint32_t *out) {
   out[3] = o.w;
 }
 
-// Global order parameter partial sums (FP64): sum cos, sum sin.
+// Global order parameter partial sums (FP64) of phi[0..n): sum cos, sum sin.
 __global__ void k_order_sum(const double *phi, int n, double *out2) {
   __shared__ double sc_[256], ss_[256];
   double c = 0.0, s = 0.0;

@@ -97,6 +97,38 @@ __global__ void __launch_bounds__(kScanThreads)
   }
 }
 
+// For many tiles the scan runs in three steps over groups of kScanGroup tiles:
+// per-(group, digit) sums, a one-block digit-major scan of those sums (the
+// same k_scan_digits with groups in place of tiles), and per-(group, digit)
+// running prefixes written back over the group's tiles.
+constexpr int kScanGroup = 32;
+
+__global__ void k_scan_group_sums(const uint32_t *__restrict__ hist, int ntiles, int bits,
+                                  uint32_t *__restrict__ part) {
+  const int R = 1 << bits;
+  const int d = blockIdx.y * blockDim.x + threadIdx.x, g = blockIdx.x;
+  if (d >= R) return;
+  const int t0 = g * kScanGroup, t1 = min(t0 + kScanGroup, ntiles);
+  uint32_t s = 0;
+  for (int t = t0; t < t1; ++t) s += hist[(size_t)t * R + d];
+  part[(size_t)g * R + d] = s;
+}
+
+__global__ void k_scan_group_apply(uint32_t *__restrict__ hist, int ntiles, int bits,
+                                   const uint32_t *__restrict__ part) {
+  const int R = 1 << bits;
+  const int d = blockIdx.y * blockDim.x + threadIdx.x, g = blockIdx.x;
+  if (d >= R) return;
+  const int t0 = g * kScanGroup, t1 = min(t0 + kScanGroup, ntiles);
+  uint32_t run = part[(size_t)g * R + d];
+  for (int t = t0; t < t1; ++t) {
+    const size_t at = (size_t)t * R + d;
+    const uint32_t v = hist[at];
+    hist[at] = run;
+    run += v;
+  }
+}
+
 // Stable scatter of one digit pass; hist_scanned is the output of k_scan_digits.
 __global__ void __launch_bounds__(kSortThreads)
     k_radix_scatter(const uint32_t *__restrict__ keys_in, const uint32_t *__restrict__ vals_in,

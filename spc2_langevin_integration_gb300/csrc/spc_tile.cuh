@@ -40,14 +40,14 @@ struct Stencil {
   float shx[9], shy[9];
 };
 
-__device__ __forceinline__ void stencil_of(const KArgs &a, int c, Stencil &s) {
-  const SysConst &sc = a.sc;
-  const int nc = sc.nc, cx = c % nc, cy = c / nc;
+__device__ __forceinline__ void stencil_of(const KArgs &a, const SysDesc &sd, int c, Stencil &s) {
+  const SysConst &sc = sd.sc;
+  const int nc = sc.nc, cl = c - sd.c0, cx = cl % nc, cy = cl / nc;
   s.prefix[0] = 0;
 #pragma unroll
   for (int q = 0; q < 9; ++q) {
     const int ox = (q % 3) - 1, oy = (q / 3) - 1;
-    const int cj = adjust_cell(cy + oy, nc) * nc + adjust_cell(cx + ox, nc);
+    const int cj = sd.c0 + adjust_cell(cy + oy, nc) * nc + adjust_cell(cx + ox, nc);
     const int ja = a.cell_start[cj], jb = a.cell_start[cj + 1];
     s.start[q] = ja;
     s.prefix[q + 1] = s.prefix[q] + (jb - ja);
@@ -131,17 +131,19 @@ __global__ void __launch_bounds__(kTileThreads32) k_tile_fp32c(KArgs a, int epi)
   __shared__ float t_s[kTileThreads32], t_c[kTileThreads32], t_s1[kTileThreads32],
       t_c1[kTileThreads32];
   __shared__ int t_n[kTileThreads32];
-  const SysConst &sc = a.sc;
-  const int n_all = sc.n;
+  const int n_all = a.n_active;
   const int tid = threadIdx.x, w = tid / kWarp, lane = tid % kWarp;
-  const float lo2 = sc.lo2, hi2 = sc.hi2;
-  const float band = 0.5f * (hi2 - lo2), mid = 0.5f * (hi2 + lo2);
-  const bool exact_all = sc.exact_all != 0;
-  for (int c = blockIdx.x; c < sc.ncell; c += gridDim.x) {
+  for (int c = blockIdx.x; c < a.ncell_total; c += gridDim.x) {
     const int cb = a.cell_start[c], ce = a.cell_start[c + 1];
     if (cb == ce) continue;
+    const SysDesc &sd = a.sys[a.sys_of_c[c]];
+    const SysConst &sc = sd.sc;
+    if (sc.allpairs) continue;
+    const float lo2 = sc.lo2, hi2 = sc.hi2;
+    const float band = 0.5f * (hi2 - lo2), mid = 0.5f * (hi2 + lo2);
+    const bool exact_all = sc.exact_all != 0;
     Stencil st;
-    stencil_of(a, c, st);
+    stencil_of(a, sd, c, st);
     const int total = st.prefix[9];
     const int rounds = (total + kTileCap - 1) / kTileCap;
     const bool masked = rounds == 1 && a.nbmask != nullptr && !exact_all;
@@ -294,13 +296,13 @@ __global__ void __launch_bounds__(kTileThreads32) k_tile_fp32c(KArgs a, int epi)
       if (tid < gi) {
         const int p = ig + tid;
         ILane il;
-        load_i<kPrecFP32C, KIND>(a, il, p, true);
+        load_i<kPrecFP32C, KIND>(a, sc, il, p, true);
         Acc<kPrecFP32C> acc;
         acc.init();
         acc.s0 = t_s[tid] - t_c[tid];
         acc.s1 = t_s1[tid] - t_c1[tid];
         acc.n = t_n[tid];
-        epilogue<kPrecFP32C, KIND>(a, epi, il, acc, a.pidx[p]);
+        epilogue<kPrecFP32C, KIND>(a, epi, sd, il, acc, a.pidx[p]);
       }
       __syncthreads();
     }
@@ -315,16 +317,18 @@ __global__ void __launch_bounds__(kTileThreads64) k_tile_fp64(KArgs a, int epi) 
   __shared__ double s_d[KIND == kKindCos2 ? kTileCap64 : 1];  // pass 2: phase rate
   __shared__ int s_p[kTileCap64];
   __shared__ uint16_t s_q[kQCap][kTileThreads64];
-  const SysConst &sc = a.sc;
   const int tid = threadIdx.x;
-  const float lo2 = sc.lo2, hi2 = sc.hi2;
-  const float band = 0.5f * (hi2 - lo2), mid = 0.5f * (hi2 + lo2);
-  const bool exact_all = sc.exact_all != 0;
-  for (int c = blockIdx.x; c < sc.ncell; c += gridDim.x) {
+  for (int c = blockIdx.x; c < a.ncell_total; c += gridDim.x) {
     const int cb = a.cell_start[c], ce = a.cell_start[c + 1];
     if (cb == ce) continue;
+    const SysDesc &sd = a.sys[a.sys_of_c[c]];
+    const SysConst &sc = sd.sc;
+    if (sc.allpairs) continue;
+    const float lo2 = sc.lo2, hi2 = sc.hi2;
+    const float band = 0.5f * (hi2 - lo2), mid = 0.5f * (hi2 + lo2);
+    const bool exact_all = sc.exact_all != 0;
     Stencil st;
-    stencil_of(a, c, st);
+    stencil_of(a, sd, c, st);
     const int total = st.prefix[9];
     const int rounds = (total + kTileCap64 - 1) / kTileCap64;
     for (int ig = cb; ig < ce; ig += kTileThreads64) {
@@ -332,7 +336,7 @@ __global__ void __launch_bounds__(kTileThreads64) k_tile_fp64(KArgs a, int epi) 
       const bool valid = tid < gi;
       const int p = ig + tid;
       ILane il;
-      load_i<kPrecFP64, KIND>(a, il, p, valid);
+      load_i<kPrecFP64, KIND>(a, sc, il, p, valid);
       if (!valid) {
         il.fx = il.fy = 3.0e30f;
         il.x = il.y = il.phi = il.dphi = 0.0;
@@ -403,7 +407,7 @@ __global__ void __launch_bounds__(kTileThreads64) k_tile_fp64(KArgs a, int epi) 
         }
         acc.n += qn;
       }
-      if (valid) epilogue<kPrecFP64, KIND>(a, epi, il, acc, a.pidx[p]);
+      if (valid) epilogue<kPrecFP64, KIND>(a, epi, sd, il, acc, a.pidx[p]);
       __syncthreads();
     }
   }

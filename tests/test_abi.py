@@ -46,11 +46,12 @@ def test_invalid_parameters_rejected_without_gpu(field, value):
 
 
 @needs_nvcc
-def test_vortex_needs_srk_and_nonpositive_n_rejected():
+def test_vortex_rk4_and_nonpositive_n_rejected():
     L = abi.lib()
     h = C.c_void_p()
+    # natural frequencies enter the Euler and SRK drifts only
     p = abi.make_params(L=1.0, v0=0.01, sigma=1.0, rho=0.1, alpha=0.0, D_phi=0.005,
-                        model=abi.MODEL_VORTEX, stepper=abi.STEPPER_EULER)
+                        model=abi.MODEL_VORTEX, stepper=abi.STEPPER_RK4)
     assert L.spc_create(C.byref(p), 16, C.byref(h)) == -1
     p = abi.make_params(L=1.0, v0=0.01, sigma=1.0, rho=0.1, alpha=0.0, D_phi=0.005)
     assert L.spc_create(C.byref(p), 0, C.byref(h)) == -1
