@@ -130,6 +130,66 @@ def cpu_baseline(w, nsteps=3):
                       f"(the reference's path is single-threaded per system)"}
 
 
+def ensemble_systems(count=512, seed=2, n_range=(256, 32768), density=1000.0):
+    """The batched-ensemble configuration: count Chimera systems, N log-uniform
+    in n_range, L = sqrt(N / density), alpha ~ U[1.2, 1.6], sigma ~ U[0.5, 2],
+    D ~ U[0, 0.02], rho ~ U[0.05, 0.15], v0 = 0.01, from numpy PCG64(seed)."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for k in range(count):
+        n = int(round(np.exp(rng.uniform(np.log(n_range[0]), np.log(n_range[1])))))
+        L = float(np.sqrt(n / density))
+        prm = dict(v0=0.01, sigma=float(rng.uniform(0.5, 2.0)), rho=float(rng.uniform(0.05, 0.15)),
+                   alpha=float(rng.uniform(1.2, 1.6)), D_phi=float(rng.uniform(0.0, 0.02)))
+        st = np.empty(3 * n)
+        st[0::3] = rng.uniform(0.0, L, n)
+        st[1::3] = rng.uniform(0.0, L, n)
+        st[2::3] = rng.uniform(-np.pi, np.pi, n)
+        out.append((k, n, L, prm, st))
+    return out
+
+
+def run_ensemble(precision, graphs, rank=0):
+    """One batch of all ensemble systems, `graphs` replays of a 100-step graph."""
+    import torch
+    from spc2_langevin_integration_gb300 import abi
+    systems = ensemble_systems()
+    ntot = sum(n for _, n, _, _, _ in systems)
+    ctot = sum(abi.cells_of(L, prm["rho"]) for _, _, L, prm, _ in systems)
+    b = abi.Batch(abi.STEPPER_EULER, precision, len(systems), ntot, ctot)
+    for k, n, L, prm, st in systems:
+        p = abi.make_params(L=L, stepper=abi.STEPPER_EULER, precision=precision, seed=2,
+                            system_id=1000 * rank + k, **prm)
+        b.admit(n, p, st)
+    stream = torch.cuda.ExternalStream(b.stream)
+    b.step(0.01, 100, graph=True)  # capture + warm
+    b.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(graphs):
+        b.step(0.01, 100, graph=True)
+    e1.record(stream)
+    b.synchronize()
+    ms = e0.elapsed_time(e1)
+    b.close()
+    return ntot, ctot, ms
+
+
+def run_serving(precision, duration, rate, seed=3):
+    from spc2_langevin_integration_gb300 import abi, serve
+    trace = serve.make_trace(rate=rate, duration=duration, seed=seed)
+    max_n, max_c, max_s = 4_200_000, 1_500_000, 1024
+    with abi.Batch(abi.STEPPER_EULER, precision, max_s, max_n, max_c) as b:
+        srv = serve.Server(b, abi.STEPPER_EULER, precision, dt=0.01, chunk=50,
+                           limits=(max_n, max_c))
+        st = srv.run(trace)
+    out = st.as_dict()
+    out.update({"requests": len(trace), "refused": len(srv.refused), "rate_per_s": rate,
+                "duration_s": duration, "batch_capacity": {"particles": max_n, "cells": max_c,
+                                                           "systems": max_s}})
+    return out
+
+
 def dist_setup(args):
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -217,7 +277,34 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--ncu-case", choices=["fp32c", "fp64"], default=None,
                     help="run a few plain (ungraphed) steps of the workload for an ncu capture")
+    ap.add_argument("--workload", choices=["vortex", "ensemble", "serve"], default="vortex",
+                    help="vortex: the headline single-system line; ensemble: 512 systems in one "
+                         "batch; serve: the Poisson request stream")
+    ap.add_argument("--serve-duration", type=float, default=10.0)
+    ap.add_argument("--serve-rate", type=float, default=200.0)
     args = ap.parse_args()
+    if args.workload == "ensemble":
+        import torch
+        from spc2_langevin_integration_gb300 import abi
+        res = {}
+        for name, prec, graphs in (("fp32c", abi.PRECISION_FP32C, 50), ("fp64", abi.PRECISION_FP64, 5)):
+            ntot, ctot, ms = run_ensemble(prec, graphs)
+            res[name] = {"value": ntot * 100 * graphs / (ms / 1e3), "steps": 100 * graphs,
+                         "ms": ms}
+        print(json.dumps({"metric": "particle-steps/s", "workload": "ensemble_512_euler",
+                          "value": res["fp32c"]["value"], "unit": "particle-steps/s",
+                          "systems": 512, "particles": ntot, "cells": ctot,
+                          "fp32c": res["fp32c"], "fp64": res["fp64"],
+                          "fp32c_over_fp64": res["fp32c"]["value"] / res["fp64"]["value"],
+                          "graph_steps": 100, "l2": "working set > L2 (about 1 GB)"}))
+        return
+    if args.workload == "serve":
+        from spc2_langevin_integration_gb300 import abi
+        out = {"metric": "served time-to-result", "workload": "poisson_requests_euler"}
+        for name, prec in (("fp32c", abi.PRECISION_FP32C), ("fp64", abi.PRECISION_FP64)):
+            out[name] = run_serving(prec, args.serve_duration, args.serve_rate)
+        print(json.dumps(out))
+        return
     if args.ncu_case:
         from spc2_langevin_integration_gb300 import abi
         w = WORKLOAD
