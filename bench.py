@@ -149,14 +149,18 @@ def ensemble_systems(count=512, seed=2, n_range=(256, 32768), density=1000.0):
     return out
 
 
-def run_ensemble(precision, graphs, rank=0):
-    """One batch of all ensemble systems, `graphs` replays of a 100-step graph."""
+def run_ensemble(precision, graphs, rank=0, sparse_below=None):
+    """One batch of all ensemble systems, `graphs` replays of a 100-step graph;
+    then a per-phase profile of 5 plain steps.  sparse_below: the tuning that
+    picks the neighbour kernel per system (None: the library's default)."""
     import torch
     from spc2_langevin_integration_gb300 import abi
     systems = ensemble_systems()
     ntot = sum(n for _, n, _, _, _ in systems)
     ctot = sum(abi.cells_of(L, prm["rho"]) for _, _, L, prm, _ in systems)
     b = abi.Batch(abi.STEPPER_EULER, precision, len(systems), ntot, ctot)
+    if sparse_below is not None:
+        b.set_tuning(abi.TUNE_SPARSE_BELOW, sparse_below)
     for k, n, L, prm, st in systems:
         p = abi.make_params(L=L, stepper=abi.STEPPER_EULER, precision=precision, seed=2,
                             system_id=1000 * rank + k, **prm)
@@ -171,8 +175,9 @@ def run_ensemble(precision, graphs, rank=0):
     e1.record(stream)
     b.synchronize()
     ms = e0.elapsed_time(e1)
+    prof = b.profile_steps(0.01, 5)
     b.close()
-    return ntot, ctot, ms
+    return ntot, ctot, ms, prof
 
 
 def run_serving(precision, duration, rate, seed=3):
@@ -188,6 +193,91 @@ def run_serving(precision, duration, rate, seed=3):
                 "duration_s": duration, "batch_capacity": {"particles": max_n, "cells": max_c,
                                                            "systems": max_s}})
     return out
+
+
+def run_drift(steps=10000, every=100, out_path=None):
+    """Drift of the order parameters of the FP32-compensated form against FP64.
+
+    (1) The vortex SRK workload (N=65,536, L=8): FP32C and the FP64 GPU path from
+    the same state with the same Philox counters (FP32C draws the same Philox
+    words through float Box-Muller), global R and local R every `every` steps.
+    (2) The Chimera Euler workload (N=1,024, L=1, rho=0.1): FP32C and FP64 on the
+    GPU and the CPU oracle, all three fed the identical normals (exported from
+    the FP64 run and injected into the others).  Reports max |delta| over time."""
+    from oracle import pyoracle as po
+    from spc2_langevin_integration_gb300 import abi
+    res = {}
+    # (1) vortex SRK N=65536
+    w = WORKLOAD
+    st, omega = init_inputs(w)
+    series = {}
+    for name, prec in (("fp64", abi.PRECISION_FP64), ("fp32c", abi.PRECISION_FP32C)):
+        p = abi.make_params(L=w["L"], v0=w["v0"], sigma=w["sigma"], rho=w["rho"], alpha=w["alpha"],
+                            D_phi=w["D_phi"], model=abi.MODEL_VORTEX, stepper=abi.STEPPER_SRK,
+                            precision=prec, seed=w["seed"])
+        rows = []
+        with abi.System(w["n"], p) as s:
+            s.upload_state(st)
+            s.upload_omega(omega)
+            o = s.order_params()
+            rows.append((0, o["R"], o["R_local"]))
+            for k in range(every, steps + 1, every):
+                s.step(w["dt"], every, graph=True)
+                o = s.order_params()
+                rows.append((k, o["R"], o["R_local"]))
+        series[name] = rows
+    a, b = np.array(series["fp64"]), np.array(series["fp32c"])
+    res["vortex_srk_n65536"] = {
+        "steps": steps, "every": every, "reference": "FP64 GPU path (same Philox counters)",
+        "max_abs_dR": float(np.abs(a[:, 1] - b[:, 1]).max()),
+        "max_abs_dR_local": float(np.abs(a[:, 2] - b[:, 2]).max()),
+        "final": {"fp64": {"R": a[-1, 1], "R_local": a[-1, 2]},
+                  "fp32c": {"R": b[-1, 1], "R_local": b[-1, 2]}},
+        "mean_abs_dR": float(np.abs(a[:, 1] - b[:, 1]).mean()),
+        "mean_abs_dR_local": float(np.abs(a[:, 2] - b[:, 2]).mean()),
+        "series": {"step": a[:, 0].tolist(), "R_fp64": a[:, 1].tolist(), "R_fp32c": b[:, 1].tolist(),
+                   "Rl_fp64": a[:, 2].tolist(), "Rl_fp32c": b[:, 2].tolist()}}
+    # (2) Chimera Euler N=1024 against the CPU oracle with identical noise
+    n, L, dt = 1024, 1.0, 0.01
+    prm = dict(v0=0.01, sigma=1.0, rho=0.1, alpha=1.45, D_phi=0.005)
+    rng = np.random.default_rng(0)
+    st0 = np.empty(3 * n)
+    st0[0::3] = rng.uniform(0.0, L, n)
+    st0[1::3] = rng.uniform(0.0, L, n)
+    st0[2::3] = rng.uniform(-np.pi, np.pi, n)
+    orc = po.OracleSystem(n, L, **prm)
+    ref = st0.copy()
+    t_ref = 0.0
+    rows = []
+    with abi.System(n, abi.make_params(L=L, stepper=abi.STEPPER_EULER, seed=0, **prm)) as s64, \
+            abi.System(n, abi.make_params(L=L, stepper=abi.STEPPER_EULER, seed=0,
+                                          precision=abi.PRECISION_FP32C, **prm)) as s32:
+        s64.upload_state(st0)
+        s32.upload_state(st0)
+        for k in range(every, steps + 1, every):
+            noise = s64.export_noise(k - every, every)
+            s32.inject_noise(noise)
+            s64.step(dt, every)
+            s32.step(dt, every)
+            t_ref = orc.run(po.EULER, ref, t_ref, dt, every, noise)
+            o64, o32, oo = s64.order_params(), s32.order_params(), orc.order_params(ref)
+            rows.append((k, oo["R"], o64["R"], o32["R"], oo["R_local"], o64["R_local"], o32["R_local"]))
+    r = np.array(rows)
+    res["chimera_euler_n1024"] = {
+        "steps": steps, "every": every, "reference": "CPU oracle (identical injected normals)",
+        "fp64_gpu": {"max_abs_dR": float(np.abs(r[:, 2] - r[:, 1]).max()),
+                     "max_abs_dR_local": float(np.abs(r[:, 5] - r[:, 4]).max())},
+        "fp32c_gpu": {"max_abs_dR": float(np.abs(r[:, 3] - r[:, 1]).max()),
+                      "max_abs_dR_local": float(np.abs(r[:, 6] - r[:, 4]).max())},
+        "final": {"oracle": {"R": r[-1, 1], "R_local": r[-1, 4]},
+                  "fp64_gpu": {"R": r[-1, 2], "R_local": r[-1, 5]},
+                  "fp32c_gpu": {"R": r[-1, 3], "R_local": r[-1, 6]}}}
+    if out_path:
+        with open(out_path, "w") as f:
+            json.dump(res, f)
+    for v in res.values():
+        v.pop("series", None)
+    return res
 
 
 def dist_setup(args):
@@ -275,11 +365,21 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--ncu-case", choices=["fp32c", "fp64"], default=None,
-                    help="run a few plain (ungraphed) steps of the workload for an ncu capture")
-    ap.add_argument("--workload", choices=["vortex", "ensemble", "serve"], default="vortex",
+    ap.add_argument("--ncu-case", choices=["fp32c", "fp64", "ensemble_fp32c", "ensemble_fp64"],
+                    default=None,
+                    help="run a few plain (ungraphed) steps of the workload (or of an ensemble of "
+                         "--ensemble-systems systems) for an ncu capture")
+    ap.add_argument("--ensemble-systems", type=int, default=512)
+    ap.add_argument("--workload", choices=["vortex", "ensemble", "serve", "drift"], default="vortex",
                     help="vortex: the headline single-system line; ensemble: 512 systems in one "
-                         "batch; serve: the Poisson request stream")
+                         "batch; serve: the Poisson request stream; drift: FP32C vs FP64 order "
+                         "parameters over 10^4 steps")
+    ap.add_argument("--sparse-below", type=float, default=None,
+                    help="ensemble: neighbour-kernel tuning (mean particles per cell below "
+                         "which a system runs the warp-per-cell passes)")
+    ap.add_argument("--compare-kernels", action="store_true",
+                    help="ensemble: also time every system on the cell-tile passes")
+    ap.add_argument("--drift-steps", type=int, default=10000)
     ap.add_argument("--serve-duration", type=float, default=10.0)
     ap.add_argument("--serve-rate", type=float, default=200.0)
     args = ap.parse_args()
@@ -287,16 +387,28 @@ def main():
         import torch
         from spc2_langevin_integration_gb300 import abi
         res = {}
-        for name, prec, graphs in (("fp32c", abi.PRECISION_FP32C, 50), ("fp64", abi.PRECISION_FP64, 5)):
-            ntot, ctot, ms = run_ensemble(prec, graphs)
+        runs = [("fp32c", abi.PRECISION_FP32C, 20, args.sparse_below),
+                ("fp64", abi.PRECISION_FP64, 3, args.sparse_below)]
+        if args.compare_kernels:
+            runs += [("fp32c_tile_only", abi.PRECISION_FP32C, 5, 0.0),
+                     ("fp64_tile_only", abi.PRECISION_FP64, 1, 0.0)]
+        for name, prec, graphs, sb in runs:
+            ntot, ctot, ms, prof = run_ensemble(prec, graphs, sparse_below=sb)
             res[name] = {"value": ntot * 100 * graphs / (ms / 1e3), "steps": 100 * graphs,
-                         "ms": ms}
+                         "ms": ms, "profile_ms": prof, "sparse_below": sb}
         print(json.dumps({"metric": "particle-steps/s", "workload": "ensemble_512_euler",
                           "value": res["fp32c"]["value"], "unit": "particle-steps/s",
                           "systems": 512, "particles": ntot, "cells": ctot,
-                          "fp32c": res["fp32c"], "fp64": res["fp64"],
+                          **res,
                           "fp32c_over_fp64": res["fp32c"]["value"] / res["fp64"]["value"],
                           "graph_steps": 100, "l2": "working set > L2 (about 1 GB)"}))
+        return
+    if args.workload == "drift":
+        out = {"metric": "order-parameter drift, FP32C vs FP64", "workload": "drift"}
+        out.update(run_drift(steps=args.drift_steps,
+                             out_path=os.path.join(ROOT, "gpurun_out", "drift_series.json")
+                             if os.path.isdir(os.path.join(ROOT, "gpurun_out")) else None))
+        print(json.dumps(out))
         return
     if args.workload == "serve":
         from spc2_langevin_integration_gb300 import abi
@@ -304,6 +416,23 @@ def main():
         for name, prec in (("fp32c", abi.PRECISION_FP32C), ("fp64", abi.PRECISION_FP64)):
             out[name] = run_serving(prec, args.serve_duration, args.serve_rate)
         print(json.dumps(out))
+        return
+    if args.ncu_case and args.ncu_case.startswith("ensemble"):
+        from spc2_langevin_integration_gb300 import abi
+        prec = abi.PRECISION_FP32C if args.ncu_case.endswith("fp32c") else abi.PRECISION_FP64
+        systems = ensemble_systems(count=args.ensemble_systems)
+        ntot = sum(n for _, n, _, _, _ in systems)
+        ctot = sum(abi.cells_of(L, prm["rho"]) for _, _, L, prm, _ in systems)
+        with abi.Batch(abi.STEPPER_EULER, prec, len(systems), ntot, ctot) as b:
+            if args.sparse_below is not None:
+                b.set_tuning(abi.TUNE_SPARSE_BELOW, args.sparse_below)
+            for k, n, L, prm, st in systems:
+                b.admit(n, abi.make_params(L=L, stepper=abi.STEPPER_EULER, precision=prec, seed=2,
+                                           system_id=k, **prm), st)
+            b.step(0.01, 3)
+            b.synchronize()
+        print(json.dumps({"ncu_case": args.ncu_case, "systems": len(systems), "particles": ntot,
+                          "cells": ctot}))
         return
     if args.ncu_case:
         from spc2_langevin_integration_gb300 import abi

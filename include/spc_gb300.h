@@ -171,6 +171,16 @@ int spc_diagnostics(spc_handle *h, int64_t *clamped_cells, int64_t *verlet_rebui
  * RK4 passes, [5] the whole step.  cap is out_ms's length (>= 6). */
 int spc_profile_steps(spc_handle *h, double dt, int32_t nsteps, double *out_ms, int32_t cap);
 
+/* Tuning knobs (no counterpart in the reference; results do not depend on
+ * them beyond floating-point summation order in the FP32C form).
+ * SPC_TUNE_SPARSE_BELOW: cell-list systems with fewer particles per cell
+ * than this value (on average) run the warp-per-cell neighbour passes, the
+ * others the cell-tile passes; 0 sends every system to the cell-tile passes.
+ * Default 24.  spc_get_tuning reads a knob back. */
+enum { SPC_TUNE_SPARSE_BELOW = 1 };
+int spc_set_tuning(spc_handle *h, int32_t key, double value);
+int spc_get_tuning(const spc_handle *h, int32_t key, double *value);
+
 /* Synchronise the handle's stream; the stream itself (a cudaStream_t) for
  * callers that time or order work around the library. */
 int spc_synchronize(spc_handle *h);
@@ -228,6 +238,12 @@ int spc_batch_usage(spc_batch *b, int64_t *particles, int64_t *cells, int32_t *s
 int spc_batch_order_params(spc_batch *b, int32_t slot, double *R, double *psi);
 int spc_batch_synchronize(spc_batch *b);
 void *spc_batch_stream(spc_batch *b);
+/* Per-phase device time of nsteps steps of the whole batch (as
+ * spc_profile_steps; the steps count against the systems' budgets). */
+int spc_batch_profile_steps(spc_batch *b, double dt, int32_t nsteps, double *out_ms, int32_t cap);
+/* The tuning knobs of spc_set_tuning, for a whole batch. */
+int spc_batch_set_tuning(spc_batch *b, int32_t key, double value);
+int spc_batch_get_tuning(const spc_batch *b, int32_t key, double *value);
 
 /* SRK-form right-hand side (as spc_rhs_srk) computed without allocating
  * any device memory.  No counterpart in the reference: it exists for callers

@@ -19,6 +19,7 @@ STEPPER_EULER, STEPPER_SRK, STEPPER_RK4, STEPPER_EULER_PTR = 0, 1, 2, 3
 NEIGHBOUR_CELL, NEIGHBOUR_VERLET = 0, 1
 PRECISION_FP64, PRECISION_FP32C = 0, 1
 FLAG_EXACT_ALL = 0x1
+TUNE_SPARSE_BELOW = 1
 
 SPC_OK = 0
 ERRORS = {
@@ -121,6 +122,11 @@ def lib() -> C.CDLL:
     L.spc_batch_synchronize.argtypes = [H]
     L.spc_batch_stream.restype = C.c_void_p
     L.spc_batch_stream.argtypes = [H]
+    L.spc_batch_profile_steps.argtypes = [H, C.c_double, C.c_int32, dp, C.c_int32]
+    L.spc_set_tuning.argtypes = [H, C.c_int32, C.c_double]
+    L.spc_get_tuning.argtypes = [H, C.c_int32, dp]
+    L.spc_batch_set_tuning.argtypes = [H, C.c_int32, C.c_double]
+    L.spc_batch_get_tuning.argtypes = [H, C.c_int32, dp]
     L.spc_alloc_pinned.argtypes = [C.c_size_t, C.POINTER(C.c_void_p)]
     L.spc_free_pinned.argtypes = [C.c_void_p]
     _lib = L
@@ -273,6 +279,14 @@ class System:
         self._check(self._L.spc_diagnostics(self.h, C.byref(c), C.byref(v), C.byref(e)), self.h)
         return {"clamped_cells": c.value, "verlet_rebuilds": v.value, "error_word": e.value}
 
+    def set_tuning(self, key: int, value: float):
+        self._check(self._L.spc_set_tuning(self.h, int(key), float(value)), self.h)
+
+    def get_tuning(self, key: int) -> float:
+        v = C.c_double()
+        self._check(self._L.spc_get_tuning(self.h, int(key), C.byref(v)), self.h)
+        return v.value
+
     def profile_steps(self, dt: float, nsteps: int) -> dict:
         out = (C.c_double * 6)()
         self._check(self._L.spc_profile_steps(self.h, dt, int(nsteps), out, 6), self.h)
@@ -400,6 +414,20 @@ class Batch:
 
     def synchronize(self):
         self._check(self._L.spc_batch_synchronize(self.h))
+
+    def set_tuning(self, key: int, value: float):
+        self._check(self._L.spc_batch_set_tuning(self.h, int(key), float(value)))
+
+    def get_tuning(self, key: int) -> float:
+        v = C.c_double()
+        self._check(self._L.spc_batch_get_tuning(self.h, int(key), C.byref(v)))
+        return v.value
+
+    def profile_steps(self, dt: float, nsteps: int) -> dict:
+        out = (C.c_double * 6)()
+        self._check(self._L.spc_batch_profile_steps(self.h, dt, int(nsteps), out, 6))
+        keys = ("stage", "sort", "gather", "pass1", "pass2", "step")
+        return {k: out[i] for i, k in enumerate(keys)}
 
     @property
     def stream(self) -> int:

@@ -398,36 +398,17 @@ void *spc_stream(spc_handle *h) { return h ? (void *)h->e.stream : nullptr; }
 int spc_profile_steps(spc_handle *h, double dt, int32_t nsteps, double *out_ms, int32_t cap) {
   if (!h || !out_ms || cap < 6 || nsteps <= 0) return hfail(h, SPC_ERR_INVALID, "bad argument");
   SPC_TRY(check_ready(h));
-  Engine *e = &h->e;
-  if (e->injecting) return fail(e, SPC_ERR_STATE, "profiling uses Philox noise");
-  SPC_TRY(engine_set_device(e));
-  SPC_TRY(engine_layout(e));
-  for (int k = 0; k < 6; ++k)
-    if (!e->prof_ev[k]) SPC_CUDA(e, cudaEventCreate(&e->prof_ev[k]));
-  double acc[6] = {0, 0, 0, 0, 0, 0};
-  SPC_TRY(open_eval(e, nsteps));
-  for (int s = 0; s < nsteps; ++s) {
-    // phase marks: 0 start, 1 after stage, 2 after sort, 3 after gather,
-    // 4 after the first pass, 5 end of step
-    SPC_CUDA(e, cudaEventRecord(e->prof_ev[0], e->stream));
-    e->profiling = true;
-    int rc = enqueue_step(e, dt, s, nullptr);
-    e->profiling = false;
-    if (rc != SPC_OK) return rc;
-    SPC_CUDA(e, cudaEventRecord(e->prof_ev[5], e->stream));
-    SPC_CUDA(e, cudaEventSynchronize(e->prof_ev[5]));
-    float ms[6] = {0, 0, 0, 0, 0, 0};
-    for (int k = 1; k <= 5; ++k) SPC_CUDA(e, cudaEventElapsedTime(&ms[k], e->prof_ev[k - 1], e->prof_ev[k]));
-    for (int k = 0; k < 5; ++k) acc[k] += ms[k + 1];
-    float tot = 0.0f;
-    SPC_CUDA(e, cudaEventElapsedTime(&tot, e->prof_ev[0], e->prof_ev[5]));
-    acc[5] += tot;
-  }
-  k_end_call<<<blocks_for(e->nsys, 128), 128, 0, e->stream>>>(e->d_sys, e->nsys);
-  SPC_LAUNCHED(e);
-  mirror_call(e, nsteps);
-  for (int k = 0; k < 6; ++k) out_ms[k] = acc[k] / nsteps;
-  return SPC_OK;
+  return engine_profile(&h->e, dt, nsteps, out_ms);
+}
+
+int spc_set_tuning(spc_handle *h, int32_t key, double value) {
+  if (!h) return fail(nullptr, SPC_ERR_INVALID, "NULL argument");
+  return engine_set_tuning(&h->e, key, value);
+}
+
+int spc_get_tuning(const spc_handle *h, int32_t key, double *value) {
+  if (!h || !value) return fail(nullptr, SPC_ERR_INVALID, "NULL argument");
+  return engine_get_tuning(&h->e, key, value);
 }
 
 int spc_philox4x32_10(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]) {
@@ -601,6 +582,22 @@ int spc_batch_synchronize(spc_batch *b) {
 
 void *spc_batch_stream(spc_batch *b) { return b ? (void *)b->e.stream : nullptr; }
 
+int spc_batch_set_tuning(spc_batch *b, int32_t key, double value) {
+  if (!b) return fail(nullptr, SPC_ERR_INVALID, "NULL argument");
+  return engine_set_tuning(&b->e, key, value);
+}
+
+int spc_batch_get_tuning(const spc_batch *b, int32_t key, double *value) {
+  if (!b || !value) return fail(nullptr, SPC_ERR_INVALID, "NULL argument");
+  return engine_get_tuning(&b->e, key, value);
+}
+
+int spc_batch_profile_steps(spc_batch *b, double dt, int32_t nsteps, double *out_ms, int32_t cap) {
+  if (!b || !out_ms || cap < 6 || nsteps <= 0)
+    return fail(b ? &b->e : nullptr, SPC_ERR_INVALID, "bad argument");
+  return engine_profile(&b->e, dt, nsteps, out_ms);
+}
+
 }  // extern "C"
 
 // ===========================================================================
@@ -754,6 +751,9 @@ extern "C" int spc_rhs_srk_noalloc(const spc_params *p, int32_t n, const double 
   a.nsys = 1;
   a.n_active = n;
   a.ncell_total = ncell;
+  a.ncell_tile = sc.allpairs ? 0 : ncell;  // cell-tile kernels only
+  e.ncell_tile = a.ncell_tile;
+  e.ncell_warp = 0;
   a.n_ap = sc.allpairs ? 1 : 0;
   a.hist_len = (1 << e.radix_bits) * e.ntiles;
   SysHost h;

@@ -33,6 +33,7 @@ struct SysConst {
   float lo2, hi2; // prefilter: float dr^2 < lo2 => inside, > hi2 => outside, else decide in FP64
   int exact_all;  // decide every candidate in FP64
   int L_pow2;     // L is a power of two: x / L == x * (1 / L) exactly
+  float cos_a, sin_a;  // FP32C: cos(alpha), sin(alpha) rounded to float
 };
 
 // PeriodicBoundaryConditions::ClassAEffectiveParticleDistance (PeriodicBoundaryConditions.cpp:22-35):
@@ -52,9 +53,14 @@ __device__ __forceinline__ bool exact_within(const SysConst &sc, double xi, doub
   return dr2 <= sc.rho2;
 }
 
-// ApplyPeriodicBoundaryConditions (PeriodicBoundaryConditions.cpp:117-121): x - floor(x * rL) * L
+// ApplyPeriodicBoundaryConditions (PeriodicBoundaryConditions.cpp:117-121): x - floor(x * rL) * L.
+// When 0 <= x * rL < 1 (an unsigned compare of the bits; -0.0 and NaN fail it)
+// floor gives +0.0 and x - 0.0 * L is x itself, so the result is returned
+// without the floor, the product and the difference.
 __device__ __forceinline__ double wrap_1d(double x, double rL, double L) {
-  return dsub(x, dmul(floor(dmul(x, rL)), L));
+  const double t = dmul(x, rL);
+  if ((unsigned long long)__double_as_longlong(t) < 0x3FF0000000000000ull) return x;
+  return dsub(x, dmul(floor(t), L));
 }
 
 // The conditional copy-wrap inside the force loops (ChimeraSystem.cpp:299-302):

@@ -27,6 +27,7 @@
 #include "spc_kernels.cuh"
 #include "spc_sort.cuh"
 #include "spc_tile.cuh"
+#include "spc_warp.cuh"
 
 namespace spc {
 
@@ -77,6 +78,8 @@ inline SysConst make_sysconst(const spc_params &p, int n) {
   sc.hi2 = (float)(sc.rho2 * (1.0 + 3e-5));
   sc.exact_all = (p.flags & SPC_FLAG_EXACT_ALL) ? 1 : 0;
   sc.L_pow2 = is_pow2(p.L);
+  sc.cos_a = (float)std::cos(p.alpha);
+  sc.sin_a = (float)std::sin(p.alpha);
   return sc;
 }
 
@@ -144,7 +147,11 @@ struct Engine {
   bool dirty = true;
   // current layout
   int nsys = 0, n_active = 0, ncell_total = 0, ntiles = 0, radix_bits = 1, sort_passes = 1;
+  int ncell_tile = 0, ncell_warp = 0;  // cells of the cell-tile and of the warp-per-cell systems
   bool has_cells = false;
+  // tuning: cell-list systems with fewer than sparse_below particles per cell
+  // (on average) run the warp-per-cell passes
+  double sparse_below = kSparseBelowDefault;
   std::vector<int> slot_layout;  // slot -> layout index (-1 if inactive)
   // noise injection (single-system handles)
   double *d_noise = nullptr;
@@ -419,6 +426,13 @@ inline SysDesc desc_of(const SysHost &h, int dense_p0, int c0) {
   return d;
 }
 
+// 0: cell list, dense cells (cell-tile kernels); 1: cell list, sparse cells
+// (warp-per-cell kernel); 2: all pairs.
+inline int system_class(const Engine *e, const SysHost &h) {
+  if (h.sc.allpairs) return 2;
+  return (double)h.n < e->sparse_below * (double)h.ncell ? 1 : 0;
+}
+
 // Rebuild the device layout tables from the host mirror.
 inline int engine_layout(Engine *e) {
   if (!e->dirty) return SPC_OK;
@@ -427,14 +441,24 @@ inline int engine_layout(Engine *e) {
   std::vector<int> ap;
   int dense = 0, cells = 0;
   std::fill(e->slot_layout.begin(), e->slot_layout.end(), -1);
-  for (int slot : e->order) {
-    const SysHost &h = e->slots[slot];
-    e->slot_layout[slot] = (int)table.size();
-    table.push_back(desc_of(h, dense, cells));
-    if (h.sc.allpairs) ap.push_back(cells);
-    dense += h.n;
-    cells += h.ncell;
+  // cell-tile systems first, then warp-per-cell systems, then all-pairs ones,
+  // so that each neighbour kernel covers one contiguous range of cells
+  int ncell_tile = 0, ncell_warp = 0;
+  for (int cls = 0; cls < 3; ++cls) {
+    for (int slot : e->order) {
+      const SysHost &h = e->slots[slot];
+      if (system_class(e, h) != cls) continue;
+      e->slot_layout[slot] = (int)table.size();
+      table.push_back(desc_of(h, dense, cells));
+      if (h.sc.allpairs) ap.push_back(cells);
+      dense += h.n;
+      cells += h.ncell;
+      if (cls == 0) ncell_tile += h.ncell;
+      if (cls == 1) ncell_warp += h.ncell;
+    }
   }
+  e->ncell_tile = ncell_tile;
+  e->ncell_warp = ncell_warp;
   e->nsys = (int)table.size();
   e->n_active = dense;
   e->ncell_total = cells;
@@ -448,6 +472,7 @@ inline int engine_layout(Engine *e) {
   a.nsys = e->nsys;
   a.n_active = e->n_active;
   a.ncell_total = e->ncell_total;
+  a.ncell_tile = e->ncell_tile;
   a.n_ap = (int)ap.size();
   a.hist_len = (1 << e->radix_bits) * e->ntiles;
   if (e->nsys > 0) {
@@ -520,16 +545,28 @@ int launch_pass_t(Engine *e, const KArgs &a, int epi) {
     SPC_LAUNCHED(e);
   }
   if (e->has_cells) {
-    const int grid = std::min(e->ncell_total, 152 * 256);
     if constexpr (KIND == kKindNb) {
       k_cell_pass<PREC, KIND><<<std::min(blocks_for(e->ncell_total, kPassWarps), 152 * 64), kPassThreads, 0,
                                 st>>>(a, epi);
-    } else if constexpr (PREC == kPrecFP32C) {
-      k_tile_fp32c<KIND><<<grid, kTileThreads32, 0, st>>>(a, epi);
+      SPC_LAUNCHED(e);
     } else {
-      k_tile_fp64<KIND><<<grid, kTileThreads64, 0, st>>>(a, epi);
+      if (e->ncell_tile > 0) {
+        const int grid = std::min(e->ncell_tile, 152 * 256);
+        if constexpr (PREC == kPrecFP32C)
+          k_tile_fp32c<KIND><<<grid, kTileThreads32, 0, st>>>(a, epi);
+        else
+          k_tile_fp64<KIND><<<grid, kTileThreads64, 0, st>>>(a, epi);
+        SPC_LAUNCHED(e);
+      }
+      if (e->ncell_warp > 0) {
+        const int grid = std::min(blocks_for(e->ncell_warp, kWarpPassWarps), 152 * 64);
+        if constexpr (PREC == kPrecFP32C)
+          k_warp_fp32c<KIND><<<grid, kWarpPassThreads, 0, st>>>(a, epi);
+        else
+          k_warp_fp64<KIND><<<grid, kWarpPassThreads, 0, st>>>(a, epi);
+        SPC_LAUNCHED(e);
+      }
     }
-    SPC_LAUNCHED(e);
   }
   return SPC_OK;
 }
@@ -640,6 +677,66 @@ inline int engine_steps(Engine *e, double dt, int nsteps, bool use_graph, const 
     SPC_CUDA(e, cudaGraphLaunch(e->graph, e->stream));
   }
   mirror_call(e, nsteps);
+  return SPC_OK;
+}
+
+inline int engine_set_tuning(Engine *e, int key, double value) {
+  if (key == SPC_TUNE_SPARSE_BELOW) {
+    if (!(value >= 0.0) || !std::isfinite(value)) return fail(e, SPC_ERR_INVALID, "sparse_below must be >= 0");
+    if (value != e->sparse_below) {
+      e->sparse_below = value;
+      e->dirty = true;  // the next step lays the systems out again
+    }
+    return SPC_OK;
+  }
+  return fail(e, SPC_ERR_INVALID, "unknown tuning key %d", key);
+}
+
+inline int engine_get_tuning(const Engine *e, int key, double *value) {
+  if (key == SPC_TUNE_SPARSE_BELOW) {
+    *value = e->sparse_below;
+    return SPC_OK;
+  }
+  return fail(nullptr, SPC_ERR_INVALID, "unknown tuning key %d", key);
+}
+
+// nsteps eagerly launched steps with CUDA events between the phases; out_ms[k]
+// is the mean per step of: stage, sort, gather, first pass, rest of the step,
+// whole step.
+inline int engine_profile(Engine *e, double dt, int nsteps, double *out_ms) {
+  if (e->injecting) return fail(e, SPC_ERR_STATE, "profiling uses Philox noise");
+  SPC_TRY(engine_set_device(e));
+  SPC_TRY(engine_layout(e));
+  for (int k = 0; k < 6; ++k) {
+    out_ms[k] = 0.0;
+    if (!e->prof_ev[k]) SPC_CUDA(e, cudaEventCreate(&e->prof_ev[k]));
+  }
+  if (e->nsys == 0 || nsteps <= 0) return SPC_OK;
+  const int sb = blocks_for(e->nsys, 128);
+  double acc[6] = {0, 0, 0, 0, 0, 0};
+  k_begin_call<<<sb, 128, 0, e->stream>>>(e->d_sys, e->nsys, nsteps);
+  SPC_LAUNCHED(e);
+  for (int s = 0; s < nsteps; ++s) {
+    // phase marks: 0 start, 1 after stage, 2 after sort, 3 after gather,
+    // 4 after the first pass, 5 end of step
+    SPC_CUDA(e, cudaEventRecord(e->prof_ev[0], e->stream));
+    e->profiling = true;
+    const int rc = enqueue_step(e, dt, s, nullptr);
+    e->profiling = false;
+    if (rc != SPC_OK) return rc;
+    SPC_CUDA(e, cudaEventRecord(e->prof_ev[5], e->stream));
+    SPC_CUDA(e, cudaEventSynchronize(e->prof_ev[5]));
+    float ms[6] = {0, 0, 0, 0, 0, 0};
+    for (int k = 1; k <= 5; ++k) SPC_CUDA(e, cudaEventElapsedTime(&ms[k], e->prof_ev[k - 1], e->prof_ev[k]));
+    for (int k = 0; k < 5; ++k) acc[k] += ms[k + 1];
+    float tot = 0.0f;
+    SPC_CUDA(e, cudaEventElapsedTime(&tot, e->prof_ev[0], e->prof_ev[5]));
+    acc[5] += tot;
+  }
+  k_end_call<<<sb, 128, 0, e->stream>>>(e->d_sys, e->nsys);
+  SPC_LAUNCHED(e);
+  mirror_call(e, nsteps);
+  for (int k = 0; k < 6; ++k) out_ms[k] = acc[k] / nsteps;
   return SPC_OK;
 }
 

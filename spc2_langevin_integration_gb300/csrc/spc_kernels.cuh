@@ -67,6 +67,7 @@ struct KArgs {
   int nsys;
   int n_active;                      // dense particles
   int ncell_total;
+  int ncell_tile;                    // cells [0, ncell_tile): cell-tile kernels; the rest: warp kernel
   const int *sys_of_p;               // dense index -> system
   const int *sys_of_c;               // global cell -> system
   // state pool (structure of arrays)
@@ -394,15 +395,15 @@ __device__ void epilogue(const KArgs &a, int epi, const SysDesc &sd, const ILane
   } else {
     // FP32C: right-hand sides and increments in float, accumulated into the
     // double positions and phase.
-    if (draws) {
-      float f0, f1;
-      philox_normal2_f(sd.seed, sd.system_id, step, (uint32_t)i, f0, f1);
-      z0 = f0;
-      z1 = f1;
-    }
-    const float ph_r = reduced_phase_f(il.phi);
-    float sph, cph;
-    sincosf(ph_r, &sph, &cph);
+    float f0 = 0.0f, f1 = 0.0f;
+    if (draws) philox_normal2_f(sd.seed, sd.system_id, step, (uint32_t)i, f0, f1);
+    auto noise_f = [&](int k) -> float {
+      if (a.noise) return (float)a.noise[(size_t)q * a.noise_m + k];
+      return k == 0 ? f0 : f1;
+    };
+    // cos / sin of the stage phase, as the gather computed them for this slot
+    const float2 csp = a.cs[p];
+    const float cph = csp.x, sph = csp.y;
     const float v0 = (float)sc.v0, D = (float)sc.D, dtf = (float)dt;
     const float d0 = v0 * cph, d1 = v0 * sph;
     if constexpr (KIND == kKindSin) {
@@ -426,7 +427,7 @@ __device__ void epilogue(const KArgs &a, int epi, const SysDesc &sd, const ILane
         }
       } else if (epi == kEpiEuler || epi == kEpiEulerPtr) {
         if (!live) return;
-        const float xi = (float)noise_at(a, q, 0, z0, z1);
+        const float xi = noise_f(0);
         const float sdt = sqrtf(dtf);
         const float s2D = sqrtf(2.0f * D);
         const float drift = (epi == kEpiEuler && sd.is_vortex) ? (float)a.omega[q] + rate : rate;
@@ -452,7 +453,7 @@ __device__ void epilogue(const KArgs &a, int epi, const SysDesc &sd, const ILane
         a.out_a[2 * (size_t)q + 1] = (double)A1;
       } else {
         if (!live) return;
-        const float U1 = (float)noise_at(a, q, 0, z0, z1), U2 = (float)noise_at(a, q, 1, z0, z1);
+        const float U1 = noise_f(0), U2 = noise_f(1);
         const float sdt = sqrtf(dtf);
         const float dW = U1 * sdt;
         const float dZ = 0.5f * dtf * sdt * (U1 + U2 * 0.57735026918962576f);
@@ -482,10 +483,11 @@ __device__ __forceinline__ void load_i(const KArgs &a, const SysConst &sc, ILane
     il.fy = f.y;
   }
   if constexpr (PREC == kPrecFP32C) {
-    float s, c;
-    sincosf(reduced_phase_f(il.phi) + (float)sc.alpha, &s, &c);
-    il.ca = c;
-    il.sa = s;
+    // cos / sin of (phi + alpha) from the stage phase's cos / sin (made by the
+    // gather) by the angle-addition identity
+    const float2 t = a.cs[p];
+    il.ca = t.x * sc.cos_a - t.y * sc.sin_a;
+    il.sa = t.y * sc.cos_a + t.x * sc.sin_a;
   }
   if constexpr (KIND == kKindCos2) {
     il.card = (double)a.cnt_s[p];

@@ -37,7 +37,6 @@ constexpr int kQCap = 64;           // FP64 per-thread queue (power of two)
 struct Stencil {
   int start[9];    // cell-order start of each stencil cell
   int prefix[10];  // offsets of each stencil cell in the staged list
-  float shx[9], shy[9];
 };
 
 __device__ __forceinline__ void stencil_of(const KArgs &a, const SysDesc &sd, int c, Stencil &s) {
@@ -51,19 +50,27 @@ __device__ __forceinline__ void stencil_of(const KArgs &a, const SysDesc &sd, in
     const int ja = a.cell_start[cj], jb = a.cell_start[cj + 1];
     s.start[q] = ja;
     s.prefix[q + 1] = s.prefix[q] + (jb - ja);
-    s.shx[q] = (float)ox * sc.cell_f;
-    s.shy[q] = (float)oy * sc.cell_f;
   }
 }
 
-// cell-order slot of staged candidate g (0 <= g < prefix[9])
+// Cell-order slot of staged candidate g (0 <= g < prefix[9]) and its stencil
+// entry q.  A select chain with constant indices keeps the stencil in
+// registers (a dynamic index would put it in local memory).
 __device__ __forceinline__ int slot_of(const Stencil &s, int g, int &q_out) {
-  int q = 0;
+  int q = 0, base = s.start[0];
 #pragma unroll
-  for (int k = 1; k < 9; ++k) q += (g >= s.prefix[k]) ? 1 : 0;
+  for (int k = 1; k < 9; ++k) {
+    const bool ge = g >= s.prefix[k];
+    q = ge ? k : q;
+    base = ge ? s.start[k] - s.prefix[k] : base;
+  }
   q_out = q;
-  return s.start[q] + (g - s.prefix[q]);
+  return base + g;
 }
+
+// periodic shift of stencil entry q in the float prefilter frame
+__device__ __forceinline__ float shift_x(int q, float cell_f) { return (float)(q % 3 - 1) * cell_f; }
+__device__ __forceinline__ float shift_y(int q, float cell_f) { return (float)(q / 3 - 1) * cell_f; }
 
 // ---------------------------------------------------------------------------
 // FP32C passes.  Pass 1 (KIND == kKindSin) also records, for cells whose
@@ -133,7 +140,7 @@ __global__ void __launch_bounds__(kTileThreads32) k_tile_fp32c(KArgs a, int epi)
   __shared__ int t_n[kTileThreads32];
   const int n_all = a.n_active;
   const int tid = threadIdx.x, w = tid / kWarp, lane = tid % kWarp;
-  for (int c = blockIdx.x; c < a.ncell_total; c += gridDim.x) {
+  for (int c = blockIdx.x; c < a.ncell_tile; c += gridDim.x) {
     const int cb = a.cell_start[c], ce = a.cell_start[c + 1];
     if (cb == ce) continue;
     const SysDesc &sd = a.sys[a.sys_of_c[c]];
@@ -164,7 +171,7 @@ __global__ void __launch_bounds__(kTileThreads32) k_tile_fp32c(KArgs a, int epi)
               const int pj = slot_of(st, rlo + k, q);
               const float2 f = a.fxy[pj];
               const float2 cs = a.cs[pj];
-              s_c4[k] = make_float4(f.x + st.shx[q], f.y + st.shy[q], cs.x, cs.y);
+              s_c4[k] = make_float4(f.x + shift_x(q, sc.cell_f), f.y + shift_y(q, sc.cell_f), cs.x, cs.y);
               s_p[k] = pj;
               if constexpr (KIND == kKindCos2) s_d[k] = a.dphi_f[pj];
             } else {  // padding: far away, never a neighbour, never near the cutoff
@@ -190,10 +197,9 @@ __global__ void __launch_bounds__(kTileThreads32) k_tile_fp32c(KArgs a, int epi)
             const float2 f = a.fxy[p];
             fxi = f.x;
             fyi = f.y;
-            float sn, cn;
-            sincosf(reduced_phase_f(a.sphi[p]) + (float)sc.alpha, &sn, &cn);
-            ca = cn;
-            sa = sn;
+            const float2 t = a.cs[p];  // cos / sin of phi_i + alpha by angle addition
+            ca = t.x * sc.cos_a - t.y * sc.sin_a;
+            sa = t.y * sc.cos_a + t.x * sc.sin_a;
             if constexpr (KIND == kKindCos2) di = a.dphi_f[p];
             xi = a.sx[p];
             yi = a.sy[p];
@@ -318,7 +324,7 @@ __global__ void __launch_bounds__(kTileThreads64) k_tile_fp64(KArgs a, int epi) 
   __shared__ int s_p[kTileCap64];
   __shared__ uint16_t s_q[kQCap][kTileThreads64];
   const int tid = threadIdx.x;
-  for (int c = blockIdx.x; c < a.ncell_total; c += gridDim.x) {
+  for (int c = blockIdx.x; c < a.ncell_tile; c += gridDim.x) {
     const int cb = a.cell_start[c], ce = a.cell_start[c + 1];
     if (cb == ce) continue;
     const SysDesc &sd = a.sys[a.sys_of_c[c]];
@@ -352,7 +358,7 @@ __global__ void __launch_bounds__(kTileThreads64) k_tile_fp64(KArgs a, int epi) 
             int q;
             const int pj = slot_of(st, rlo + k, q);
             const float2 f = a.fxy[pj];
-            s_xy[k] = make_float2(f.x + st.shx[q], f.y + st.shy[q]);
+            s_xy[k] = make_float2(f.x + shift_x(q, sc.cell_f), f.y + shift_y(q, sc.cell_f));
             s_phi[k] = a.sphi[pj];
             s_p[k] = pj;
             if constexpr (KIND == kKindCos2) s_d[k] = a.dphi_s[pj];

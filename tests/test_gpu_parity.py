@@ -24,11 +24,19 @@ TRAJ_TOL = 1e-9
 PRM0 = dict(v0=0.01, sigma=1.0, rho=0.1, alpha=1.45, D_phi=0.005)
 
 
+# neighbour-pass kernels: cell-tile (one CTA per cell) and warp-per-cell;
+# the value is the SPARSE_BELOW tuning that sends every system to that kernel
+KERNELS = {"tile": 0.0, "warp": 1e9}
+
+
 def gpu(n, L, prm, stepper, model=abi.MODEL_CHIMERA, precision=abi.PRECISION_FP64,
-        neighbour=abi.NEIGHBOUR_CELL, flags=0, seed=0):
+        neighbour=abi.NEIGHBOUR_CELL, flags=0, seed=0, kernel=None):
     p = abi.make_params(L=L, stepper=stepper, model=model, precision=precision,
                         neighbour=neighbour, flags=flags, seed=seed, **prm)
-    return abi.System(n, p)
+    s = abi.System(n, p)
+    if kernel is not None:
+        s.set_tuning(abi.TUNE_SPARSE_BELOW, KERNELS[kernel])
+    return s
 
 
 def golden_stepper(g):
@@ -47,12 +55,13 @@ def test_device_philox_known_answers(ctr, key, expect):
     assert abi.philox4x32_10(ctr, key) == expect
 
 
+@pytest.mark.parametrize("kernel", sorted(KERNELS))
 @pytest.mark.parametrize("name", golden_cases())
-def test_trajectory_matches_reference_golden(name):
+def test_trajectory_matches_reference_golden(name, kernel):
     g = load_golden(name)
     n, L = int(g["n"]), float(g["L"])
     model = abi.MODEL_VORTEX if "omega" in g else abi.MODEL_CHIMERA
-    with gpu(n, L, golden_params(g), golden_stepper(g), model=model) as s:
+    with gpu(n, L, golden_params(g), golden_stepper(g), model=model, kernel=kernel) as s:
         s.upload_state(g["state0"])
         if "omega" in g:
             s.upload_omega(g["omega"])
@@ -77,13 +86,14 @@ def _phase_rate_ok(got, ref, scale, v0):
     assert not bad.any(), (np.flatnonzero(bad)[:5], got[bad][:3], ref[bad][:3])
 
 
+@pytest.mark.parametrize("kernel", sorted(KERNELS))
 @pytest.mark.parametrize("name", golden_cases())
-def test_rhs_matches_reference_golden(name):
+def test_rhs_matches_reference_golden(name, kernel):
     g = load_golden(name)
     n, L = int(g["n"]), float(g["L"])
     prm = golden_params(g)
     o = po.OracleSystem(n, L, **prm)
-    with gpu(n, L, prm, abi.STEPPER_RK4) as s:
+    with gpu(n, L, prm, abi.STEPPER_RK4, kernel=kernel) as s:
         s.upload_state(g["state0"])
         kn = s.rhs_rk(g["k_prev"], float(g["k_coef"]), float(g["dt"]), g["k_next_init"])
         stage = g["state0"] + float(g["k_coef"]) * float(g["dt"]) * g["k_prev"]
@@ -162,12 +172,13 @@ def _oracle_run(n, L, prm, kind, state, dt, nsteps, noise=None, omega=None):
     (abi.STEPPER_RK4, 4096, 4.0, dict(v0=0.01, sigma=1.0, rho=0.25, alpha=1.45, D_phi=0.0), 100, 0.01),
     (abi.STEPPER_EULER, 256, 0.5, dict(PRM0, rho=0.15), 100, 0.01),
 ])
-def test_100_step_trajectory_with_philox_noise(stepper, n, L, prm, nsteps, dt):
+@pytest.mark.parametrize("kernel", sorted(KERNELS))
+def test_100_step_trajectory_with_philox_noise(stepper, n, L, prm, nsteps, dt, kernel):
     st0 = init_state(n, L, 21)
     vortex = stepper == abi.STEPPER_SRK
     omega = np.random.default_rng(22).normal(0, 0.5, n) if vortex else None
     with gpu(n, L, prm, stepper, model=abi.MODEL_VORTEX if vortex else abi.MODEL_CHIMERA,
-             seed=1234) as s:
+             seed=1234, kernel=kernel) as s:
         s.upload_state(st0)
         if vortex:
             s.upload_omega(omega)
@@ -244,15 +255,64 @@ def test_order_parameters_match_oracle():
         assert abs(got[k] - ref[k]) <= 1e-12
 
 
-def test_fp32c_rhs_error_is_small():
+@pytest.mark.parametrize("kernel", sorted(KERNELS))
+def test_fp32c_rhs_error_is_small(kernel):
     g = load_golden("chimera_euler_n1024")
     n, L = int(g["n"]), float(g["L"])
     prm = golden_params(g)
     o = po.OracleSystem(n, L, **prm)
     off, idx = o.neighbour_lists(g["state0"])
     scale, counts = alignment_scale(g["state0"], off, idx, prm["sigma"], prm["alpha"])
-    with gpu(n, L, prm, abi.STEPPER_SRK, precision=abi.PRECISION_FP32C) as s:
+    with gpu(n, L, prm, abi.STEPPER_SRK, precision=abi.PRECISION_FP32C, kernel=kernel) as s:
         s.upload_state(g["state0"])
         d, _ = s.rhs_srk()
     err = np.abs(d[2::3] - g["srk_derivative"][2::3])
     assert np.all(err <= 2e-6 * np.maximum(scale, 1e-3))
+
+
+@pytest.mark.parametrize("stepper", [abi.STEPPER_EULER, abi.STEPPER_SRK, abi.STEPPER_RK4])
+def test_fp64_kernels_agree_bitwise(stepper):
+    """Both neighbour kernels sum every particle's terms in the reference's
+    visiting order with the same FP64 operations, so their FP64 trajectories
+    are identical bit for bit (sparse and dense cells, ragged cell sizes)."""
+    cases = [(3000, 1.7, dict(v0=0.02, sigma=1.3, rho=0.09, alpha=1.4, D_phi=0.01)),
+             (6000, 1.0, dict(v0=0.01, sigma=0.8, rho=0.2, alpha=1.2, D_phi=0.005))]
+    for n, L, prm in cases:
+        st0 = init_state(n, L, 51)
+        out = {}
+        for kernel in KERNELS:
+            with gpu(n, L, prm, stepper, seed=5, kernel=kernel) as s:
+                s.upload_state(st0)
+                s.step(0.01, 20)
+                out[kernel] = s.download_state()
+        assert np.array_equal(out["tile"], out["warp"])
+
+
+def test_fp32c_kernels_agree_closely():
+    """The FP32C form sums in a different order in the two kernels (blocked
+    per-thread Kahan sums vs per-lane Kahan sums and a shuffle tree); after
+    one SRK right-hand side the phase rates agree to float rounding."""
+    n, L = 3000, 1.7
+    prm = dict(v0=0.02, sigma=1.3, rho=0.09, alpha=1.4, D_phi=0.01)
+    st0 = init_state(n, L, 52)
+    out = {}
+    for kernel in KERNELS:
+        with gpu(n, L, prm, abi.STEPPER_SRK, precision=abi.PRECISION_FP32C, kernel=kernel) as s:
+            s.upload_state(st0)
+            out[kernel] = s.rhs_srk()
+    d_t, a_t = out["tile"]
+    d_w, a_w = out["warp"]
+    assert np.array_equal(d_t[0::3], d_w[0::3]) and np.array_equal(d_t[1::3], d_w[1::3])
+    assert np.abs(d_t[2::3] - d_w[2::3]).max() <= 1e-5 * prm["sigma"]
+    assert np.abs(a_t - a_w).max() <= 1e-5
+
+
+def test_tuning_knob_round_trip():
+    with gpu(256, 1.0, PRM0, abi.STEPPER_EULER) as s:
+        assert s.get_tuning(abi.TUNE_SPARSE_BELOW) == 24.0
+        s.set_tuning(abi.TUNE_SPARSE_BELOW, 3.5)
+        assert s.get_tuning(abi.TUNE_SPARSE_BELOW) == 3.5
+        with pytest.raises(abi.SpcError):
+            s.set_tuning(abi.TUNE_SPARSE_BELOW, -1.0)
+        with pytest.raises(abi.SpcError):
+            s.set_tuning(99, 1.0)
