@@ -29,7 +29,7 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 WORKLOAD = dict(name="vortex_srk_n65536_L8", n=65536, L=8.0, v0=0.02, sigma=2.0, rho=0.25,
-                alpha=0.0, D_phi=0.01, dt=0.005, seed=1, omega_sd=0.5)
+                alpha=0.0, D_phi=0.01, dt=0.005, seed=1, omega_sd=0.5, skin=0.05)
 SIM_STEPS_PER_BENCH_STEP = 100
 # Algorithmic (compulsory) HBM bytes per particle for one SRK step, by phase,
 # for state resident in HBM: doubles x, y, phi (24 B), omega (8 B), the cell
@@ -202,41 +202,55 @@ def run_drift(steps=10000, every=100, out_path=None):
     the same state with the same Philox counters (FP32C draws the same Philox
     words through float Box-Muller), global R and local R every `every` steps.
     (2) The Chimera Euler workload (N=1,024, L=1, rho=0.1): FP32C and FP64 on the
-    GPU and the CPU oracle, all three fed the identical normals (exported from
-    the FP64 run and injected into the others).  Reports max |delta| over time."""
+    GPU and the CPU oracle, all fed the identical normals (exported from the FP64
+    run and injected into the others).
+    Both also run FP64 from the initial state with every phase moved by one ulp:
+    its drift is the dynamics' own sensitivity, the floor for any perturbation.
+    Reports max and mean |delta| over the recorded points."""
     from oracle import pyoracle as po
     from spc2_langevin_integration_gb300 import abi
-    res = {}
+
+    def stats(ref, got):
+        # pointwise |delta| over the recorded points, and the time means of both
+        # series over the second half of the run (the statistical comparison)
+        ref, got = np.asarray(ref), np.asarray(got)
+        d = np.abs(got - ref)
+        h = len(ref) // 2
+        return {"max_abs": float(d.max()), "mean_abs": float(d.mean()),
+                "time_mean_ref": float(ref[h:].mean()), "time_mean": float(got[h:].mean()),
+                "time_sd_ref": float(ref[h:].std())}
+
+    res, dump = {}, {}
     # (1) vortex SRK N=65536
     w = WORKLOAD
     st, omega = init_inputs(w)
+    st_ulp = st.copy()
+    st_ulp[2::3] = np.nextafter(st[2::3], np.inf)
     series = {}
-    for name, prec in (("fp64", abi.PRECISION_FP64), ("fp32c", abi.PRECISION_FP32C)):
+    for name, prec, s0 in (("fp64", abi.PRECISION_FP64, st), ("fp32c", abi.PRECISION_FP32C, st),
+                           ("fp64_ulp", abi.PRECISION_FP64, st_ulp)):
         p = abi.make_params(L=w["L"], v0=w["v0"], sigma=w["sigma"], rho=w["rho"], alpha=w["alpha"],
                             D_phi=w["D_phi"], model=abi.MODEL_VORTEX, stepper=abi.STEPPER_SRK,
                             precision=prec, seed=w["seed"])
         rows = []
         with abi.System(w["n"], p) as s:
-            s.upload_state(st)
+            s.upload_state(s0)
             s.upload_omega(omega)
-            o = s.order_params()
-            rows.append((0, o["R"], o["R_local"]))
             for k in range(every, steps + 1, every):
                 s.step(w["dt"], every, graph=True)
                 o = s.order_params()
                 rows.append((k, o["R"], o["R_local"]))
-        series[name] = rows
-    a, b = np.array(series["fp64"]), np.array(series["fp32c"])
+        series[name] = np.array(rows)
+    a64 = series["fp64"]
     res["vortex_srk_n65536"] = {
         "steps": steps, "every": every, "reference": "FP64 GPU path (same Philox counters)",
-        "max_abs_dR": float(np.abs(a[:, 1] - b[:, 1]).max()),
-        "max_abs_dR_local": float(np.abs(a[:, 2] - b[:, 2]).max()),
-        "final": {"fp64": {"R": a[-1, 1], "R_local": a[-1, 2]},
-                  "fp32c": {"R": b[-1, 1], "R_local": b[-1, 2]}},
-        "mean_abs_dR": float(np.abs(a[:, 1] - b[:, 1]).mean()),
-        "mean_abs_dR_local": float(np.abs(a[:, 2] - b[:, 2]).mean()),
-        "series": {"step": a[:, 0].tolist(), "R_fp64": a[:, 1].tolist(), "R_fp32c": b[:, 1].tolist(),
-                   "Rl_fp64": a[:, 2].tolist(), "Rl_fp32c": b[:, 2].tolist()}}
+        "fp32c": {"R": stats(a64[:, 1], series["fp32c"][:, 1]),
+                  "R_local": stats(a64[:, 2], series["fp32c"][:, 2])},
+        "fp64_one_ulp_phases": {"R": stats(a64[:, 1], series["fp64_ulp"][:, 1]),
+                                "R_local": stats(a64[:, 2], series["fp64_ulp"][:, 2])},
+        "final_R": {k: float(v[-1, 1]) for k, v in series.items()},
+        "final_R_local": {k: float(v[-1, 2]) for k, v in series.items()}}
+    dump["vortex_srk_n65536"] = {k: v.tolist() for k, v in series.items()}
     # (2) Chimera Euler N=1024 against the CPU oracle with identical noise
     n, L, dt = 1024, 1.0, 0.01
     prm = dict(v0=0.01, sigma=1.0, rho=0.1, alpha=1.45, D_phi=0.005)
@@ -245,38 +259,40 @@ def run_drift(steps=10000, every=100, out_path=None):
     st0[0::3] = rng.uniform(0.0, L, n)
     st0[1::3] = rng.uniform(0.0, L, n)
     st0[2::3] = rng.uniform(-np.pi, np.pi, n)
+    st0u = st0.copy()
+    st0u[2::3] = np.nextafter(st0[2::3], np.inf)
     orc = po.OracleSystem(n, L, **prm)
     ref = st0.copy()
     t_ref = 0.0
     rows = []
-    with abi.System(n, abi.make_params(L=L, stepper=abi.STEPPER_EULER, seed=0, **prm)) as s64, \
-            abi.System(n, abi.make_params(L=L, stepper=abi.STEPPER_EULER, seed=0,
-                                          precision=abi.PRECISION_FP32C, **prm)) as s32:
+    mk = lambda prec: abi.System(n, abi.make_params(L=L, stepper=abi.STEPPER_EULER, seed=0,  # noqa: E731
+                                                    precision=prec, **prm))
+    with mk(abi.PRECISION_FP64) as s64, mk(abi.PRECISION_FP32C) as s32, mk(abi.PRECISION_FP64) as s64u:
         s64.upload_state(st0)
         s32.upload_state(st0)
+        s64u.upload_state(st0u)
         for k in range(every, steps + 1, every):
             noise = s64.export_noise(k - every, every)
             s32.inject_noise(noise)
-            s64.step(dt, every)
-            s32.step(dt, every)
+            s64u.inject_noise(noise)
+            for s in (s64, s32, s64u):
+                s.step(dt, every)
             t_ref = orc.run(po.EULER, ref, t_ref, dt, every, noise)
-            o64, o32, oo = s64.order_params(), s32.order_params(), orc.order_params(ref)
-            rows.append((k, oo["R"], o64["R"], o32["R"], oo["R_local"], o64["R_local"], o32["R_local"]))
+            oo = orc.order_params(ref)
+            og = [s.order_params() for s in (s64, s32, s64u)]
+            rows.append([k, oo["R"], oo["R_local"]] + [v for o in og for v in (o["R"], o["R_local"])])
     r = np.array(rows)
     res["chimera_euler_n1024"] = {
         "steps": steps, "every": every, "reference": "CPU oracle (identical injected normals)",
-        "fp64_gpu": {"max_abs_dR": float(np.abs(r[:, 2] - r[:, 1]).max()),
-                     "max_abs_dR_local": float(np.abs(r[:, 5] - r[:, 4]).max())},
-        "fp32c_gpu": {"max_abs_dR": float(np.abs(r[:, 3] - r[:, 1]).max()),
-                      "max_abs_dR_local": float(np.abs(r[:, 6] - r[:, 4]).max())},
-        "final": {"oracle": {"R": r[-1, 1], "R_local": r[-1, 4]},
-                  "fp64_gpu": {"R": r[-1, 2], "R_local": r[-1, 5]},
-                  "fp32c_gpu": {"R": r[-1, 3], "R_local": r[-1, 6]}}}
+        "fp64_gpu": {"R": stats(r[:, 1], r[:, 3]), "R_local": stats(r[:, 2], r[:, 4])},
+        "fp32c_gpu": {"R": stats(r[:, 1], r[:, 5]), "R_local": stats(r[:, 2], r[:, 6])},
+        "fp64_gpu_one_ulp_phases": {"R": stats(r[:, 1], r[:, 7]), "R_local": stats(r[:, 2], r[:, 8])},
+        "final_R": {"oracle": r[-1, 1], "fp64_gpu": r[-1, 3], "fp32c_gpu": r[-1, 5],
+                    "fp64_gpu_one_ulp_phases": r[-1, 7]}}
+    dump["chimera_euler_n1024"] = r.tolist()
     if out_path:
         with open(out_path, "w") as f:
-            json.dump(res, f)
-    for v in res.values():
-        v.pop("series", None)
+            json.dump(dump, f)
     return res
 
 
@@ -302,12 +318,16 @@ def reduce_max(dist, v):
     return float(t.item())
 
 
-def run_form(abi, torch, w, precision, steps, warmup, rank, dist):
+def run_form(abi, torch, w, precision, steps, warmup, rank, dist, neighbour=None, e2e=True):
+    """Device-timed graph replays of the workload; then (e2e) the same through
+    the C-ABI with host buffers, and a per-phase profile."""
     n = w["n"]
     st, omega = init_inputs(w, seed_offset=rank)
     p = abi.make_params(L=w["L"], v0=w["v0"], sigma=w["sigma"], rho=w["rho"], alpha=w["alpha"],
                         D_phi=w["D_phi"], model=abi.MODEL_VORTEX, stepper=abi.STEPPER_SRK,
-                        precision=precision, seed=w["seed"], system_id=rank)
+                        precision=precision, seed=w["seed"], system_id=rank,
+                        neighbour=abi.NEIGHBOUR_VERLET if neighbour is None else neighbour,
+                        skin=w["skin"])
     s = abi.System(n, p)
     s.upload_state(st)
     s.upload_omega(omega)
@@ -333,6 +353,10 @@ def run_form(abi, torch, w, precision, steps, warmup, rank, dist):
         dist.barrier()
     ms = sum(a.elapsed_time(b) for a, b in ev)
     ms = reduce_max(dist, ms)
+    if not e2e:
+        prof = s.profile_steps(dt, 20)
+        s.close()
+        return ms, None, prof, None
     # e2e through the C-ABI with host buffers: pinned upload, 100 steps, download
     import ctypes as C
     L = abi.lib()
@@ -370,6 +394,8 @@ def main():
                     help="run a few plain (ungraphed) steps of the workload (or of an ensemble of "
                          "--ensemble-systems systems) for an ncu capture")
     ap.add_argument("--ensemble-systems", type=int, default=512)
+    ap.add_argument("--cell-list", action="store_true",
+                    help="--ncu-case fp32c/fp64: the cell-list passes instead of the Verlet rows")
     ap.add_argument("--workload", choices=["vortex", "ensemble", "serve", "drift"], default="vortex",
                     help="vortex: the headline single-system line; ensemble: 512 systems in one "
                          "batch; serve: the Poisson request stream; drift: FP32C vs FP64 order "
@@ -441,7 +467,9 @@ def main():
         prec = abi.PRECISION_FP32C if args.ncu_case == "fp32c" else abi.PRECISION_FP64
         p = abi.make_params(L=w["L"], v0=w["v0"], sigma=w["sigma"], rho=w["rho"],
                             alpha=w["alpha"], D_phi=w["D_phi"], model=abi.MODEL_VORTEX,
-                            stepper=abi.STEPPER_SRK, precision=prec, seed=w["seed"])
+                            stepper=abi.STEPPER_SRK, precision=prec, seed=w["seed"],
+                            neighbour=abi.NEIGHBOUR_CELL if args.cell_list else abi.NEIGHBOUR_VERLET,
+                            skin=w["skin"])
         with abi.System(w["n"], p) as s:
             s.upload_state(st)
             s.upload_omega(omega)
@@ -452,7 +480,8 @@ def main():
     world, rank, local, dist = dist_setup(args)
     n_total = w["n"] * world
     config = {"workload": w["name"], "N": w["n"], "L": w["L"], "stepper": "srk",
-              "model": "vortex (alignment + natural frequencies)", "neighbour": "cell",
+              "model": "vortex (alignment + natural frequencies)",
+              "neighbour": "verlet rows, skin %g (r_max = rho + skin)" % w["skin"],
               "dt": w["dt"], "sim_steps_per_bench_step": SIM_STEPS_PER_BENCH_STEP,
               "l2": "flushed between bench steps (512 MB write, outside the timed events)",
               "parallelism": f"replicas{world}"}
@@ -487,6 +516,9 @@ def main():
                                             args.warmup, rank, dist)
         ms64, e2e64, prof64, R64 = run_form(abi, torch, w, abi.PRECISION_FP64,
                                             max(2, args.steps // 2), args.warmup, rank, dist)
+        steps_c = max(2, args.steps // 2)
+        msc, _, profc, _ = run_form(abi, torch, w, abi.PRECISION_FP32C, steps_c, args.warmup, rank,
+                                    dist, neighbour=abi.NEIGHBOUR_CELL, e2e=False)
     steps64 = max(2, args.steps // 2)
     psteps = n_total * SIM_STEPS_PER_BENCH_STEP
     value = psteps * args.steps / (ms32 / 1e3)
@@ -506,6 +538,7 @@ def main():
         "fp64": {"value": value64, "ms_per_step": ms64 / steps64, "profile_ms": prof64,
                  "order_params": R64},
         "fp32c_over_fp64": value / value64,
+        "fp32c_cell_list": {"value": psteps * steps_c / (msc / 1e3), "profile_ms": profc},
         "order_params_fp32c": R32,
         "gpu_launches": None,
         "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm,

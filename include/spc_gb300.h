@@ -168,7 +168,10 @@ int spc_diagnostics(spc_handle *h, int64_t *clamped_cells, int64_t *verlet_rebui
  * the average milliseconds per step of: [0] stage + cell keys, [1] radix
  * sort, [2] cell bounds + cell-order gather, [3] first neighbour pass
  * (with its fused epilogue), [4] second neighbour pass (SRK) or the other
- * RK4 passes, [5] the whole step.  cap is out_ms's length (>= 6). */
+ * RK4 passes, [5] the whole step.  On a Verlet handle [0] is the refresh of
+ * the Verlet-order state (with the displacement test), [1] the cell binning
+ * and [2] the row build, both of which return at once unless the rows must be
+ * rebuilt.  cap is out_ms's length (>= 6). */
 int spc_profile_steps(spc_handle *h, double dt, int32_t nsteps, double *out_ms, int32_t cap);
 
 /* Tuning knobs (no counterpart in the reference; results do not depend on
@@ -176,8 +179,13 @@ int spc_profile_steps(spc_handle *h, double dt, int32_t nsteps, double *out_ms, 
  * SPC_TUNE_SPARSE_BELOW: cell-list systems with fewer particles per cell
  * than this value (on average) run the warp-per-cell neighbour passes, the
  * others the cell-tile passes; 0 sends every system to the cell-tile passes.
- * Default 24.  spc_get_tuning reads a knob back. */
-enum { SPC_TUNE_SPARSE_BELOW = 1 };
+ * Default 24.
+ * SPC_TUNE_VERLET_ROW_LIMIT (Verlet handles only): the longest neighbour row
+ * kept; a particle with more candidates within rho + skin scans its whole
+ * cell stencil instead (same results).  Between 1 and the row capacity the
+ * handle allocated (its default value); the rows are rebuilt on the next step.
+ * spc_get_tuning reads a knob back. */
+enum { SPC_TUNE_SPARSE_BELOW = 1, SPC_TUNE_VERLET_ROW_LIMIT = 2 };
 int spc_set_tuning(spc_handle *h, int32_t key, double value);
 int spc_get_tuning(const spc_handle *h, int32_t key, double *value);
 

@@ -85,6 +85,14 @@ int spc_create(const spc_params *p, int32_t n, spc_handle **out) {
   h->n = n;
   const SysConst sc = make_sysconst(*p, n);
   rc = engine_init(&h->e, p->stepper, p->precision, n, 1, sc.allpairs ? 1 : sc.ncell);
+  if (rc == SPC_OK && sc.vR > 0) {
+    // rows of about pi r_max^2 n / L^2 entries: room for twice that (and for
+    // eight standard deviations of a uniform layout), at most 1024
+    const double rmax = p->rho + p->skin;
+    const double mean = 3.141592653589793 * rmax * rmax * (double)n / (p->L * p->L);
+    const double want = std::max(2.0 * mean, mean + 8.0 * std::sqrt(mean)) + 64.0;
+    rc = engine_init_verlet(&h->e, ((int)want + 31) / 32 * 32);
+  }
   if (rc == SPC_OK) rc = engine_admit(&h->e, *p, n, -1, &h->slot);
   if (rc == SPC_OK) {
     Engine &e = h->e;
@@ -282,6 +290,7 @@ int spc_rhs_rk(spc_handle *h, const double *k_prev, double k_coef, double dt, do
   SPC_LAUNCHED(e);
   KArgs a = base;
   a.dt = dt;
+  SPC_TRY(verlet_prepare(e));
   SPC_TRY(open_eval(e, 1));
   SPC_TRY(eval_stage(e, a, 1, 4, k_coef * dt));
   a.kq_out = 5;
@@ -304,6 +313,7 @@ int spc_rhs_srk(spc_handle *h, double *derivative, double *additional) {
   KArgs a = e->a;
   a.out_d = e->aos;
   a.out_a = e->aos + 3 * N;
+  SPC_TRY(verlet_prepare(e));
   SPC_TRY(eval_stage(e, a, 0, -1, 0.0));
   SPC_TRY(launch_pass(e, a, kKindSin, kEpiSrk1));
   SPC_TRY(launch_pass(e, a, kKindCos2, kEpiSrk2Out));
@@ -323,7 +333,7 @@ int spc_neighbours(spc_handle *h, int32_t *counts, int32_t *idx, int64_t cap, in
   KArgs a = e->a;
   int *d_cnt = (int *)e->aos;
   a.out_cnt = d_cnt;
-  SPC_TRY(eval_stage(e, a, 0, -1, 0.0));
+  SPC_TRY(eval_stage(e, a, 0, -1, 0.0, false));
   SPC_TRY(launch_pass(e, a, kKindNb, kEpiCount));
   SPC_CUDA(e, cudaMemcpyAsync(counts, d_cnt, N * 4, cudaMemcpyDeviceToHost, e->stream));
   SPC_CUDA(e, cudaStreamSynchronize(e->stream));
@@ -361,7 +371,7 @@ int spc_order_params(spc_handle *h, double *R, double *psi, double *R_local) {
     const size_t N = h->n;
     KArgs a = e->a;
     a.out_r = e->aos;
-    SPC_TRY(eval_stage(e, a, 0, -1, 0.0));
+    SPC_TRY(eval_stage(e, a, 0, -1, 0.0, false));
     SPC_TRY(launch_pass(e, a, kKindNb, kEpiLocalOrder));
     std::vector<double> r(N);
     SPC_CUDA(e, cudaMemcpyAsync(r.data(), a.out_r, N * 8, cudaMemcpyDeviceToHost, e->stream));
@@ -381,7 +391,12 @@ int spc_diagnostics(spc_handle *h, int64_t *clamped_cells, int64_t *verlet_rebui
   SPC_CUDA(e, cudaMemcpyAsync(&c, e->d_clamped, 8, cudaMemcpyDeviceToHost, e->stream));
   SPC_CUDA(e, cudaStreamSynchronize(e->stream));
   if (clamped_cells) *clamped_cells = (int64_t)c;
-  if (verlet_rebuilds) *verlet_rebuilds = 0;
+  unsigned long long vb = 0;
+  if (e->verlet) {
+    SPC_CUDA(e, cudaMemcpyAsync(&vb, e->vrebuilds, 8, cudaMemcpyDeviceToHost, e->stream));
+    SPC_CUDA(e, cudaStreamSynchronize(e->stream));
+  }
+  if (verlet_rebuilds) *verlet_rebuilds = (int64_t)vb;
   if (error_word) *error_word = 0;
   return SPC_OK;
 }

@@ -34,6 +34,10 @@ struct SysConst {
   int exact_all;  // decide every candidate in FP64
   int L_pow2;     // L is a power of two: x / L == x * (1 / L) exactly
   float cos_a, sin_a;  // FP32C: cos(alpha), sin(alpha) rounded to float
+  // Verlet rows (vR = 0: the system uses the cell-list passes)
+  int vR;         // stencil radius in cells, ceil(r_max / cell)
+  float vr2;      // build: candidates with float dr^2 <= vr2 (r_max^2 plus a margin) are listed
+  double vdisp2;  // a displacement with dr^2 > vdisp2 (about (skin / 2)^2) forces a rebuild
 };
 
 // PeriodicBoundaryConditions::ClassAEffectiveParticleDistance (PeriodicBoundaryConditions.cpp:22-35):

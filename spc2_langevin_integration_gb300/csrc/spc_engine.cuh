@@ -28,6 +28,7 @@
 #include "spc_sort.cuh"
 #include "spc_tile.cuh"
 #include "spc_warp.cuh"
+#include "spc_verlet.cuh"
 
 namespace spc {
 
@@ -80,6 +81,17 @@ inline SysConst make_sysconst(const spc_params &p, int n) {
   sc.L_pow2 = is_pow2(p.L);
   sc.cos_a = (float)std::cos(p.alpha);
   sc.sin_a = (float)std::sin(p.alpha);
+  // Verlet rows over a (2R+1)^2 stencil of rho-cells; needs 2R+1 distinct cells
+  if (p.neighbour == SPC_NEIGHBOUR_VERLET && !sc.allpairs) {
+    const double rmax = p.rho + p.skin;
+    const int R = (int)std::ceil(rmax / sc.cell);
+    if (R >= 1 && R <= kVMaxR && sc.nc >= 2 * R + 1) {
+      sc.vR = R;
+      sc.vr2 = (float)(rmax * rmax * (1.0 + 1e-4));
+      const double h = 0.5 * p.skin * (1.0 - 1e-6);
+      sc.vdisp2 = h * h;
+    }
+  }
   return sc;
 }
 
@@ -167,6 +179,14 @@ struct Engine {
   bool profiling = false;
   // an engine that is a view over caller-provided memory owns nothing
   bool view = false;
+  // Verlet rows (single-system handles whose parameters ask for them)
+  bool verlet = false;
+  bool verlet_stale = true;  // the build tables are not valid: force a build
+  int vcap_alloc = 0;        // row capacity allocated
+  uint16_t *vrows = nullptr;
+  int *vrowlen = nullptr, *vsys = nullptr, *vcell = nullptr, *vflags = nullptr;
+  double *vxb = nullptr, *vyb = nullptr;
+  unsigned long long *vrebuilds = nullptr;
 };
 
 inline int fail(Engine *e, int code, const char *fmt, ...) {
@@ -312,6 +332,49 @@ inline int engine_init(Engine *e, int stepper, int precision, int pool_cap, int 
   return SPC_OK;
 }
 
+// Verlet buffers for rows of up to `cap` entries (cap <= 1024, so that the
+// FP32C pass-1 bits of a row fit the 32 mask words of a particle).
+inline int engine_init_verlet(Engine *e, int cap) {
+  const size_t N = (size_t)e->pool_cap;
+  cap = std::max(32, std::min(cap, kMaskWords * kWarp));
+  e->verlet = true;
+  e->vcap_alloc = cap;
+  SPC_TRY(dalloc(e, &e->vrows, (size_t)cap * N));
+  SPC_TRY(dalloc(e, &e->vrowlen, N));
+  SPC_TRY(dalloc(e, &e->vsys, N));
+  SPC_TRY(dalloc(e, &e->vcell, N));
+  SPC_TRY(dalloc(e, &e->vxb, N));
+  SPC_TRY(dalloc(e, &e->vyb, N));
+  SPC_TRY(dalloc(e, &e->vflags, 2));
+  SPC_TRY(dalloc(e, &e->vrebuilds, 1));
+  cudaStream_t st = e->stream;
+  SPC_CUDA(e, cudaMemsetAsync(e->vrowlen, 0, N * 4, st));
+  SPC_CUDA(e, cudaMemsetAsync(e->vsys, 0, N * 4, st));
+  SPC_CUDA(e, cudaMemsetAsync(e->vcell, 0, N * 4, st));
+  SPC_CUDA(e, cudaMemsetAsync(e->vflags, 0, 8, st));
+  SPC_CUDA(e, cudaMemsetAsync(e->vrebuilds, 0, 8, st));
+  SPC_CUDA(e, cudaStreamSynchronize(st));
+  KArgs &a = e->a;
+  a.vrows = e->vrows;
+  a.vrowlen = e->vrowlen;
+  a.vcap = cap;
+  a.vxb = e->vxb;
+  a.vyb = e->vyb;
+  a.vflags = e->vflags;
+  a.vrebuilds = e->vrebuilds;
+  e->verlet_stale = true;
+  return SPC_OK;
+}
+
+// Before enqueueing evaluations (outside any graph capture): a stale build is
+// forced through the device flag that the next gather reads.
+inline int verlet_prepare(Engine *e) {
+  if (!e->verlet || !e->verlet_stale) return SPC_OK;
+  SPC_CUDA(e, cudaMemsetAsync(e->vflags + 1, 1, 1, e->stream));
+  e->verlet_stale = false;
+  return SPC_OK;
+}
+
 inline void engine_free(Engine *e) {
   if (!e || e->view) return;
   cudaSetDevice(e->device);
@@ -437,6 +500,7 @@ inline int system_class(const Engine *e, const SysHost &h) {
 inline int engine_layout(Engine *e) {
   if (!e->dirty) return SPC_OK;
   drop_graph(e);
+  e->verlet_stale = true;  // slots and systems move: rebuild the rows
   std::vector<SysDesc> table;
   std::vector<int> ap;
   int dense = 0, cells = 0;
@@ -498,34 +562,73 @@ inline void mark(Engine *e, int slot) {
   if (e->profiling) cudaEventRecord(e->prof_ev[slot], e->stream);
 }
 
-// One evaluation's binning: stage, sort, cell bounds, cell-order gather.
-inline int eval_stage(Engine *e, KArgs &a, int rk_form, int kq, double kcdt) {
+inline int eval_cells(Engine *e, KArgs &a, int rk_form, int kq, double kcdt, bool marks = true);
+
+// One evaluation's binning.  Verlet engines: refresh the Verlet-order copies
+// of the stage state and rebuild the rows when the displacement test (or a
+// stale build) asks for it; the rebuild is the cell-list binning plus the row
+// build, all gated on the device flag.  verlet_ok = false (diagnostics, which
+// need the reference's current cells) runs the cell-list binning and leaves
+// the build stale.
+inline int eval_stage(Engine *e, KArgs &a, int rk_form, int kq, double kcdt, bool verlet_ok = true) {
+  if (!e->verlet) return eval_cells(e, a, rk_form, kq, kcdt);
+  if (!verlet_ok) {
+    e->verlet_stale = true;
+    return eval_cells(e, a, rk_form, kq, kcdt);
+  }
+  const int n = e->n_active;
+  cudaStream_t st = e->stream;
+  // the gather and the rebuild see the build tables; the caller's arguments
+  // (and the cell-list path's) leave them null
+  KArgs b = a;
+  b.gate = e->vflags;
+  b.vsys = e->vsys;
+  b.vcell = e->vcell;
+  if (e->precision == SPC_PRECISION_FP32C)
+    k_vgather<kPrecFP32C><<<blocks_for(n, 256), 256, 0, st>>>(b, rk_form, kq, kcdt);
+  else
+    k_vgather<kPrecFP64><<<blocks_for(n, 256), 256, 0, st>>>(b, rk_form, kq, kcdt);
+  SPC_LAUNCHED(e);
+  mark(e, 1);
+  SPC_TRY(eval_cells(e, b, rk_form, kq, kcdt, false));
+  mark(e, 2);
+  k_verlet_build<<<std::min(std::max(e->ncell_total, 1), 152 * 16), kVThreads, 0, st>>>(b);
+  SPC_LAUNCHED(e);
+  mark(e, 3);
+  a.skeys = b.skeys;
+  a.svals = b.svals;
+  return SPC_OK;
+}
+
+// Cell-list binning: stage, sort, cell bounds, cell-order gather.  marks:
+// record the profiling events after each part.
+inline int eval_cells(Engine *e, KArgs &a, int rk_form, int kq, double kcdt, bool marks) {
   const int n = e->n_active;
   cudaStream_t st = e->stream;
   const int bits = e->radix_bits;
   k_stage<<<blocks_for(n, kStageThreads), kStageThreads, 0, st>>>(a, rk_form, kq, kcdt, bits, e->hist);
   SPC_LAUNCHED(e);
-  mark(e, 1);
+  if (marks) mark(e, 1);
   uint32_t *kin = a.keys, *vin = a.vals, *kout = e->keys_alt, *vout = e->vals_alt;
   for (int pass = 0; pass < e->sort_passes; ++pass) {
     const int shift = pass * bits;
-    if (pass > 0) k_radix_hist<<<e->ntiles, kSortThreads, 0, st>>>(kin, n, shift, bits, e->hist);
+    if (pass > 0) k_radix_hist<<<e->ntiles, kSortThreads, 0, st>>>(kin, n, shift, bits, e->hist, a.gate);
     if (e->ntiles <= kScanGroup) {
-      k_scan_digits<<<1, kScanThreads, 0, st>>>(e->hist, e->ntiles, bits);
+      k_scan_digits<<<1, kScanThreads, 0, st>>>(e->hist, e->ntiles, bits, a.gate);
     } else {
       const int ng = (e->ntiles + kScanGroup - 1) / kScanGroup;
       const dim3 grid(ng, blocks_for(1 << bits, 256));
-      k_scan_group_sums<<<grid, 256, 0, st>>>(e->hist, e->ntiles, bits, e->part);
-      k_scan_digits<<<1, kScanThreads, 0, st>>>(e->part, ng, bits);
-      k_scan_group_apply<<<grid, 256, 0, st>>>(e->hist, e->ntiles, bits, e->part);
+      k_scan_group_sums<<<grid, 256, 0, st>>>(e->hist, e->ntiles, bits, e->part, a.gate);
+      k_scan_digits<<<1, kScanThreads, 0, st>>>(e->part, ng, bits, a.gate);
+      k_scan_group_apply<<<grid, 256, 0, st>>>(e->hist, e->ntiles, bits, e->part, a.gate);
     }
     k_radix_scatter<<<e->ntiles, kSortThreads, scatter_smem_bytes(bits), st>>>(kin, vin, kout, vout, n,
-                                                                               shift, bits, e->hist);
+                                                                               shift, bits, e->hist, a.gate);
     SPC_LAUNCHED(e);
     std::swap(kin, kout);
     std::swap(vin, vout);
   }
-  mark(e, 2);
+  if (marks) mark(e, 2);
   a.skeys = kin;
   a.svals = vin;
   if (e->precision == SPC_PRECISION_FP32C)
@@ -533,7 +636,7 @@ inline int eval_stage(Engine *e, KArgs &a, int rk_form, int kq, double kcdt) {
   else
     k_gather<kPrecFP64><<<blocks_for(n + 1, 256), 256, 0, st>>>(a);
   SPC_LAUNCHED(e);
-  mark(e, 3);
+  if (marks) mark(e, 3);
   return SPC_OK;
 }
 
@@ -543,6 +646,13 @@ int launch_pass_t(Engine *e, const KArgs &a, int epi) {
   if (a.n_ap > 0) {
     k_allpairs_pass<PREC, KIND><<<std::min(a.n_ap, 152 * 16), kAllPairsThreads, 0, st>>>(a, epi);
     SPC_LAUNCHED(e);
+  }
+  if constexpr (KIND != kKindNb) {
+    if (e->has_cells && e->verlet) {
+      k_vtile<PREC, KIND><<<std::min(e->ncell_total, 152 * 256), kVThreads, 0, st>>>(a, epi);
+      SPC_LAUNCHED(e);
+      return SPC_OK;
+    }
   }
   if (e->has_cells) {
     if constexpr (KIND == kKindNb) {
@@ -642,6 +752,7 @@ inline int engine_steps(Engine *e, double dt, int nsteps, bool use_graph, const 
   SPC_TRY(engine_set_device(e));
   SPC_TRY(engine_layout(e));
   if (e->nsys == 0 || nsteps == 0) return SPC_OK;
+  SPC_TRY(verlet_prepare(e));
   const int sb = blocks_for(e->nsys, 128);
   if (!use_graph) {
     k_begin_call<<<sb, 128, 0, e->stream>>>(e->d_sys, e->nsys, nsteps);
@@ -681,6 +792,15 @@ inline int engine_steps(Engine *e, double dt, int nsteps, bool use_graph, const 
 }
 
 inline int engine_set_tuning(Engine *e, int key, double value) {
+  if (key == SPC_TUNE_VERLET_ROW_LIMIT) {
+    if (!e->verlet) return fail(e, SPC_ERR_STATE, "no Verlet rows on this handle");
+    if (!(value >= 1.0) || !(value <= (double)e->vcap_alloc))
+      return fail(e, SPC_ERR_INVALID, "row limit must be in [1, %d]", e->vcap_alloc);
+    e->a.vcap = (int)value;
+    e->verlet_stale = true;  // rebuild the rows under the new limit
+    drop_graph(e);
+    return SPC_OK;
+  }
   if (key == SPC_TUNE_SPARSE_BELOW) {
     if (!(value >= 0.0) || !std::isfinite(value)) return fail(e, SPC_ERR_INVALID, "sparse_below must be >= 0");
     if (value != e->sparse_below) {
@@ -693,6 +813,10 @@ inline int engine_set_tuning(Engine *e, int key, double value) {
 }
 
 inline int engine_get_tuning(const Engine *e, int key, double *value) {
+  if (key == SPC_TUNE_VERLET_ROW_LIMIT) {
+    *value = e->verlet ? (double)e->a.vcap : 0.0;
+    return SPC_OK;
+  }
   if (key == SPC_TUNE_SPARSE_BELOW) {
     *value = e->sparse_below;
     return SPC_OK;
@@ -707,6 +831,7 @@ inline int engine_profile(Engine *e, double dt, int nsteps, double *out_ms) {
   if (e->injecting) return fail(e, SPC_ERR_STATE, "profiling uses Philox noise");
   SPC_TRY(engine_set_device(e));
   SPC_TRY(engine_layout(e));
+  SPC_TRY(verlet_prepare(e));
   for (int k = 0; k < 6; ++k) {
     out_ms[k] = 0.0;
     if (!e->prof_ev[k]) SPC_CUDA(e, cudaEventCreate(&e->prof_ev[k]));

@@ -104,6 +104,15 @@ struct KArgs {
   int noise_m;                       // normals per particle
   int step_off;                      // this step = sys.step + step_off
   unsigned long long *clamped;
+  // Verlet rows (null / 0 on the cell-list path)
+  const int *gate;                   // binning kernels return at once when *gate == 0
+  int *vsys, *vcell;                 // build: system and cell of each cell-order slot
+  uint16_t *vrows;                   // row entry k of slot v at vrows[((k / 8) * n_active + v) * 8 + k % 8]
+  int *vrowlen;                      // entries of each row, -1: overflow (scan the stencil)
+  int vcap;                          // row limit of the current build
+  double *vxb, *vyb;                 // stage positions at the build
+  int *vflags;                       // [0] rebuild needed this evaluation, [1] forced
+  unsigned long long *vrebuilds;
 };
 
 // ---------------------------------------------------------------------------
@@ -119,6 +128,7 @@ constexpr int kMaxHistBits = 11;
 
 __global__ void __launch_bounds__(kStageThreads)
     k_stage(KArgs a, int rk_form, int kq, double kcdt, int hist_bits, uint32_t *hist) {
+  if (a.gate && *a.gate == 0) return;
   __shared__ uint32_t h[1 << kMaxHistBits];
   const int R = 1 << hist_bits;
   const int d = blockIdx.x * blockDim.x + threadIdx.x;
@@ -176,6 +186,7 @@ __device__ __forceinline__ float reduced_phase_f(double ph) {
 
 template <int PREC>
 __global__ void k_gather(KArgs a) {
+  if (a.gate && *a.gate == 0) return;
   const int p = blockIdx.x * blockDim.x + threadIdx.x;
   const int n = a.n_active;
   if (p > n) return;
@@ -192,6 +203,10 @@ __global__ void k_gather(KArgs a) {
   a.sy[p] = y;
   a.sphi[p] = ph;
   a.pidx[p] = sd.pool_p0 + (d - sd.dense_p0);
+  if (a.vsys) {  // Verlet build: remember each slot's system and cell until the next build
+    a.vsys[p] = a.sys_of_p[d];
+    a.vcell[p] = (int)a.skeys[p];
+  }
   if (!sc.allpairs) {
     const int key = (int)a.skeys[p] - sd.c0;
     const int cx = key % sc.nc, cy = key / sc.nc;

@@ -1,5 +1,8 @@
 // Stable LSD radix sort of 32-bit cell keys with a 32-bit particle-index
-// payload, and the cell start table derived from the sorted keys.
+// payload, and the cell start table derived from the sorted keys.  Every
+// kernel takes an optional device gate: when it points to 0 the kernel
+// returns at once (the Verlet path keeps its rebuild in a captured step and
+// runs it only on the evaluations that need one).
 //
 // This replaces the reference's serial linked-list rebuild
 // (`linked_list_[pre_linked_list_[i]].push_back(i)` for i = 0..N-1,
@@ -28,7 +31,8 @@ constexpr int kScanThreads = 1024;
 // Tile-major digit histogram of keys[tile*2048 ...] for the digit at `shift`.
 __global__ void __launch_bounds__(kSortThreads)
     k_radix_hist(const uint32_t *__restrict__ keys, int n, int shift, int bits,
-                 uint32_t *__restrict__ hist) {
+                 uint32_t *__restrict__ hist, const int *gate) {
+  if (gate && *gate == 0) return;
   __shared__ uint32_t h[1 << 11];
   const int R = 1 << bits;
   for (int d = threadIdx.x; d < R; d += blockDim.x) h[d] = 0;
@@ -49,7 +53,8 @@ __global__ void __launch_bounds__(kSortThreads)
 // coalesced loads), the block scans the digit totals with warp shuffles, and
 // the thread writes its digits' running prefixes back.
 __global__ void __launch_bounds__(kScanThreads)
-    k_scan_digits(uint32_t *__restrict__ hist, int ntiles, int bits) {
+    k_scan_digits(uint32_t *__restrict__ hist, int ntiles, int bits, const int *gate) {
+  if (gate && *gate == 0) return;
   __shared__ uint32_t wsum[kScanThreads / kWarp];
   const int R = 1 << bits;
   const int t = threadIdx.x, lane = t % kWarp, w = t / kWarp;
@@ -104,7 +109,8 @@ __global__ void __launch_bounds__(kScanThreads)
 constexpr int kScanGroup = 32;
 
 __global__ void k_scan_group_sums(const uint32_t *__restrict__ hist, int ntiles, int bits,
-                                  uint32_t *__restrict__ part) {
+                                  uint32_t *__restrict__ part, const int *gate) {
+  if (gate && *gate == 0) return;
   const int R = 1 << bits;
   const int d = blockIdx.y * blockDim.x + threadIdx.x, g = blockIdx.x;
   if (d >= R) return;
@@ -115,7 +121,8 @@ __global__ void k_scan_group_sums(const uint32_t *__restrict__ hist, int ntiles,
 }
 
 __global__ void k_scan_group_apply(uint32_t *__restrict__ hist, int ntiles, int bits,
-                                   const uint32_t *__restrict__ part) {
+                                   const uint32_t *__restrict__ part, const int *gate) {
+  if (gate && *gate == 0) return;
   const int R = 1 << bits;
   const int d = blockIdx.y * blockDim.x + threadIdx.x, g = blockIdx.x;
   if (d >= R) return;
@@ -133,7 +140,8 @@ __global__ void k_scan_group_apply(uint32_t *__restrict__ hist, int ntiles, int 
 __global__ void __launch_bounds__(kSortThreads)
     k_radix_scatter(const uint32_t *__restrict__ keys_in, const uint32_t *__restrict__ vals_in,
                     uint32_t *__restrict__ keys_out, uint32_t *__restrict__ vals_out, int n,
-                    int shift, int bits, const uint32_t *__restrict__ hist_scanned) {
+                    int shift, int bits, const uint32_t *__restrict__ hist_scanned, const int *gate) {
+  if (gate && *gate == 0) return;
   extern __shared__ uint32_t smem_sort[];
   const int R = 1 << bits;
   uint32_t *wcount = smem_sort;                      // [kSortWarps][R]
