@@ -318,17 +318,39 @@ def reduce_max(dist, v):
     return float(t.item())
 
 
-def run_form(abi, torch, w, precision, steps, warmup, rank, dist, neighbour=None, e2e=True):
+def workload_params(abi, w, precision, rank=0):
+    return abi.make_params(L=w["L"], v0=w["v0"], sigma=w["sigma"], rho=w["rho"], alpha=w["alpha"],
+                           D_phi=w["D_phi"], model=abi.MODEL_VORTEX, stepper=abi.STEPPER_SRK,
+                           precision=precision, seed=w["seed"], system_id=rank,
+                           neighbour=abi.NEIGHBOUR_VERLET, skin=w["skin"])
+
+
+def tune_form(abi, w, precision, rank=0):
+    """The autotuner's choice for this workload and precision (neighbour
+    method, skin, kernel class), with every candidate's ms per step."""
+    st, omega = init_inputs(w, seed_offset=rank)
+    t0 = time.perf_counter()
+    best, sb, ms = abi.autotune(w["n"], workload_params(abi, w, precision, rank), st, omega,
+                                dt=w["dt"], trial_steps=20)
+    names = ["cell (default kernels)", "cell (cell-tile)", "cell (warp-per-cell)"]
+    names += ["verlet skin %.3g" % (f * w["rho"]) for f in (0.1, 0.2, 0.4)][: len(ms) - 3]
+    info = {"choice": {"neighbour": "verlet" if best.neighbour == abi.NEIGHBOUR_VERLET else "cell",
+                       "skin": best.skin, "sparse_below": sb},
+            "candidates_ms_per_step": dict(zip(names, ms)),
+            "tuning_s": time.perf_counter() - t0}
+    return best, sb, info
+
+
+def run_form(abi, torch, w, precision, steps, warmup, rank, dist, params=None, sparse_below=None,
+             e2e=True):
     """Device-timed graph replays of the workload; then (e2e) the same through
     the C-ABI with host buffers, and a per-phase profile."""
     n = w["n"]
     st, omega = init_inputs(w, seed_offset=rank)
-    p = abi.make_params(L=w["L"], v0=w["v0"], sigma=w["sigma"], rho=w["rho"], alpha=w["alpha"],
-                        D_phi=w["D_phi"], model=abi.MODEL_VORTEX, stepper=abi.STEPPER_SRK,
-                        precision=precision, seed=w["seed"], system_id=rank,
-                        neighbour=abi.NEIGHBOUR_VERLET if neighbour is None else neighbour,
-                        skin=w["skin"])
+    p = params if params is not None else workload_params(abi, w, precision, rank)
     s = abi.System(n, p)
+    if sparse_below is not None and p.neighbour == abi.NEIGHBOUR_CELL:
+        s.set_tuning(abi.TUNE_SPARSE_BELOW, sparse_below)
     s.upload_state(st)
     s.upload_omega(omega)
     stream = torch.cuda.ExternalStream(s.stream)
@@ -481,7 +503,7 @@ def main():
     n_total = w["n"] * world
     config = {"workload": w["name"], "N": w["n"], "L": w["L"], "stepper": "srk",
               "model": "vortex (alignment + natural frequencies)",
-              "neighbour": "verlet rows, skin %g (r_max = rho + skin)" % w["skin"],
+              "neighbour": "autotuned per precision (cell list or Verlet rows; see autotune)",
               "dt": w["dt"], "sim_steps_per_bench_step": SIM_STEPS_PER_BENCH_STEP,
               "l2": "flushed between bench steps (512 MB write, outside the timed events)",
               "parallelism": f"replicas{world}"}
@@ -511,14 +533,14 @@ def main():
     import torch
     from spc2_langevin_integration_gb300 import abi
     torch.cuda.set_device(local)
+    best32, sb32, tune32 = tune_form(abi, w, abi.PRECISION_FP32C, rank)
+    best64, sb64, tune64 = tune_form(abi, w, abi.PRECISION_FP64, rank)
     with ClockSampler(local) as clk:
         ms32, e2e32, prof32, R32 = run_form(abi, torch, w, abi.PRECISION_FP32C, args.steps,
-                                            args.warmup, rank, dist)
+                                            args.warmup, rank, dist, best32, sb32)
         ms64, e2e64, prof64, R64 = run_form(abi, torch, w, abi.PRECISION_FP64,
-                                            max(2, args.steps // 2), args.warmup, rank, dist)
-        steps_c = max(2, args.steps // 2)
-        msc, _, profc, _ = run_form(abi, torch, w, abi.PRECISION_FP32C, steps_c, args.warmup, rank,
-                                    dist, neighbour=abi.NEIGHBOUR_CELL, e2e=False)
+                                            max(2, args.steps // 2), args.warmup, rank, dist,
+                                            best64, sb64)
     steps64 = max(2, args.steps // 2)
     psteps = n_total * SIM_STEPS_PER_BENCH_STEP
     value = psteps * args.steps / (ms32 / 1e3)
@@ -538,7 +560,7 @@ def main():
         "fp64": {"value": value64, "ms_per_step": ms64 / steps64, "profile_ms": prof64,
                  "order_params": R64},
         "fp32c_over_fp64": value / value64,
-        "fp32c_cell_list": {"value": psteps * steps_c / (msc / 1e3), "profile_ms": profc},
+        "autotune": {"fp32c": tune32, "fp64": tune64},
         "order_params_fp32c": R32,
         "gpu_launches": None,
         "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm,

@@ -189,6 +189,21 @@ enum { SPC_TUNE_SPARSE_BELOW = 1, SPC_TUNE_VERLET_ROW_LIMIT = 2 };
 int spc_set_tuning(spc_handle *h, int32_t key, double value);
 int spc_get_tuning(const spc_handle *h, int32_t key, double *value);
 
+/* Autotuner (no counterpart in the reference).  Times `trial_steps` steps
+ * (as captured graphs, after one warm-up call) of every candidate on the
+ * caller's state and keeps the fastest: the cell-list passes with the
+ * cell-tile or the warp-per-cell kernels, and, where the stencil allows
+ * Verlet rows, rows with skins of 0.1, 0.2 and 0.4 rho.  Every candidate
+ * computes the same neighbour sets; FP64 results differ between them only by
+ * summation order.  omega is required for the vortex model.  On return *best
+ * holds p with the winning neighbour method and skin, *sparse_below the
+ * SPC_TUNE_SPARSE_BELOW value to set on the handle, and (when not NULL)
+ * ms_out[k] the milliseconds per step of candidate k for k < min(cap, count),
+ * *count the number of candidates.  The caller's state is not touched. */
+int spc_autotune(const spc_params *p, int32_t n, const double *aos3n, const double *omega, double dt,
+                 int32_t trial_steps, spc_params *best, double *sparse_below, double *ms_out,
+                 int32_t cap, int32_t *count);
+
 /* Synchronise the handle's stream; the stream itself (a cudaStream_t) for
  * callers that time or order work around the library. */
 int spc_synchronize(spc_handle *h);

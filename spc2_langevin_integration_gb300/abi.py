@@ -128,6 +128,9 @@ def lib() -> C.CDLL:
     L.spc_get_tuning.argtypes = [H, C.c_int32, dp]
     L.spc_batch_set_tuning.argtypes = [H, C.c_int32, C.c_double]
     L.spc_batch_get_tuning.argtypes = [H, C.c_int32, dp]
+    L.spc_autotune.argtypes = [C.POINTER(Params), C.c_int32, C.c_void_p, C.c_void_p, C.c_double,
+                               C.c_int32, C.POINTER(Params), dp, dp, C.c_int32,
+                               C.POINTER(C.c_int32)]
     L.spc_alloc_pinned.argtypes = [C.c_size_t, C.POINTER(C.c_void_p)]
     L.spc_free_pinned.argtypes = [C.c_void_p]
     _lib = L
@@ -433,3 +436,20 @@ class Batch:
     @property
     def stream(self) -> int:
         return self._L.spc_batch_stream(self.h)
+
+
+def autotune(n: int, params: Params, state, omega=None, dt: float = 0.01, trial_steps: int = 20):
+    """Time the neighbour-method candidates on this state (spc_autotune) and
+    return (best params, sparse_below tuning, per-candidate ms per step)."""
+    L = lib()
+    st = _f64(state, 3 * n)
+    om = None if omega is None else _f64(omega, n)
+    best = Params()
+    sb = C.c_double()
+    ms = (C.c_double * 16)()
+    cnt = C.c_int32()
+    rc = L.spc_autotune(C.byref(params), int(n), _ptr(st), None if om is None else _ptr(om), dt,
+                        int(trial_steps), C.byref(best), C.byref(sb), ms, 16, C.byref(cnt))
+    if rc != SPC_OK:
+        raise SpcError(rc, (L.spc_last_error(None) or b"").decode())
+    return best, sb.value, [ms[k] for k in range(min(cnt.value, 16))]

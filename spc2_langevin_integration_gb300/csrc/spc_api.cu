@@ -426,6 +426,74 @@ int spc_get_tuning(const spc_handle *h, int32_t key, double *value) {
   return engine_get_tuning(&h->e, key, value);
 }
 
+int spc_autotune(const spc_params *p, int32_t n, const double *aos3n, const double *omega, double dt,
+                 int32_t trial_steps, spc_params *best, double *sparse_below, double *ms_out,
+                 int32_t cap, int32_t *count) {
+  if (!p || !aos3n || !best || !sparse_below || trial_steps <= 0)
+    return fail(nullptr, SPC_ERR_INVALID, "bad argument");
+  if (p->model == SPC_MODEL_VORTEX && !omega) return fail(nullptr, SPC_ERR_INVALID, "vortex model needs omega");
+  std::string why;
+  int rc = validate_params(p, n, why);
+  if (rc) return fail(nullptr, rc, "%s", why.c_str());
+  struct Cand {
+    int neighbour;
+    double skin, sparse;
+  };
+  std::vector<Cand> cands = {{SPC_NEIGHBOUR_CELL, p->skin, kSparseBelowDefault},
+                             {SPC_NEIGHBOUR_CELL, p->skin, 0.0},
+                             {SPC_NEIGHBOUR_CELL, p->skin, 1e9}};
+  for (double f : {0.1, 0.2, 0.4}) {
+    spc_params q = *p;
+    q.neighbour = SPC_NEIGHBOUR_VERLET;
+    q.skin = f * p->rho;
+    if (make_sysconst(q, n).vR > 0) cands.push_back({SPC_NEIGHBOUR_VERLET, q.skin, kSparseBelowDefault});
+  }
+  double best_ms = 1e300;
+  int best_k = -1;
+  for (size_t k = 0; k < cands.size(); ++k) {
+    spc_params q = *p;
+    q.neighbour = cands[k].neighbour;
+    q.skin = cands[k].skin;
+    spc_handle *h = nullptr;
+    rc = spc_create(&q, n, &h);
+    if (rc == SPC_OK) rc = spc_upload_state(h, aos3n);
+    if (rc == SPC_OK && omega) rc = spc_upload_omega(h, omega);
+    if (rc == SPC_OK && cands[k].neighbour == SPC_NEIGHBOUR_CELL)
+      rc = spc_set_tuning(h, SPC_TUNE_SPARSE_BELOW, cands[k].sparse);
+    double t = 0.0, ms = 1e300;
+    if (rc == SPC_OK) rc = spc_step_graph(h, &t, dt, trial_steps);  // capture + warm-up
+    if (rc == SPC_OK) {
+      cudaEvent_t e0 = nullptr, e1 = nullptr;
+      cudaError_t ce = cudaEventCreate(&e0);
+      if (ce == cudaSuccess) ce = cudaEventCreate(&e1);
+      if (ce == cudaSuccess) ce = cudaEventRecord(e0, h->e.stream);
+      if (ce == cudaSuccess) rc = spc_step_graph(h, &t, dt, trial_steps);
+      if (ce == cudaSuccess && rc == SPC_OK) ce = cudaEventRecord(e1, h->e.stream);
+      if (ce == cudaSuccess && rc == SPC_OK) ce = cudaEventSynchronize(e1);
+      float f = 0.0f;
+      if (ce == cudaSuccess && rc == SPC_OK) ce = cudaEventElapsedTime(&f, e0, e1);
+      if (e0) cudaEventDestroy(e0);
+      if (e1) cudaEventDestroy(e1);
+      if (ce != cudaSuccess && rc == SPC_OK) rc = fail(nullptr, SPC_ERR_CUDA, "autotune timing: %s", cudaGetErrorString(ce));
+      ms = (double)f / trial_steps;
+    }
+    std::string msg = h ? h->e.err : std::string();
+    spc_destroy(h);
+    if (rc != SPC_OK) return fail(nullptr, rc, "autotune candidate %d: %s", (int)k, msg.c_str());
+    if (ms_out && (int)k < cap) ms_out[k] = ms;
+    if (ms < best_ms) {
+      best_ms = ms;
+      best_k = (int)k;
+    }
+  }
+  *best = *p;
+  best->neighbour = cands[best_k].neighbour;
+  best->skin = cands[best_k].skin;
+  *sparse_below = cands[best_k].sparse;
+  if (count) *count = (int32_t)cands.size();
+  return SPC_OK;
+}
+
 int spc_philox4x32_10(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]) {
   if (!ctr || !key || !out) return fail(nullptr, SPC_ERR_INVALID, "NULL argument");
   uint32_t *d = nullptr;

@@ -80,10 +80,18 @@ __device__ __forceinline__ float shift_y(int q, float cell_f) { return (float)(q
 // candidate.  Cells with more candidates run the filter in pass 2 as well.
 constexpr int kMaskWords = kTileCap / 32;
 
+// Per-part results of one 128-particle group: each part's compensated sums
+// (sum minus compensation) and counts; pass 1 has one sum, pass 2 two.
+template <int KIND>
 struct TileRed {
-  float s[4][kTileThreads32], c[4][kTileThreads32], s1[4][kTileThreads32], c1[4][kTileThreads32];
+  float s0[4][kTileThreads32];
+  float s1[KIND == kKindCos2 ? 4 : 1][kTileThreads32];
   int n[4][kTileThreads32];
 };
+
+// Shared memory of k_tile_fp32c is kept under ~31 KB (and registers at 72)
+// so that 7 CTAs fit an SM: a 1024-cell system then runs in a single wave.
+constexpr int kTileMinBlocks32 = 7;
 
 __device__ __forceinline__ int split_point(int rcnt, int part, int S) {
   // part boundaries on multiples of 32 so that mask words are not shared
@@ -130,13 +138,12 @@ __device__ __forceinline__ void block32(const float4 *__restrict__ s_c4, const f
 }
 
 template <int KIND>
-__global__ void __launch_bounds__(kTileThreads32) k_tile_fp32c(KArgs a, int epi) {
+__global__ void __launch_bounds__(kTileThreads32, kTileMinBlocks32) k_tile_fp32c(KArgs a, int epi) {
   __shared__ float4 s_c4[kTileCap];   // x+shift, y+shift, cos phi, sin phi (padded to 32)
   __shared__ float s_d[KIND == kKindCos2 ? kTileCap : 1];  // pass 2: phase rate (float)
-  __shared__ int s_p[kTileCap];       // cell-order slot (exact fallback)
-  __shared__ TileRed red;
-  __shared__ float t_s[kTileThreads32], t_c[kTileThreads32], t_s1[kTileThreads32],
-      t_c1[kTileThreads32];
+  __shared__ TileRed<KIND> red;
+  constexpr int kT2 = KIND == kKindCos2 ? kTileThreads32 : 1;
+  __shared__ float t_s[kTileThreads32], t_c[kTileThreads32], t_s1[kT2], t_c1[kT2];
   __shared__ int t_n[kTileThreads32];
   const int n_all = a.n_active;
   const int tid = threadIdx.x, w = tid / kWarp, lane = tid % kWarp;
@@ -157,7 +164,8 @@ __global__ void __launch_bounds__(kTileThreads32) k_tile_fp32c(KArgs a, int epi)
     for (int ig = cb; ig < ce; ig += kTileThreads32) {
       const int gi = min(kTileThreads32, ce - ig);
       if (tid < gi) {
-        t_s[tid] = t_c[tid] = t_s1[tid] = t_c1[tid] = 0.0f;
+        t_s[tid] = t_c[tid] = 0.0f;
+        if constexpr (KIND == kKindCos2) t_s1[tid] = t_c1[tid] = 0.0f;
         t_n[tid] = 0;
       }
       for (int r = 0; r < rounds; ++r) {
@@ -172,11 +180,9 @@ __global__ void __launch_bounds__(kTileThreads32) k_tile_fp32c(KArgs a, int epi)
               const float2 f = a.fxy[pj];
               const float2 cs = a.cs[pj];
               s_c4[k] = make_float4(f.x + shift_x(q, sc.cell_f), f.y + shift_y(q, sc.cell_f), cs.x, cs.y);
-              s_p[k] = pj;
               if constexpr (KIND == kKindCos2) s_d[k] = a.dphi_f[pj];
             } else {  // padding: far away, never a neighbour, never near the cutoff
               s_c4[k] = make_float4(3.0e18f, 3.0e18f, 0.0f, 0.0f);
-              s_p[k] = 0;
               if constexpr (KIND == kKindCos2) s_d[k] = 0.0f;
             }
           }
@@ -252,7 +258,9 @@ __global__ void __launch_bounds__(kTileThreads32) k_tile_fp32c(KArgs a, int epi)
                     const float dx = cj.x - fxi, dy = cj.y - fyi;
                     const float d2 = fmaf(dx, dx, dy * dy);
                     if (!(exact_all || fabsf(d2 - mid) <= band)) continue;
-                    if (!exact_within(sc, xi, yi, a.sx[s_p[j]], a.sy[s_p[j]])) continue;
+                    int q;
+                    const int pj = slot_of(st, rlo + j, q);
+                    if (!exact_within(sc, xi, yi, a.sx[pj], a.sy[pj])) continue;
                     if constexpr (KIND == kKindSin) {
                       b0 += fmaf(cj.w, ca, -cj.z * sa);
                     } else {
@@ -272,31 +280,28 @@ __global__ void __launch_bounds__(kTileThreads32) k_tile_fp32c(KArgs a, int epi)
             }
           }
           if (valid) {
-            red.s[part][li] = S0;
-            red.c[part][li] = C0;
-            red.s1[part][li] = S1;
-            red.c1[part][li] = C1;
+            red.s0[part][li] = S0 - C0;
+            if constexpr (KIND == kKindCos2) red.s1[part][li] = S1 - C1;
             red.n[part][li] = n;
           }
         }
         __syncthreads();
         if (tid < gi) {
-          float ts = t_s[tid], tc = t_c[tid], ts1 = t_s1[tid], tc1 = t_c1[tid];
+          float ts = t_s[tid], tc = t_c[tid];
           int tn = t_n[tid];
           for (int part = 0; part < S; ++part) {
-            kahan_add(ts, tc, red.s[part][tid]);
-            kahan_add(ts, tc, -red.c[part][tid]);
-            if constexpr (KIND == kKindCos2) {
-              kahan_add(ts1, tc1, red.s1[part][tid]);
-              kahan_add(ts1, tc1, -red.c1[part][tid]);
-            }
+            kahan_add(ts, tc, red.s0[part][tid]);
             tn += red.n[part][tid];
           }
           t_s[tid] = ts;
           t_c[tid] = tc;
-          t_s1[tid] = ts1;
-          t_c1[tid] = tc1;
           t_n[tid] = tn;
+          if constexpr (KIND == kKindCos2) {
+            float ts1 = t_s1[tid], tc1 = t_c1[tid];
+            for (int part = 0; part < S; ++part) kahan_add(ts1, tc1, red.s1[part][tid]);
+            t_s1[tid] = ts1;
+            t_c1[tid] = tc1;
+          }
         }
       }
       if (tid < gi) {
@@ -306,7 +311,7 @@ __global__ void __launch_bounds__(kTileThreads32) k_tile_fp32c(KArgs a, int epi)
         Acc<kPrecFP32C> acc;
         acc.init();
         acc.s0 = t_s[tid] - t_c[tid];
-        acc.s1 = t_s1[tid] - t_c1[tid];
+        if constexpr (KIND == kKindCos2) acc.s1 = t_s1[tid] - t_c1[tid];
         acc.n = t_n[tid];
         epilogue<kPrecFP32C, KIND>(a, epi, sd, il, acc, a.pidx[p]);
       }

@@ -35,7 +35,7 @@ namespace spc {
 constexpr int kVThreads = 128;
 constexpr int kVMaxR = 3;                 // stencil radius limit (7 x 7 cells)
 constexpr int kVMaxCells = (2 * kVMaxR + 1) * (2 * kVMaxR + 1);
-constexpr int kVStage32 = 2048;           // FP32C / build: candidates staged per round
+constexpr int kVStage32 = 1664;           // FP32C / build: candidates staged per round
 constexpr int kVStage64 = 1536;           // FP64: candidates staged per round
 
 // The (2R+1)^2 stencil of cell c: start of each stencil cell in cell order and
@@ -362,7 +362,78 @@ __global__ void __launch_bounds__(kVThreads) k_vtile(KArgs a, int epi) {
                                           sm.phi, sm.dd);
         __syncthreads();
         if (!valid) continue;
-        if (rows) {
+        if (rows && rounds == 1 && !exact_all) {
+          // the common case: every row entry is in the one staged round.
+          // Chunks of 8 entries, unrolled, the next chunk loaded ahead.
+          for (int c8 = 0; c8 * 8 < len; ++c8) {
+            const uint4 ch = cur;
+            if ((c8 + 1) * 8 < len) cur = chunks[(size_t)(c8 + 1) * n_all + v];
+            if (KIND == kKindCos2 && masked && (c8 & 3) == 0)
+              word = a.nbmask[(size_t)(c8 >> 2) * n_all + v];
+#pragma unroll
+            for (int t = 0; t < 8; ++t) {
+              const int kk = c8 * 8 + t;
+              if (kk < len) {
+                const int j = chunk_entry(ch, t);
+                bool in;
+                if (KIND == kKindCos2 && masked) {
+                  in = (word >> (kk & (kWarp - 1))) & 1u;
+                } else {
+                  float cx, cy;
+                  if constexpr (PREC == kPrecFP32C) {
+                    const float4 cj = sm.c4[j];
+                    cx = cj.x;
+                    cy = cj.y;
+                  } else {
+                    const float2 cj = sm.xy[j];
+                    cx = cj.x;
+                    cy = cj.y;
+                  }
+                  const float dx = cx - il.fx, dy = cy - il.fy;
+                  const float d2 = fmaf(dx, dx, dy * dy);
+                  in = d2 < lo2;
+                  if (fabsf(d2 - mid) <= band) {  // rare: the reference's FP64 test
+                    const int pj = vslot_of(sc, s_start, s_prefix, j);
+                    in = exact_within(sc, il.x, il.y, a.sx[pj], a.sy[pj]);
+                  }
+                }
+                if (in) {
+                  if constexpr (PREC == kPrecFP32C) {
+                    const float4 cj = sm.c4[j];
+                    if constexpr (KIND == kKindSin) {
+                      b0 += fmaf(cj.w, il.ca, -cj.z * il.sa);  // sin(phi_j - phi_i - alpha)
+                    } else {
+                      const float tv = fmaf(cj.z, il.ca, cj.w * il.sa);  // cos(phi_j - phi_i - alpha)
+                      b0 += tv;
+                      b1 = fmaf(sm.df[j] - il.dphif, tv, b1);
+                    }
+                  } else {
+                    const double dp = dsub(dsub(sm.phi[j], il.phi), sc.alpha);
+                    if constexpr (KIND == kKindSin) {
+                      acc.s0 = dadd(acc.s0, sin(dp));  // ChimeraSystem.cpp:412
+                    } else {
+                      const double cc = cos(dp);  // ChimeraSystem.cpp:634-637
+                      acc.s0 = dadd(acc.s0, ddiv(cc, il.card));
+                      acc.s1 = dadd(acc.s1, ddiv(dmul(dsub(sm.dd[j], il.dphi), cc), il.card));
+                    }
+                  }
+                  bits |= 1u << (kk & (kWarp - 1));
+                }
+              }
+            }
+            if ((c8 & 3) == 3 && (c8 + 1) * 8 <= len) {  // a complete block of 32 entries
+              acc.n += __popc(bits);
+              if constexpr (PREC == kPrecFP32C) {
+                kahan_add(acc.s0, acc.c0, b0);
+                if constexpr (KIND == kKindCos2) kahan_add(acc.s1, acc.c1, b1);
+                b0 = b1 = 0.0f;
+                if (KIND == kKindSin && masked) a.nbmask[(size_t)(c8 >> 2) * n_all + v] = bits;
+              }
+              bits = 0u;
+            }
+          }
+          k = len;
+        } else if (rows) {
           // row entries are ascending staged indices: take those of this round
           while (k < len) {
             if ((k >> 3) != cur_chunk) {

@@ -187,3 +187,22 @@ def test_verlet_falls_back_to_cells_when_the_stencil_wraps():
             out.append(s.download_state())
             assert s.diagnostics()["verlet_rebuilds"] == 0
     assert np.array_equal(out[0], out[1])
+
+
+def test_autotune_picks_an_exact_candidate():
+    n, L, dt = 4096, 2.0, 0.005
+    prm = dict(v0=0.02, sigma=2.0, rho=0.2, alpha=1.2, D_phi=0.01)
+    st0 = init_state(n, L, 67)
+    p = abi.make_params(L=L, stepper=abi.STEPPER_SRK, seed=12, skin=0.05, **prm)
+    best, sparse_below, ms = abi.autotune(n, p, st0, dt=dt, trial_steps=5)
+    assert len(ms) == 6 and all(m > 0 for m in ms)
+    assert best.neighbour in (abi.NEIGHBOUR_CELL, abi.NEIGHBOUR_VERLET)
+    with abi.System(n, best) as s:
+        if best.neighbour == abi.NEIGHBOUR_CELL:
+            s.set_tuning(abi.TUNE_SPARSE_BELOW, sparse_below)
+        s.upload_state(st0)
+        s.step(dt, 50)
+        got = s.download_state()
+        noise = s.export_noise(0, 50)
+    ref = oracle_run(n, L, prm, abi.STEPPER_SRK, st0, dt, 50, noise)
+    assert np.abs(periodic_diff(got, ref, L)).max() <= TRAJ_TOL
