@@ -37,12 +37,16 @@ SIM_STEPS_PER_BENCH_STEP = 100
 # and n_i (4 B).
 ALG_BYTES = {
     "stage": 24 + 8,          # read x, y, phi; write key, index
-    "sort": 2 * 2 * 8,        # two 8-bit passes: read + write (key, index)
+    "sort": 2 * 8,            # one digit pass (<= 2048 cells): read + write (key, index)
     "gather": 8 + 40,         # read (key, index); write cell-order x, y, phi, float x/y offsets
     "pass1": 32 + 12,         # read cell-order x, y, phi, offsets; write phase rate, n_i
     "pass2": 32 + 12 + 8 + 24 + 24,  # + own rate/n_i, omega, state in, state out
 }
 ALG_BYTES_STEP = 168 + 8      # survey accounting for the whole SRK step (+ omega)
+# DRAM bytes (read + write) per launch of the dominant kernel (k_tile_fp32c,
+# SRK pass 1) at this workload, from one ncu capture; the command and the raw
+# figures are in profiles/k_tile_fp32c_vortex_srk_n65536.md.
+NCU_TRAFFIC_PASS1 = 2.41e6
 
 
 def init_inputs(w, seed_offset=0):
@@ -149,13 +153,53 @@ def ensemble_systems(count=512, seed=2, n_range=(256, 32768), density=1000.0):
     return out
 
 
-def run_ensemble(precision, graphs, rank=0, sparse_below=None):
-    """One batch of all ensemble systems, `graphs` replays of a 100-step graph;
-    then a per-phase profile of 5 plain steps.  sparse_below: the tuning that
-    picks the neighbour kernel per system (None: the library's default)."""
+_ENSEMBLE = None
+
+
+def _cpu_system_worker(job):
+    """One ensemble system on one host core: `steps` Euler steps of the oracle
+    port with seeded normals.  Returns particle-steps done and seconds."""
+    k, steps = job
+    from oracle import pyoracle as po
+    global _ENSEMBLE
+    if _ENSEMBLE is None:  # once per worker process
+        _ENSEMBLE = ensemble_systems()
+    _, n, L, prm, st = _ENSEMBLE[k]
+    o = po.OracleSystem(n, L, **prm)
+    noise = np.random.default_rng(1000 + k).standard_normal(n * steps)
+    t0 = time.perf_counter()
+    o.run(po.EULER, st, 0.0, 0.01, steps, noise)
+    return n * steps, time.perf_counter() - t0
+
+
+def cpu_ensemble_baseline(count=64, steps=100):
+    """The reference's parameter-scan form on the host: one process per system
+    over every host core (a spawn pool, started before any GPU work), on a
+    seeded sample of `count` of the 512 systems for `steps` Euler steps."""
+    import multiprocessing as mpc
+    cores = os.cpu_count() or 1
+    pick = sorted(np.random.default_rng(5).choice(512, size=count, replace=False).tolist())
+    ctx = mpc.get_context("spawn")
+    t0 = time.perf_counter()
+    with ctx.Pool(cores) as pool:
+        out = pool.map(_cpu_system_worker, [(k, steps) for k in pick])
+    wall = time.perf_counter() - t0
+    work = sum(w for w, _ in out)
+    return {"value": work / wall, "unit": "particle-steps/s", "cores": cores, "kind": "port",
+            "sample": f"{count} of the 512 systems (seeded), {steps} Euler steps each, one "
+                      f"process per system over {cores} host cores (wall time incl. pool start)"}
+
+
+def run_ensemble(precision, graphs, rank=0, sparse_below=None, subset=None):
+    """One batch of the ensemble's systems (all, or the indices in `subset`),
+    `graphs` replays of a 100-step graph; then a per-phase profile of 5 plain
+    steps.  sparse_below: the tuning that picks the neighbour kernel per system
+    (None: the library's default)."""
     import torch
     from spc2_langevin_integration_gb300 import abi
     systems = ensemble_systems()
+    if subset is not None:
+        systems = [systems[i] for i in subset]
     ntot = sum(n for _, n, _, _, _ in systems)
     ctot = sum(abi.cells_of(L, prm["rho"]) for _, _, L, prm, _ in systems)
     b = abi.Batch(abi.STEPPER_EULER, precision, len(systems), ntot, ctot)
@@ -296,6 +340,55 @@ def run_drift(steps=10000, every=100, out_path=None):
     return res
 
 
+LARGE = dict(name="chimera_rk4_n4194304_L64", n=1 << 22, L=64.0, v0=0.01, sigma=1.0, rho=0.25,
+             alpha=1.45, D_phi=0.0, dt=0.01, seed=0, skin=0.05)
+
+
+def run_large(precision, steps):
+    """The large single system: Chimera, N = 2^22 in L = 64, RK4, dt = 0.01,
+    positions and phases uniform from seed 0.  The autotuner picks the
+    neighbour method on the initial state (2 trial steps per candidate); then
+    `steps` steps run as one graph replay, timed with CUDA events."""
+    import torch
+    from spc2_langevin_integration_gb300 import abi
+    w = LARGE
+    n, L = w["n"], w["L"]
+    rng = np.random.default_rng(w["seed"])
+    st = np.empty(3 * n)
+    st[0::3] = rng.uniform(0.0, L, n)
+    st[1::3] = rng.uniform(0.0, L, n)
+    st[2::3] = rng.uniform(-np.pi, np.pi, n)
+    p = abi.make_params(L=L, v0=w["v0"], sigma=w["sigma"], rho=w["rho"], alpha=w["alpha"],
+                        D_phi=w["D_phi"], stepper=abi.STEPPER_RK4, precision=precision,
+                        seed=w["seed"], neighbour=abi.NEIGHBOUR_VERLET, skin=w["skin"])
+    t0 = time.perf_counter()
+    best, sb, ms = abi.autotune(n, p, st, dt=w["dt"], trial_steps=2)
+    tune_s = time.perf_counter() - t0
+    names = ["cell (default kernels)", "cell (cell-tile)", "cell (warp-per-cell)"]
+    names += ["verlet skin %.3g" % (f * w["rho"]) for f in (0.1, 0.2, 0.4)][: len(ms) - 3]
+    with abi.System(n, best) as s:
+        if best.neighbour == abi.NEIGHBOUR_CELL:
+            s.set_tuning(abi.TUNE_SPARSE_BELOW, sb)
+        s.upload_state(st)
+        stream = torch.cuda.ExternalStream(s.stream)
+        s.step(w["dt"], steps, graph=True)  # capture + warm
+        s.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        s.step(w["dt"], steps, graph=True)
+        e1.record(stream)
+        s.synchronize()
+        t_ms = e0.elapsed_time(e1)
+        prof = s.profile_steps(w["dt"], 1)
+        launches = s.graph_nodes()
+    return {"value": n * steps / (t_ms / 1e3), "unit": "particle-steps/s", "steps": steps,
+            "ms_per_step": t_ms / steps, "profile_ms_one_step": prof,
+            "gpu_launches_per_replay": launches,
+            "autotune": {"choice": {"neighbour": "verlet" if best.neighbour == abi.NEIGHBOUR_VERLET
+                                    else "cell", "skin": best.skin, "sparse_below": sb},
+                         "candidates_ms_per_step": dict(zip(names, ms)), "tuning_s": tune_s}}
+
+
 def dist_setup(args):
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -375,10 +468,11 @@ def run_form(abi, torch, w, precision, steps, warmup, rank, dist, params=None, s
         dist.barrier()
     ms = sum(a.elapsed_time(b) for a, b in ev)
     ms = reduce_max(dist, ms)
+    launches = s.graph_nodes() * steps  # one graph replay per bench step
     if not e2e:
         prof = s.profile_steps(dt, 20)
         s.close()
-        return ms, None, prof, None
+        return ms, None, prof, None, launches
     # e2e through the C-ABI with host buffers: pinned upload, 100 steps, download
     import ctypes as C
     L = abi.lib()
@@ -401,7 +495,7 @@ def run_form(abi, torch, w, precision, steps, warmup, rank, dist, params=None, s
     del host
     L.spc_free_pinned(ptr)
     s.close()
-    return ms, e2e_ms, prof, R
+    return ms, e2e_ms, prof, R, launches
 
 
 def main():
@@ -416,12 +510,21 @@ def main():
                     help="run a few plain (ungraphed) steps of the workload (or of an ensemble of "
                          "--ensemble-systems systems) for an ncu capture")
     ap.add_argument("--ensemble-systems", type=int, default=512)
+    ap.add_argument("--ensemble-shard", action="store_true",
+                    help="ensemble on N GPUs: partition the 512 systems over the ranks by "
+                         "footprint (strong scaling) instead of one full ensemble per rank")
+    ap.add_argument("--form", choices=["fp32c", "fp64"], default=None,
+                    help="time only this precision form of the workload with --neighbour / "
+                         "--skin (no autotune): the command for a launch list of the timed region")
+    ap.add_argument("--neighbour", choices=["cell", "verlet"], default="cell")
+    ap.add_argument("--skin", type=float, default=None)
     ap.add_argument("--cell-list", action="store_true",
                     help="--ncu-case fp32c/fp64: the cell-list passes instead of the Verlet rows")
-    ap.add_argument("--workload", choices=["vortex", "ensemble", "serve", "drift"], default="vortex",
+    ap.add_argument("--workload", choices=["vortex", "ensemble", "serve", "drift", "large"],
+                    default="vortex",
                     help="vortex: the headline single-system line; ensemble: 512 systems in one "
                          "batch; serve: the Poisson request stream; drift: FP32C vs FP64 order "
-                         "parameters over 10^4 steps")
+                         "parameters over 10^4 steps; large: Chimera RK4, N=2^22, L=64")
     ap.add_argument("--sparse-below", type=float, default=None,
                     help="ensemble: neighbour-kernel tuning (mean particles per cell below "
                          "which a system runs the warp-per-cell passes)")
@@ -433,23 +536,53 @@ def main():
     args = ap.parse_args()
     if args.workload == "ensemble":
         import torch
-        from spc2_langevin_integration_gb300 import abi
+        from spc2_langevin_integration_gb300 import abi, replicas
+        # the host baseline first: its process pool starts before any GPU call
+        cpu = None
+        if int(os.environ.get("RANK", "0")) == 0 and not args.no_cpu_baseline:
+            cpu = cpu_ensemble_baseline()
+        world, rank, local, dist = dist_setup(args)
+        subset = None
+        if world > 1 and args.ensemble_shard:
+            # strong scaling: the 512 systems partitioned by footprint
+            sizes = [n for _, n, _, _, _ in ensemble_systems()]
+            subset = replicas.shard(sizes, world, rank)
         res = {}
         runs = [("fp32c", abi.PRECISION_FP32C, 20, args.sparse_below),
                 ("fp64", abi.PRECISION_FP64, 3, args.sparse_below)]
         if args.compare_kernels:
             runs += [("fp32c_tile_only", abi.PRECISION_FP32C, 5, 0.0),
                      ("fp64_tile_only", abi.PRECISION_FP64, 1, 0.0)]
+        dev = "cuda" if world > 1 else None
         for name, prec, graphs, sb in runs:
-            ntot, ctot, ms, prof = run_ensemble(prec, graphs, sparse_below=sb)
-            res[name] = {"value": ntot * 100 * graphs / (ms / 1e3), "steps": 100 * graphs,
+            ntot, ctot, ms, prof = run_ensemble(prec, graphs, rank=rank, sparse_below=sb,
+                                                subset=subset)
+            ms = replicas.max_over_ranks(ms, dist, dev)
+            work = replicas.sum_over_ranks(ntot * 100 * graphs, dist, dev)
+            res[name] = {"value": work / (ms / 1e3), "steps": 100 * graphs,
                          "ms": ms, "profile_ms": prof, "sparse_below": sb}
-        print(json.dumps({"metric": "particle-steps/s", "workload": "ensemble_512_euler",
-                          "value": res["fp32c"]["value"], "unit": "particle-steps/s",
-                          "systems": 512, "particles": ntot, "cells": ctot,
-                          **res,
-                          "fp32c_over_fp64": res["fp32c"]["value"] / res["fp64"]["value"],
-                          "graph_steps": 100, "l2": "working set > L2 (about 1 GB)"}))
+        ntot = int(replicas.sum_over_ranks(ntot, dist, dev))
+        if rank == 0:
+            print(json.dumps({"metric": "particle-steps/s", "workload": "ensemble_512_euler",
+                              "value": res["fp32c"]["value"], "unit": "particle-steps/s",
+                              "n_gpus": world, "scaling": "strong" if subset is not None else "weak",
+                              "systems": 512, "particles": ntot, "cells": ctot,
+                              **res,
+                              "fp32c_over_fp64": res["fp32c"]["value"] / res["fp64"]["value"],
+                              "graph_steps": 100, "l2": "working set > L2 (about 1 GB)",
+                              "cpu_baseline": cpu}))
+        if dist is not None:
+            dist.destroy_process_group()
+        return
+    if args.workload == "large":
+        from spc2_langevin_integration_gb300 import abi
+        out = {"metric": "particle-steps/s", "workload": LARGE["name"], "config": LARGE,
+               "fp32c": run_large(abi.PRECISION_FP32C, 20),
+               "fp64": run_large(abi.PRECISION_FP64, 4),
+               "note": "throughput over a timed prefix of the 2,000-step run (one graph replay "
+                       "per form after a warm replay); working set >> L2"}
+        out["fp32c_over_fp64"] = out["fp32c"]["value"] / out["fp64"]["value"]
+        print(json.dumps(out))
         return
     if args.workload == "drift":
         out = {"metric": "order-parameter drift, FP32C vs FP64", "workload": "drift"}
@@ -533,14 +666,29 @@ def main():
     import torch
     from spc2_langevin_integration_gb300 import abi
     torch.cuda.set_device(local)
+    if args.form:
+        prec = abi.PRECISION_FP32C if args.form == "fp32c" else abi.PRECISION_FP64
+        p = workload_params(abi, w, prec, rank)
+        p.neighbour = abi.NEIGHBOUR_VERLET if args.neighbour == "verlet" else abi.NEIGHBOUR_CELL
+        if args.skin is not None:
+            p.skin = args.skin
+        ms, e2e_ms, prof, _, launches = run_form(abi, torch, w, prec, args.steps, args.warmup,
+                                                 rank, dist, p)
+        if rank == 0:
+            print(json.dumps({"form": args.form, "neighbour": args.neighbour, "skin": p.skin,
+                              "value": n_total * SIM_STEPS_PER_BENCH_STEP * args.steps / (ms / 1e3),
+                              "ms_per_bench_step": ms / args.steps, "profile_ms": prof,
+                              "gpu_launches": launches}))
+        return
     best32, sb32, tune32 = tune_form(abi, w, abi.PRECISION_FP32C, rank)
     best64, sb64, tune64 = tune_form(abi, w, abi.PRECISION_FP64, rank)
     with ClockSampler(local) as clk:
-        ms32, e2e32, prof32, R32 = run_form(abi, torch, w, abi.PRECISION_FP32C, args.steps,
-                                            args.warmup, rank, dist, best32, sb32)
-        ms64, e2e64, prof64, R64 = run_form(abi, torch, w, abi.PRECISION_FP64,
-                                            max(2, args.steps // 2), args.warmup, rank, dist,
-                                            best64, sb64)
+        ms32, e2e32, prof32, R32, launches32 = run_form(abi, torch, w, abi.PRECISION_FP32C,
+                                                        args.steps, args.warmup, rank, dist,
+                                                        best32, sb32)
+        ms64, e2e64, prof64, R64, _ = run_form(abi, torch, w, abi.PRECISION_FP64,
+                                               max(2, args.steps // 2), args.warmup, rank, dist,
+                                               best64, sb64)
     steps64 = max(2, args.steps // 2)
     psteps = n_total * SIM_STEPS_PER_BENCH_STEP
     value = psteps * args.steps / (ms32 / 1e3)
@@ -550,6 +698,12 @@ def main():
     phases = {k: prof32[k] for k in ("stage", "sort", "gather", "pass1", "pass2")}
     dom = max(phases, key=phases.get)
     achieved = ALG_BYTES[dom] * w["n"] / (phases[dom] * 1e-3) / 1e9
+    # compute-side work of one neighbour pass: candidate tests (3x3 cells of
+    # side L / int(L / rho)) and pair terms (neighbours within rho) per second
+    dens = w["n"] / w["L"] ** 2
+    cell = w["L"] / int(w["L"] / w["rho"])
+    cand, pairs = 9 * dens * cell ** 2, np.pi * w["rho"] ** 2 * dens
+    t_pass = phases["pass1"] * 1e-3
     out = {
         "metric": "particle-steps/s", "value": value, "unit": "particle-steps/s",
         "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
@@ -565,17 +719,23 @@ def main():
         "gpu_launches": None,
         "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm,
                      "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / hbm,
-                     "traffic": None, "alg_bytes_per_particle": ALG_BYTES[dom],
-                     "note": "compute-bound path (float prefilter + per-pair trig); HBM fraction "
-                             "is low by construction"},
+                     "traffic": NCU_TRAFFIC_PASS1 if dom == "pass1" else None,
+                     "alg_bytes_per_particle": ALG_BYTES[dom],
+                     "alg_bytes_per_launch": ALG_BYTES[dom] * w["n"],
+                     "compute": {"candidate_tests_per_s": w["n"] * cand / t_pass,
+                                 "pair_terms_per_s": w["n"] * pairs / t_pass,
+                                 "candidates_per_particle": cand, "pairs_per_particle": pairs},
+                     "note": "the passes are bound by issue / latency (float prefilter and "
+                             "per-pair trig on an L2-resident working set), not by HBM: the "
+                             "HBM fraction is low by construction"},
         "profile_ms_fp32c": prof32,
         "e2e": {"value": e2e_value, "unit": "particle-steps/s",
                 "h2d_bytes_per_step": 3 * w["n"] * 8, "d2h_bytes_per_step": 3 * w["n"] * 8},
         "clocks": clk.summary(),
     }
-    # launches inside the timed region per bench step (graph of 100 steps)
-    per_step = 1 + 3 * 2 + 1 + 1 + 2  # stage, 2 radix passes x 3, bounds, gather, 2 passes
-    out["gpu_launches"] = per_step * SIM_STEPS_PER_BENCH_STEP * args.steps
+    # kernels launched inside the timed region: the captured graph's node count
+    # (spc_graph_nodes) times the replays
+    out["gpu_launches"] = launches32
     if rank == 0 and not args.no_cpu_baseline:
         out["cpu_baseline"] = cpu_baseline(w)
     if rank == 0:

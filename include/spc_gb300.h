@@ -204,6 +204,10 @@ int spc_autotune(const spc_params *p, int32_t n, const double *aos3n, const doub
                  int32_t trial_steps, spc_params *best, double *sparse_below, double *ms_out,
                  int32_t cap, int32_t *count);
 
+/* Nodes (kernel launches) of the CUDA graph the last spc_step_graph call
+ * captured or replayed: every replay launches exactly this many kernels. */
+int spc_graph_nodes(const spc_handle *h, int64_t *nodes);
+
 /* Synchronise the handle's stream; the stream itself (a cudaStream_t) for
  * callers that time or order work around the library. */
 int spc_synchronize(spc_handle *h);

@@ -27,9 +27,11 @@ def available() -> bool:
 def run_reference(n, L, *, mode, family=FAMILY_VECTOR, stepper=STEP_EULER, nsteps=0,
                   record_every=0, v0=0.01, sigma=1.0, rho=0.1, alpha=1.45, D_phi=0.005,
                   rho_0=1.0, t0=0.0, dt=0.01, k_coef=0.0, state=None, k_prev=None,
-                  k_next_init=None, noise=None):
-    """Returns the raw float64 output of the reference driver."""
-    binary = build_oracle.build_reference()
+                  k_next_init=None, noise=None, binary=None, extra_env=None):
+    """Returns the raw float64 output of the reference driver (or of another
+    program reading the same input format, e.g. the drop-in driver)."""
+    if binary is None:
+        binary = build_oracle.build_reference()
     if binary is None:
         binary = build_oracle.REF_BIN
     n3 = 3 * n
@@ -50,7 +52,7 @@ def run_reference(n, L, *, mode, family=FAMILY_VECTOR, stepper=STEP_EULER, nstep
             f.write(k_next_init.tobytes())
             f.write(struct.pack("<q", noise.size))
             f.write(noise.tobytes())
-        env = dict(os.environ, SPC_REF_N=str(n), SPC_REF_L=repr(float(L)))
+        env = dict(os.environ, SPC_REF_N=str(n), SPC_REF_L=repr(float(L)), **(extra_env or {}))
         subprocess.run([binary, fin, fout], check=True, env=env,
                        stdout=subprocess.DEVNULL)
         return np.fromfile(fout, dtype=np.float64)

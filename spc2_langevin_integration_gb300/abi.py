@@ -131,6 +131,7 @@ def lib() -> C.CDLL:
     L.spc_autotune.argtypes = [C.POINTER(Params), C.c_int32, C.c_void_p, C.c_void_p, C.c_double,
                                C.c_int32, C.POINTER(Params), dp, dp, C.c_int32,
                                C.POINTER(C.c_int32)]
+    L.spc_graph_nodes.argtypes = [H, C.POINTER(C.c_int64)]
     L.spc_alloc_pinned.argtypes = [C.c_size_t, C.POINTER(C.c_void_p)]
     L.spc_free_pinned.argtypes = [C.c_void_p]
     _lib = L
@@ -282,6 +283,11 @@ class System:
         c, v, e = C.c_int64(), C.c_int64(), C.c_int64()
         self._check(self._L.spc_diagnostics(self.h, C.byref(c), C.byref(v), C.byref(e)), self.h)
         return {"clamped_cells": c.value, "verlet_rebuilds": v.value, "error_word": e.value}
+
+    def graph_nodes(self) -> int:
+        v = C.c_int64()
+        self._check(self._L.spc_graph_nodes(self.h, C.byref(v)), self.h)
+        return v.value
 
     def set_tuning(self, key: int, value: float):
         self._check(self._L.spc_set_tuning(self.h, int(key), float(value)), self.h)

@@ -410,6 +410,12 @@ int spc_synchronize(spc_handle *h) {
 
 void *spc_stream(spc_handle *h) { return h ? (void *)h->e.stream : nullptr; }
 
+int spc_graph_nodes(const spc_handle *h, int64_t *nodes) {
+  if (!h || !nodes) return fail(nullptr, SPC_ERR_INVALID, "NULL argument");
+  *nodes = h->e.graph ? (int64_t)h->e.graph_nodes : 0;
+  return SPC_OK;
+}
+
 int spc_profile_steps(spc_handle *h, double dt, int32_t nsteps, double *out_ms, int32_t cap) {
   if (!h || !out_ms || cap < 6 || nsteps <= 0) return hfail(h, SPC_ERR_INVALID, "bad argument");
   SPC_TRY(check_ready(h));

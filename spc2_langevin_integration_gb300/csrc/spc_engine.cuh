@@ -173,6 +173,7 @@ struct Engine {
   // graph cache
   cudaGraphExec_t graph = nullptr;
   int graph_steps = 0;
+  size_t graph_nodes = 0;  // kernel and memset nodes of the cached graph
   double graph_dt = 0.0;
   // profiling marks
   cudaEvent_t prof_ev[8] = {};
@@ -776,6 +777,8 @@ inline int engine_steps(Engine *e, double dt, int nsteps, bool use_graph, const 
         return rc;
       }
       if (ce != cudaSuccess) return fail(e, SPC_ERR_CUDA, "graph capture: %s", cudaGetErrorString(ce));
+      e->graph_nodes = 0;
+      cudaGraphGetNodes(g, nullptr, &e->graph_nodes);
       ce = cudaGraphInstantiate(&e->graph, g, 0);
       cudaGraphDestroy(g);
       if (ce != cudaSuccess) {

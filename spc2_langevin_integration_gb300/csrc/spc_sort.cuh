@@ -64,8 +64,18 @@ __global__ void __launch_bounds__(kScanThreads)
   for (int k = 0; k < kPer; ++k) {
     const int d = t * kPer + k;
     uint32_t s = 0;
-    if (d < R)
-      for (int tile = 0; tile < ntiles; ++tile) s += hist[(size_t)tile * R + d];
+    if (d < R) {
+      // eight independent loads in flight per iteration (tiles are <= 32 here)
+      int tile = 0;
+      for (; tile + 8 <= ntiles; tile += 8) {
+        uint32_t v[8];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) v[u] = hist[(size_t)(tile + u) * R + d];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) s += v[u];
+      }
+      for (; tile < ntiles; ++tile) s += hist[(size_t)tile * R + d];
+    }
     tot[k] = s;
   }
   const uint32_t mine = tot[0] + tot[1];
@@ -92,13 +102,25 @@ __global__ void __launch_bounds__(kScanThreads)
 #pragma unroll
   for (int k = 0; k < kPer; ++k) {
     const int d = t * kPer + k;
-    if (d < R)
-      for (int tile = 0; tile < ntiles; ++tile) {
+    if (d < R) {
+      int tile = 0;
+      for (; tile + 8 <= ntiles; tile += 8) {
+        uint32_t v[8];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) v[u] = hist[(size_t)(tile + u) * R + d];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+          hist[(size_t)(tile + u) * R + d] = run;
+          run += v[u];
+        }
+      }
+      for (; tile < ntiles; ++tile) {
         const size_t at = (size_t)tile * R + d;
         const uint32_t v = hist[at];
         hist[at] = run;
         run += v;
       }
+    }
   }
 }
 

@@ -8,12 +8,13 @@ from .. import build as lib_build
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 OUT = os.path.join(HERE, "_build", "spc_dropin_driver")
-SOURCES = [os.path.join(HERE, f) for f in ("dropin_driver.cpp", "spc_dropin.cpp")]
+SOURCES = [os.path.join(HERE, f) for f in ("dropin_driver.cpp", "spc_dropin.cpp", "spc_observer.cpp")]
 
 
 def build_driver(force: bool = False) -> str:
     lib = lib_build.build_library()
-    deps = SOURCES + [os.path.join(HERE, "spc_dropin.hpp"), lib, __file__]
+    deps = SOURCES + [os.path.join(HERE, "spc_dropin.hpp"), os.path.join(HERE, "spc_observer.hpp"),
+                      lib, __file__]
     if not force and os.path.exists(OUT) and all(
             os.path.getmtime(d) <= os.path.getmtime(OUT) for d in deps):
         return OUT

@@ -6,6 +6,8 @@
 // usage: SPC_REF_N=<N> SPC_REF_L=<L> spc_dropin_driver <input.bin> <output.bin>
 // (mode 0 = run, family 0 = vector classes, family 1 + SRK = vortex with the
 //  first N injected values as frequencies; modes 1/2 = one EvaluateRhs.)
+// With SPC_OUTPUT_DIR set, a run also writes the reference's observer files
+// there (a frame and a summary line after every step, as the engine loop does).
 #include <cstdint>
 #include <cstdio>
 #include <cstdlib>
@@ -13,6 +15,7 @@
 #include <vector>
 
 #include "spc_dropin.hpp"
+#include "spc_observer.hpp"
 
 static int env_int(const char *k) {
   const char *v = std::getenv(k);
@@ -60,6 +63,15 @@ int main(int argc, char **argv) {
   try {
     Thread thread(argc, argv);
     PeriodicBoundaryConditions pbc_config(&thread, kL, kL);
+    BinaryObserver *observer = nullptr;
+    if (std::getenv("SPC_OUTPUT_DIR") && h.mode == 0)
+      observer = new BinaryObserver(&thread, h.v0, h.sigma, h.rho, h.alpha, h.D_phi, h.rho_0, pbc_config,
+                                    h.dt, 0);
+    auto observe = [&](std::vector<Real> &s, Real t) {
+      if (!observer) return;
+      observer->SaveSystemState(s, t);
+      observer->SaveSummaryStatistics(s, t);
+    };
     if (h.family == 1 && h.stepper == 1 && h.mode == 0) {
       std::vector<Real> omega(noise.begin(), noise.begin() + kN);
       std::vector<Real> rest(noise.begin() + kN, noise.end());
@@ -72,6 +84,7 @@ int main(int argc, char **argv) {
         stepper.DoStep(system, state, t, h.dt);
         pbc_config.ApplyPeriodicBoundaryConditions(state);
         thread.SynchronizeVector(state);
+        observe(state, t);
         if ((h.record_every > 0 && k % h.record_every == 0) || k == h.nsteps) dump(state.data(), n3);
       }
     } else if (h.family == 0) {
@@ -101,6 +114,7 @@ int main(int argc, char **argv) {
             rk4.DoStep(chimera_system, state, t, h.dt);
           pbc_config.ApplyPeriodicBoundaryConditions(state);
           thread.SynchronizeVector(state);
+          observe(state, t);
           if ((h.record_every > 0 && k % h.record_every == 0) || k == h.nsteps) dump(state.data(), n3);
         }
       }
@@ -108,6 +122,7 @@ int main(int argc, char **argv) {
       std::fprintf(stderr, "spc_dropin_driver: unsupported family/stepper\n");
       return 5;
     }
+    delete observer;
   } catch (const std::exception &e) {
     std::fprintf(stderr, "%s\n", e.what());
     return 3;
