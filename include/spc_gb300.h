@@ -27,7 +27,7 @@
 extern "C" {
 #endif
 
-#define SPC_ABI_VERSION 1
+#define SPC_ABI_VERSION 2
 
 typedef enum spc_status {
   SPC_OK = 0,
@@ -45,7 +45,14 @@ typedef enum spc_status {
  * frequencies omega_i added to the phase drift of the stochastic
  * Runge-Kutta update, as StochasticRungeKuttaStepperPtr does
  * (Steppers/StochasticRungeKuttaStepperPtr.hpp:27-34, :65). */
-enum { SPC_MODEL_CHIMERA = 0, SPC_MODEL_VORTEX = 1 };
+enum { SPC_MODEL_CHIMERA = 0, SPC_MODEL_VORTEX = 1, SPC_MODEL_VORTEX_ARRAYS = 2 };
+/* VORTEX_ARRAYS: VortexArraysSystemPtr (DynamicalSystems/VortexArraysSystemPtr.cpp),
+ * velocity v0, distance-dependent alignment mu_plus (1 - r^2/xi_a^2) inside
+ * xi_a and anti-alignment -4 mu_minus (r - xi_a)(rho - r)/(rho - xi_a)^2 up to
+ * rho (:737-763), cohesion -kappa sin(atan2(dy, dx) - phi_i) inside xi_r, and
+ * its heavier stochastic Runge-Kutta second pass (:659-732).  Plain FP64 only;
+ * steppers EULER_PTR, SRK and RK4 (the *StepperPtr forms the reference pairs it
+ * with); the cell-list search (or all pairs when rho > L/4). */
 
 /* Stepper.  EULER: StochasticEulerStepper (Steppers/StochasticEulerStepper.hpp:31-47);
  * SRK: StochasticRungeKuttaStepper(Ptr) strong order 1.5
@@ -82,6 +89,8 @@ typedef struct spc_params {
   uint64_t seed;      /* Philox4x32-10 key */
   uint32_t system_id; /* Philox counter word: distinguishes systems sharing a seed */
   uint32_t flags;     /* SPC_FLAG_* */
+  /* VORTEX_ARRAYS only (VortexArraysSystemPtr ctor, VortexArraysSystemPtr.cpp:9-18) */
+  double mu_plus, mu_minus, xi_a, xi_r, kappa;
 } spc_params;
 
 typedef struct spc_handle spc_handle;

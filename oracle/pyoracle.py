@@ -53,6 +53,12 @@ def lib() -> C.CDLL:
                                        C.POINTER(D)]
         L.orc_philox4x32_10.argtypes = [C.POINTER(C.c_uint32), C.POINTER(C.c_uint32),
                                         C.POINTER(C.c_uint32)]
+        L.orc_va_create.restype = P
+        L.orc_va_create.argtypes = [C.c_int, D, D, D, D, D, D, D, D, D]
+        L.orc_va_rhs_rk.argtypes = [P, dp, dp, dp, D, D, C.c_void_p]
+        L.orc_va_rhs_srk.argtypes = [P, dp, dp, dp, C.c_void_p]
+        L.orc_va_run.restype = D
+        L.orc_va_run.argtypes = [P, C.c_int, dp, D, D, C.c_int, C.c_void_p]
         _lib = L
     return _lib
 
@@ -144,6 +150,33 @@ class OracleSystem:
                                C.byref(pf), C.byref(Rl))
         return {"R": R.value, "psi": psi.value, "R_f32": Rf.value, "psi_f32": pf.value,
                 "R_local": Rl.value}
+
+
+class OracleVortexArrays(OracleSystem):
+    """One VortexArraysSystemPtr with its steppers' persistent buffers."""
+
+    def __init__(self, n, L, velocity, mu_plus, mu_minus, xi_a, xi_r, D_phi, kappa, rho):
+        self.n = int(n)
+        self.h = lib().orc_va_create(self.n, L, velocity, mu_plus, mu_minus, xi_a, xi_r, D_phi,
+                                     kappa, rho)
+        if not self.h:
+            raise ValueError("bad oracle parameters")
+
+    def rhs_rk(self, state, k_prev, k_next, k_coef, dt, with_counts=False):
+        counts = np.zeros(3 * self.n, np.int32) if with_counts else None
+        lib().orc_va_rhs_rk(self.h, state, k_prev, k_next, k_coef, dt, _ptr(counts))
+        return counts
+
+    def rhs_srk(self, state, with_counts=False):
+        d = np.zeros(3 * self.n)
+        a = np.zeros(2 * self.n)
+        counts = np.zeros(3 * self.n, np.int32) if with_counts else None
+        lib().orc_va_rhs_srk(self.h, state, d, a, _ptr(counts))
+        return d, a, counts
+
+    def run(self, stepper, state, t0, dt, nsteps, noise=None, omega=None):
+        noise = None if noise is None else np.ascontiguousarray(noise, np.float64)
+        return lib().orc_va_run(self.h, stepper, state, t0, dt, nsteps, _ptr(noise))
 
 
 def philox4x32_10(ctr, key):

@@ -16,7 +16,7 @@ import numpy as np
 from . import build_oracle
 
 MODE_RUN, MODE_RHS_RK, MODE_RHS_SRK = 0, 1, 2
-FAMILY_VECTOR, FAMILY_PTR = 0, 1
+FAMILY_VECTOR, FAMILY_PTR, FAMILY_VA = 0, 1, 2
 STEP_EULER, STEP_SRK, STEP_RK4 = 0, 1, 2
 
 
@@ -27,7 +27,7 @@ def available() -> bool:
 def run_reference(n, L, *, mode, family=FAMILY_VECTOR, stepper=STEP_EULER, nsteps=0,
                   record_every=0, v0=0.01, sigma=1.0, rho=0.1, alpha=1.45, D_phi=0.005,
                   rho_0=1.0, t0=0.0, dt=0.01, k_coef=0.0, state=None, k_prev=None,
-                  k_next_init=None, noise=None, binary=None, extra_env=None):
+                  k_next_init=None, noise=None, binary=None, extra_env=None, va=None):
     """Returns the raw float64 output of the reference driver (or of another
     program reading the same input format, e.g. the drop-in driver)."""
     if binary is None:
@@ -52,6 +52,9 @@ def run_reference(n, L, *, mode, family=FAMILY_VECTOR, stepper=STEP_EULER, nstep
             f.write(k_next_init.tobytes())
             f.write(struct.pack("<q", noise.size))
             f.write(noise.tobytes())
+            if family == FAMILY_VA:
+                # mu_plus, mu_minus, xi_a, xi_r, kappa
+                f.write(struct.pack("<5d", *[float(v) for v in va]))
         env = dict(os.environ, SPC_REF_N=str(n), SPC_REF_L=repr(float(L)), **(extra_env or {}))
         subprocess.run([binary, fin, fout], check=True, env=env,
                        stdout=subprocess.DEVNULL)

@@ -14,13 +14,17 @@
 // mode 1 = one RK-form EvaluateRhs -> k_next[3N];
 // mode 2 = one SRK-form EvaluateRhs -> derivative[3N] then additional[2N] ([i][0], [i][1]).
 // family 0 = vector classes (Thread, ChimeraSystem, *Stepper);
-// family 1 = shared-window classes (ThreadSharedMemory, ChimeraSystemPtr, *StepperPtr).
+// family 1 = shared-window classes (ThreadSharedMemory, ChimeraSystemPtr, *StepperPtr);
+// family 2 = VortexArraysSystemPtr with the *StepperPtr classes; its five extra
+//            parameters follow the noise block: double mu_plus, mu_minus, xi_a,
+//            xi_r, kappa (velocity = v0, rho, D_phi from the header).
 // stepper 0 = StochasticEuler, 1 = StochasticRungeKutta, 2 = RungeKutta4.
 #include "Parallelization/Thread.hpp"
 #include "Parallelization/ThreadSharedMemory.hpp"
 #include "BoundaryConfiguration/PeriodicBoundaryConditions.hpp"
 #include "DynamicalSystems/ChimeraSystem.hpp"
 #include "DynamicalSystems/ChimeraSystemPtr.hpp"
+#include "DynamicalSystems/VortexArraysSystemPtr.hpp"
 #include "Steppers/StochasticEulerStepper.hpp"
 #include "Steppers/StochasticRungeKuttaStepper.hpp"
 #include "Steppers/RungeKutta4Stepper.hpp"
@@ -102,6 +106,8 @@ int main(int argc, char **argv) {
   read_exact(in, &n_noise, sizeof(n_noise));
   spc_ref::g_noise.resize((std::size_t)n_noise);
   if (n_noise) read_exact(in, spc_ref::g_noise.data(), (std::size_t)n_noise * sizeof(double));
+  double va[5] = {0, 0, 0, 0, 0};
+  if (h.family == 2) read_exact(in, va, sizeof(va));
   std::fclose(in);
 
   FILE *out = std::fopen(argv[2], "wb");
@@ -137,6 +143,43 @@ int main(int argc, char **argv) {
         pbc.ApplyPeriodicBoundaryConditions(state);
         if ((h.record_every > 0 && k % h.record_every == 0) || k == h.nsteps)
           dump(state.data(), n3);
+      }
+    }
+  } else if (h.family == 2) {
+    ThreadSharedMemory thread(argc, argv);
+    PeriodicBoundaryConditions pbc(&thread, kL, kL);
+    {
+      VortexArraysSystemPtr system(&thread, h.v0, va[0], va[1], va[2], va[3], h.D_phi, va[4], h.rho, pbc);
+      if (h.mode == 1) {
+        system.EvaluateRhs(state.data(), k_prev, k_next, h.k_coef, h.dt);
+        dump(k_next.data(), n3);
+      } else if (h.mode == 2) {
+        std::vector<Real> derivative(n3, 0.0);
+        std::vector<std::vector<Real>> additional(kN, std::vector<Real>(2, 0.0));
+        system.EvaluateRhs(state.data(), derivative, additional, h.dt);
+        dump(derivative.data(), n3);
+        for (int i = 0; i < kN; ++i) dump(additional[i].data(), 2);
+      } else {
+        // the SRK-Ptr constructor draws N natural frequencies first, which the
+        // vortex-arrays update does not use
+        StochasticRungeKuttaStepperPtr *srk =
+            h.stepper == 1 ? new StochasticRungeKuttaStepperPtr(&thread) : nullptr;
+        StochasticEulerStepperPtr euler(&thread);
+        RungeKutta4StepperPtr rk4(&thread);
+        Real t = h.t0;
+        for (int k = 1; k <= h.nsteps; ++k) {
+          t += h.dt;
+          if (h.stepper == 0)
+            euler.DoStep(system, state.data(), t, h.dt);
+          else if (h.stepper == 1)
+            srk->DoStep(system, state.data(), t, h.dt);
+          else
+            rk4.DoStep(system, state.data(), t, h.dt);
+          pbc.ApplyPeriodicBoundaryConditions(state.data(), (long)n3);
+          if ((h.record_every > 0 && k % h.record_every == 0) || k == h.nsteps)
+            dump(state.data(), n3);
+        }
+        delete srk;
       }
     }
   } else {

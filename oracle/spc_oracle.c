@@ -31,6 +31,11 @@ struct orc_system {
   double *det, *sto;    /* StochasticEulerStepper statics (StochasticEulerStepper.hpp:33) */
   double *deriv, *addl; /* StochasticRungeKuttaStepper statics (StochasticRungeKuttaStepper.hpp:36-38) */
   double *k[4];         /* RungeKutta4Stepper members (RungeKutta4Stepper.cpp:7-13) */
+  /* VortexArraysSystemPtr (VortexArraysSystemPtr.cpp:9-38); v0 is velocity_ */
+  int va;
+  double mu_plus, mu_minus, xi_a, xi_r, kappa;
+  double *anti, *coh;   /* antialignment_force_, cohesion_force_ */
+  double *card1, *card2;/* neighborhood_cardinality_[i][1], [i][2] ([i][0] is card) */
 };
 
 /* neighboring_cells_ in visiting order, {dx, dy} (ChimeraSystem.cpp:39-44) */
@@ -90,6 +95,10 @@ void orc_destroy(orc_system *s) {
   free(s->deriv);
   free(s->addl);
   for (int q = 0; q < 4; ++q) free(s->k[q]);
+  free(s->anti);
+  free(s->coh);
+  free(s->card1);
+  free(s->card2);
   free(s);
 }
 
@@ -520,4 +529,262 @@ void orc_philox4x32_10(const uint32_t ctr[4], const uint32_t key[2],
   out[1] = c1;
   out[2] = c2;
   out[3] = c3;
+}
+
+/* ======================================================================
+ * VortexArraysSystemPtr (DynamicalSystems/VortexArraysSystemPtr.cpp): the
+ * reference's second model.  Distance-dependent alignment mu+ (1 - r^2/xi_a^2)
+ * inside xi_a and anti-alignment -4 mu- (r - xi_a)(rho - r)/(rho - xi_a)^2 up
+ * to rho (:740-761), and cohesion -kappa sin(atan2(dy, dx) - phi_i) inside xi_r.
+ * The cutoffs compare dr = sqrt(dx^2 + dy^2); candidates are the 3x3 stencil
+ * of rho-cells (a cohesion partner beyond the stencil is not seen, as in the
+ * reference).
+ * ====================================================================== */
+
+orc_system *orc_va_create(int n, double L, double velocity, double mu_plus, double mu_minus,
+                          double xi_a, double xi_r, double D_phi, double kappa, double rho) {
+  orc_system *s = orc_create(n, L, velocity, 0.0, rho, 0.0, D_phi);
+  if (!s) return NULL;
+  s->va = 1;
+  s->mu_plus = mu_plus;
+  s->mu_minus = mu_minus;
+  s->xi_a = xi_a;
+  s->xi_r = xi_r;
+  s->kappa = kappa;
+  s->anti = (double *)calloc((size_t)n, sizeof(double));
+  s->coh = (double *)calloc((size_t)n, sizeof(double));
+  s->card1 = (double *)calloc((size_t)n, sizeof(double));
+  s->card2 = (double *)calloc((size_t)n, sizeof(double));
+  if (!s->anti || !s->coh || !s->card1 || !s->card2) {
+    orc_destroy(s);
+    return NULL;
+  }
+  return s;
+}
+
+/* AlignmentStrength (VortexArraysSystemPtr.cpp:737-749) */
+static double va_strength(const orc_system *s, double r) {
+  if (r < s->xi_a) return s->mu_plus * (1.0 - r * r / (s->xi_a * s->xi_a));
+  if (r < s->rho)
+    return -s->mu_minus * 4.0 * (r - s->xi_a) * (s->rho - r) / (s->rho - s->xi_a) / (s->rho - s->xi_a);
+  return 0.0;
+}
+
+/* AlignmentStrengthDerivative (VortexArraysSystemPtr.cpp:751-763) */
+static double va_strength_derivative(const orc_system *s, double r) {
+  if (r < s->xi_a) return s->mu_plus * (-2.0 * r / s->xi_a / s->xi_a);
+  if (r < s->rho)
+    return -s->mu_minus * 4.0 * (-2.0 * r + s->rho + s->xi_a) / (s->rho - s->xi_a) / (s->rho - s->xi_a);
+  return 0.0;
+}
+
+/* Every candidate j != i of i with its minimum-image (dx, dy): the 3x3
+ * stencil with copy-wrapped positions (VortexArraysSystemPtr.cpp:446-473), or
+ * all pairs on the unwrapped stage positions (:164-183). */
+typedef void (*va_visit_fn)(void *ctx, int i, int j, double dx, double dy, const double *pos);
+
+static void va_for_each_candidate(orc_system *s, const double *pos, int i, va_visit_fn fn,
+                                  void *ctx) {
+  if (!orc_uses_cell_list(s)) {
+    const double xi = pos[3 * i], yi = pos[3 * i + 1];
+    for (int j = 0; j < s->n; ++j) {
+      if (j == i) continue;
+      double dx, dy;
+      orc_min_image(s, xi, yi, pos[3 * j], pos[3 * j + 1], &dx, &dy);
+      fn(ctx, i, j, dx, dy, pos);
+    }
+    return;
+  }
+  const int nc = s->nc;
+  double xi = pos[3 * i], yi = pos[3 * i + 1];
+  wrap_if_outside(s, &xi, &yi);
+  int cx = cell_coord(s, xi, 0);
+  int cy = cell_coord(s, yi, 0);
+  for (int q = 0; q < 9; ++q) {
+    int jx = adjust_cell(cx + kStencil[q][0], nc);
+    int jy = adjust_cell(cy + kStencil[q][1], nc);
+    int c = jy * nc + jx;
+    for (int p = s->cell_start[c]; p < s->cell_start[c + 1]; ++p) {
+      int j = s->cell_items[p];
+      if (j == i) continue;
+      double xj = pos[3 * j], yj = pos[3 * j + 1];
+      wrap_if_outside(s, &xj, &yj);
+      double dx, dy;
+      orc_min_image(s, xi, yi, xj, yj, &dx, &dy);
+      fn(ctx, i, j, dx, dy, pos);
+    }
+  }
+}
+
+/* pass 1 (VortexArraysSystemPtr.cpp:472-488, all pairs :183-199) */
+static void va_visit_pass1(void *ctx, int i, int j, double dx, double dy, const double *pos) {
+  orc_system *s = (orc_system *)ctx;
+  const double phi_i = pos[3 * i + 2], phi_j = pos[3 * j + 2];
+  const double dr = sqrt(dx * dx + dy * dy);
+  if (dr <= s->xi_a) {
+    s->af[i] += va_strength(s, dr) * sin(phi_j - phi_i);
+    s->card[i] += 1.0;
+  } else if (dr <= s->rho) {
+    s->anti[i] += va_strength(s, dr) * sin(phi_j - phi_i);
+    s->card1[i] += 1.0;
+  }
+  if (dr <= s->xi_r) {
+    s->coh[i] += -s->kappa * sin(atan2(dy, dx) - phi_i);
+    s->card2[i] += 1.0;
+  }
+}
+
+static void va_reset(orc_system *s) {
+  const size_t n = (size_t)s->n;
+  memset(s->af, 0, n * sizeof(double));
+  memset(s->anti, 0, n * sizeof(double));
+  memset(s->coh, 0, n * sizeof(double));
+  memset(s->card, 0, n * sizeof(double));
+  memset(s->card1, 0, n * sizeof(double));
+  memset(s->card2, 0, n * sizeof(double));
+}
+
+/* the phase rate of k_next / derivative (VortexArraysSystemPtr.cpp:493-504):
+ * written only when the particle has (anti-)alignment partners, then the
+ * cohesion mean added on top when it has cohesion partners */
+static void va_rate(const orc_system *s, int i, double *out) {
+  if ((s->card[i] + s->card1[i]) > 0)
+    *out = (s->af[i] + s->anti[i]) / (s->card[i] + s->card1[i]);
+  if (s->card2[i] > 0) *out += s->coh[i] / s->card2[i];
+}
+
+void orc_va_rhs_rk(orc_system *s, const double *state, const double *k_prev, double *k_next,
+                   double k_coef, double dt, int *counts3) {
+  const int n = s->n;
+  va_reset(s);
+  for (int i = 0; i < 3 * n; ++i) s->rk[i] = state[i] + k_coef * dt * k_prev[i];
+  if (orc_uses_cell_list(s)) build_linked_list(s, s->rk);
+  for (int i = 0; i < n; ++i) {
+    va_for_each_candidate(s, s->rk, i, va_visit_pass1, s);
+    const double phi_i = s->rk[3 * i + 2];
+    k_next[3 * i] = s->v0 * cos(phi_i);
+    k_next[3 * i + 1] = s->v0 * sin(phi_i);
+    va_rate(s, i, &k_next[3 * i + 2]);
+    if (counts3) {
+      counts3[3 * i] = (int)s->card[i];
+      counts3[3 * i + 1] = (int)s->card1[i];
+      counts3[3 * i + 2] = (int)s->card2[i];
+    }
+  }
+}
+
+typedef struct {
+  orc_system *s;
+  const double *d;
+  double *a;
+} va_pass2_ctx;
+
+/* pass 2 (VortexArraysSystemPtr.cpp:659-732, all pairs :302-352) */
+static void va_visit_pass2(void *vctx, int i, int j, double dx, double dy, const double *pos) {
+  va_pass2_ctx *c = (va_pass2_ctx *)vctx;
+  orc_system *s = c->s;
+  const double *d = c->d;
+  const int ii = 3 * i, jj = 3 * j;
+  const double phi_i = pos[ii + 2], phi_j = pos[jj + 2];
+  const double dr = sqrt(dx * dx + dy * dy);
+  const double norm_1 = s->card[i] + s->card1[i];
+  const double norm_2 = s->card2[i];
+  if ((dr <= s->rho) && (norm_1 > 0.0)) {
+    const double cp = cos(phi_j - phi_i);
+    const double sp = sin(phi_j - phi_i);
+    const double as = va_strength(s, dr);
+    const double asd = va_strength_derivative(s, dr);
+    c->a[2 * i] += -as * cp / norm_1;
+    c->a[2 * i + 1] += ((d[jj] - d[ii]) * asd * dx / dr + (d[jj + 1] - d[ii + 1]) * asd * dy / dr) * sp / norm_1
+                       + (d[jj + 2] - d[ii + 2]) * as * cp / norm_1
+                       - 2.0 * s->D_phi * sp * as / norm_1;
+  }
+  if ((dr <= s->xi_r) && (norm_2 > 0.0)) {
+    const double cq = cos(atan2(dy, dx) - phi_i);
+    const double sq = sin(atan2(dy, dx) - phi_i);
+    c->a[2 * i] += s->kappa * cq / norm_2;
+    c->a[2 * i + 1] += -s->kappa * ((d[jj] - d[ii]) * (-dy) / dr / dr + (d[jj + 1] - d[ii + 1]) * dx / dr / dr
+                                    - d[ii + 2]) * cq / norm_2
+                       + s->kappa * s->D_phi * sq / norm_2;
+  }
+}
+
+void orc_va_rhs_srk(orc_system *s, const double *state, double *derivative, double *additional,
+                    int *counts3) {
+  const int n = s->n;
+  va_reset(s);
+  if (orc_uses_cell_list(s)) build_linked_list(s, state);
+  for (int i = 0; i < n; ++i) {
+    va_for_each_candidate(s, state, i, va_visit_pass1, s);
+    const double phi_i = state[3 * i + 2];
+    derivative[3 * i] = s->v0 * cos(phi_i);
+    derivative[3 * i + 1] = s->v0 * sin(phi_i);
+    va_rate(s, i, &derivative[3 * i + 2]);
+    if (counts3) {
+      counts3[3 * i] = (int)s->card[i];
+      counts3[3 * i + 1] = (int)s->card1[i];
+      counts3[3 * i + 2] = (int)s->card2[i];
+    }
+  }
+  va_pass2_ctx c = {s, derivative, additional};
+  for (int i = 0; i < n; ++i) {
+    va_for_each_candidate(s, state, i, va_visit_pass2, &c);
+    additional[2 * i] *= sqrt(2.0 * s->D_phi);
+  }
+}
+
+/* StochasticEulerStepperPtr / StochasticRungeKuttaStepperPtr /
+ * RungeKutta4StepperPtr DoStep for VortexArraysSystemPtr
+ * (StochasticEulerStepperPtr.hpp:56-76, StochasticRungeKuttaStepperPtr.hpp:70-96,
+ * RungeKutta4StepperPtr.cpp:45-63). */
+static void va_step(orc_system *s, int stepper, double *state, double dt, const double *noise) {
+  const int n = s->n;
+  if (stepper == ORC_RK4) {
+    double *k1 = s->k[0], *k2 = s->k[1], *k3 = s->k[2], *k4 = s->k[3];
+    orc_va_rhs_rk(s, state, k1, k1, 0.0, dt, NULL);
+    orc_va_rhs_rk(s, state, k1, k2, 0.5, dt, NULL);
+    orc_va_rhs_rk(s, state, k2, k3, 0.5, dt, NULL);
+    orc_va_rhs_rk(s, state, k3, k4, 1.0, dt, NULL);
+    for (int i = 0; i < n; ++i) {
+      int ii = 3 * i;
+      state[ii] += (k1[ii] + 2.0 * k2[ii] + 2.0 * k3[ii] + k4[ii]) * dt / 6.0;
+      state[ii + 1] += (k1[ii + 1] + 2.0 * k2[ii + 1] + 2.0 * k3[ii + 1] + k4[ii + 1]) * dt / 6.0;
+      state[ii + 2] += (k1[ii + 2] + 2.0 * k2[ii + 2] + 2.0 * k3[ii + 2] + k4[ii + 2]) / 6.0 * dt;
+    }
+    return;
+  }
+  memset(s->deriv, 0, (size_t)3 * n * sizeof(double));
+  memset(s->addl, 0, (size_t)2 * n * sizeof(double));
+  orc_va_rhs_srk(s, state, s->deriv, s->addl, NULL);
+  const double D = s->D_phi;
+  for (int i = 0; i < n; ++i) {
+    const double *d = s->deriv + 3 * i;
+    const double *a = s->addl + 2 * i;
+    if (stepper == ORC_EULER_PTR) {
+      double delta_W = sqrt(dt) * noise[i];
+      state[3 * i] += d[0] * dt;
+      state[3 * i + 1] += d[1] * dt;
+      state[3 * i + 2] += d[2] * dt + sqrt(2.0 * D) * delta_W;
+    } else {
+      double U_1 = noise[2 * i], U_2 = noise[2 * i + 1];
+      double delta_W = U_1 * sqrt(dt);
+      double delta_Z = 0.5 * dt * sqrt(dt) * (U_1 + U_2 / sqrt(3.0));
+      state[3 * i] += d[0] * dt - sqrt(2.0 * D) * d[1] * delta_Z - 0.5 * (d[2] * d[1] + D * d[0]) * dt * dt;
+      state[3 * i + 1] += d[1] * dt + sqrt(2.0 * D) * d[0] * delta_Z + 0.5 * (d[2] * d[0] - D * d[1]) * dt * dt;
+      state[3 * i + 2] += d[2] * dt + sqrt(2.0 * D) * delta_W + a[0] * delta_Z + 0.5 * a[1] * dt * dt;
+    }
+  }
+}
+
+double orc_va_run(orc_system *s, int stepper, double *state, double t0, double dt, int nsteps,
+                  const double *noise) {
+  double t = t0;
+  const int n = s->n;
+  const int per = stepper == ORC_SRK ? 2 * n : (stepper == ORC_EULER_PTR ? n : 0);
+  for (int k = 0; k < nsteps; ++k) {
+    t += dt;
+    va_step(s, stepper, state, dt, noise ? noise + (size_t)k * per : NULL);
+    orc_wrap_state(s, state); /* SimulationEnginePtr.cpp:111 */
+  }
+  return t;
 }

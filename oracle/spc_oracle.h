@@ -108,6 +108,24 @@ void orc_order_params(orc_system *s, const double *state, double *R,
                       double *psi, float *R_f32, float *psi_f32,
                       double *R_local);
 
+/* VortexArraysSystemPtr (DynamicalSystems/VortexArraysSystemPtr.cpp): the
+ * reference's second model, alignment mu+ / anti-alignment mu- by distance and
+ * cohesion kappa (ctor :9-88; RHS :357-507 RK form, :509-735 SRK form, all
+ * pairs :136-355).  Destroy with orc_destroy; the RK4 buffers are
+ * orc_get/set_rk4_buffers.  counts3 (may be NULL) receives per particle the
+ * three neighborhood_cardinality_ entries. */
+orc_system *orc_va_create(int n, double L, double velocity, double mu_plus, double mu_minus,
+                          double xi_a, double xi_r, double D_phi, double kappa, double rho);
+void orc_va_rhs_rk(orc_system *s, const double *state, const double *k_prev, double *k_next,
+                   double k_coef, double dt, int *counts3);
+void orc_va_rhs_srk(orc_system *s, const double *state, double *derivative, double *additional,
+                    int *counts3);
+/* Engine loop with StochasticEulerStepperPtr (ORC_EULER_PTR, N normals per
+ * step), StochasticRungeKuttaStepperPtr (ORC_SRK, 2N: U1, U2 per particle) or
+ * RungeKutta4StepperPtr (ORC_RK4, no noise). */
+double orc_va_run(orc_system *s, int stepper, double *state, double t0, double dt, int nsteps,
+                  const double *noise);
+
 /* Philox4x32-10 (Salmon, Moraes, Dror, Shaw, SC'11): 10 rounds on counter
  * ctr[4] with key key[2]; out[4]. */
 void orc_philox4x32_10(const uint32_t ctr[4], const uint32_t key[2],

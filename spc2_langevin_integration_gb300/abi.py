@@ -14,7 +14,7 @@ import numpy as np
 
 from . import build as _build
 
-MODEL_CHIMERA, MODEL_VORTEX = 0, 1
+MODEL_CHIMERA, MODEL_VORTEX, MODEL_VORTEX_ARRAYS = 0, 1, 2
 STEPPER_EULER, STEPPER_SRK, STEPPER_RK4, STEPPER_EULER_PTR = 0, 1, 2, 3
 NEIGHBOUR_CELL, NEIGHBOUR_VERLET = 0, 1
 PRECISION_FP64, PRECISION_FP32C = 0, 1
@@ -42,6 +42,8 @@ class Params(C.Structure):
         ("sigma", C.c_double), ("rho", C.c_double), ("alpha", C.c_double),
         ("D_phi", C.c_double), ("rho_0", C.c_double), ("skin", C.c_double),
         ("seed", C.c_uint64), ("system_id", C.c_uint32), ("flags", C.c_uint32),
+        ("mu_plus", C.c_double), ("mu_minus", C.c_double), ("xi_a", C.c_double),
+        ("xi_r", C.c_double), ("kappa", C.c_double),
     ]
 
 
@@ -149,11 +151,20 @@ def _f64(a, n: int) -> np.ndarray:
     return a
 
 
-def make_params(*, L, v0, sigma, rho, alpha, D_phi, rho_0=1.0, model=MODEL_CHIMERA,
+def make_params(*, L, v0, sigma=0.0, rho, alpha=0.0, D_phi, rho_0=1.0, model=MODEL_CHIMERA,
                 stepper=STEPPER_EULER, neighbour=NEIGHBOUR_CELL, precision=PRECISION_FP64,
-                skin=0.05, seed=0, system_id=0, flags=0) -> Params:
+                skin=0.05, seed=0, system_id=0, flags=0, mu_plus=0.0, mu_minus=0.0, xi_a=0.0,
+                xi_r=0.0, kappa=0.0) -> Params:
     return Params(model, stepper, neighbour, precision, L, v0, sigma, rho, alpha, D_phi, rho_0,
-                  skin, seed, system_id, flags)
+                  skin, seed, system_id, flags, mu_plus, mu_minus, xi_a, xi_r, kappa)
+
+
+def make_va_params(*, L, velocity, mu_plus, mu_minus, xi_a, xi_r, D_phi, kappa, rho,
+                   stepper=STEPPER_SRK, seed=0, system_id=0, flags=0) -> Params:
+    """VortexArraysSystemPtr parameters in the reference's ctor order."""
+    return make_params(L=L, v0=velocity, rho=rho, D_phi=D_phi, model=MODEL_VORTEX_ARRAYS,
+                       stepper=stepper, seed=seed, system_id=system_id, flags=flags,
+                       mu_plus=mu_plus, mu_minus=mu_minus, xi_a=xi_a, xi_r=xi_r, kappa=kappa)
 
 
 class System:

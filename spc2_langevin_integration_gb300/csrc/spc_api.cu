@@ -841,6 +841,7 @@ extern "C" int spc_rhs_srk_noalloc(const spc_params *p, int32_t n, const double 
   a.n_active = n;
   a.ncell_total = ncell;
   a.ncell_tile = sc.allpairs ? 0 : ncell;  // cell-tile kernels only
+  a.va_c0 = a.va_c1 = ncell;
   e.ncell_tile = a.ncell_tile;
   e.ncell_warp = 0;
   a.n_ap = sc.allpairs ? 1 : 0;

@@ -26,6 +26,7 @@ struct SysConst {
   int ncell;      // nc * nc
   int allpairs;   // rho > 0.25 L: EvaluateInteractionsWithAllPairs (ChimeraSystem.cpp:90-98)
   double L, rL;   // x_size_, x_rsize_ = 1.0 / x_size
+  double rho;     // rho_
   double rho2;    // rho_squared_ = rho * rho
   double v0, sigma, alpha, D;
   double cell;    // cell side L / nc, origin of the float prefilter coordinates
@@ -38,6 +39,10 @@ struct SysConst {
   int vR;         // stencil radius in cells, ceil(r_max / cell)
   float vr2;      // build: candidates with float dr^2 <= vr2 (r_max^2 plus a margin) are listed
   double vdisp2;  // a displacement with dr^2 > vdisp2 (about (skin / 2)^2) forces a rebuild
+  // VortexArraysSystemPtr (va = 1): v0 is velocity_, D the rotational diffusion
+  int va;
+  double mu_plus, mu_minus, xi_a, xi_r, kappa;
+  float va_r2;    // float dr^2 above this: beyond rho and xi_r for certain
 };
 
 // PeriodicBoundaryConditions::ClassAEffectiveParticleDistance (PeriodicBoundaryConditions.cpp:22-35):

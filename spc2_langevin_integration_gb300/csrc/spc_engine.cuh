@@ -29,6 +29,7 @@
 #include "spc_tile.cuh"
 #include "spc_warp.cuh"
 #include "spc_verlet.cuh"
+#include "spc_va.cuh"
 
 namespace spc {
 
@@ -63,6 +64,7 @@ inline SysConst make_sysconst(const spc_params &p, int n) {
   sc.n = n;
   sc.L = p.L;
   sc.rL = 1.0 / p.L;
+  sc.rho = p.rho;
   sc.rho2 = p.rho * p.rho;
   sc.v0 = p.v0;
   sc.sigma = p.sigma;
@@ -81,8 +83,18 @@ inline SysConst make_sysconst(const spc_params &p, int n) {
   sc.L_pow2 = is_pow2(p.L);
   sc.cos_a = (float)std::cos(p.alpha);
   sc.sin_a = (float)std::sin(p.alpha);
+  if (p.model == SPC_MODEL_VORTEX_ARRAYS) {
+    sc.va = 1;
+    sc.mu_plus = p.mu_plus;
+    sc.mu_minus = p.mu_minus;
+    sc.xi_a = p.xi_a;
+    sc.xi_r = p.xi_r;
+    sc.kappa = p.kappa;
+    const double rm = std::max(p.rho, p.xi_r);
+    sc.va_r2 = (float)(rm * rm * (1.0 + 3e-5));
+  }
   // Verlet rows over a (2R+1)^2 stencil of rho-cells; needs 2R+1 distinct cells
-  if (p.neighbour == SPC_NEIGHBOUR_VERLET && !sc.allpairs) {
+  if (p.neighbour == SPC_NEIGHBOUR_VERLET && !sc.allpairs && !sc.va) {
     const double rmax = p.rho + p.skin;
     const int R = (int)std::ceil(rmax / sc.cell);
     if (R >= 1 && R <= kVMaxR && sc.nc >= 2 * R + 1) {
@@ -111,7 +123,16 @@ inline int validate_params(const spc_params *p, int n, std::string &why) {
   if (!(p->D_phi >= 0.0) || !std::isfinite(p->D_phi)) return bad("D_phi must be >= 0");
   if (!std::isfinite(p->v0) || !std::isfinite(p->sigma) || !std::isfinite(p->alpha))
     return bad("v0, sigma, alpha must be finite");
-  if (p->model != SPC_MODEL_CHIMERA && p->model != SPC_MODEL_VORTEX) return bad("unknown model");
+  if (p->model != SPC_MODEL_CHIMERA && p->model != SPC_MODEL_VORTEX && p->model != SPC_MODEL_VORTEX_ARRAYS)
+    return bad("unknown model");
+  if (p->model == SPC_MODEL_VORTEX_ARRAYS) {
+    if (p->precision != SPC_PRECISION_FP64) return bad("the vortex-arrays model runs in plain FP64");
+    if (p->stepper == SPC_STEPPER_EULER)
+      return bad("the vortex-arrays model pairs with the Euler-Ptr, SRK and RK4 steppers");
+    if (!(p->xi_a > 0.0) || !std::isfinite(p->xi_a) || !(p->xi_r >= 0.0) || !std::isfinite(p->xi_r) ||
+        !std::isfinite(p->mu_plus) || !std::isfinite(p->mu_minus) || !std::isfinite(p->kappa))
+      return bad("vortex arrays: xi_a > 0, xi_r >= 0, finite mu and kappa");
+  }
   if (p->stepper < SPC_STEPPER_EULER || p->stepper > SPC_STEPPER_EULER_PTR) return bad("unknown stepper");
   if (p->model == SPC_MODEL_VORTEX && p->stepper != SPC_STEPPER_SRK && p->stepper != SPC_STEPPER_EULER)
     return bad("the vortex model's natural frequencies enter the Euler and stochastic Runge-Kutta drifts only");
@@ -145,7 +166,9 @@ struct Engine {
   int pool_cap = 0, sys_cap = 0, cell_cap = 0, tile_cap = 0;
   KArgs a{};
   SysDesc *d_sys = nullptr;
-  int *d_ap = nullptr;
+  int *d_ap = nullptr;      // cells of the all-pairs systems the all-pairs kernel integrates
+  int *d_ap_all = nullptr;  // ... and of every all-pairs system (diagnostics)
+  int n_ap_all = 0;
   unsigned long long *d_clamped = nullptr;
   uint32_t *keys_alt = nullptr, *vals_alt = nullptr, *hist = nullptr, *part = nullptr;
   double *aos = nullptr;  // AoS staging (12 x pool_cap doubles)
@@ -159,7 +182,7 @@ struct Engine {
   bool dirty = true;
   // current layout
   int nsys = 0, n_active = 0, ncell_total = 0, ntiles = 0, radix_bits = 1, sort_passes = 1;
-  int ncell_tile = 0, ncell_warp = 0;  // cells of the cell-tile and of the warp-per-cell systems
+  int ncell_tile = 0, ncell_warp = 0, ncell_va = 0;  // cells of the tile, warp and vortex-arrays systems
   bool has_cells = false;
   // tuning: cell-list systems with fewer than sparse_below particles per cell
   // (on average) run the warp-per-cell passes
@@ -248,6 +271,7 @@ inline void engine_footprint(int stepper, int precision, long long *per_particle
   if (stepper == SPC_STEPPER_RK4) b += 12 * 8;  // k1..k4
   b += 3 * 8 + 4 * 4 + 3 * 8 + 8 + 4 + 8 + 4 + 4 + 4;  // stage, sort, cell order, fxy, pidx, dphi, cnt, sys_of_p
   if (precision == SPC_PRECISION_FP32C) b += 8 + 4 + (long long)kMaskWords * 4;  // cs, dphi_f, masks
+  if (precision == SPC_PRECISION_FP64) b += 8 + 8 + 4;                          // vortex-arrays outputs
   b += 12 * 8 + 4 + 4;                       // AoS staging, histogram share
   *per_particle = b;
   *per_cell = 4 + 4;                         // cell_start, sys_of_c
@@ -291,6 +315,11 @@ inline int engine_init(Engine *e, int stepper, int precision, int pool_cap, int 
   SPC_TRY(dalloc(e, &a.pidx, N));
   SPC_TRY(dalloc(e, &a.dphi_s, N));
   SPC_TRY(dalloc(e, &a.cnt_s, N));
+  if (precision == SPC_PRECISION_FP64) {  // vortex-arrays pass-1 outputs
+    SPC_TRY(dalloc(e, &a.va_vx, N));
+    SPC_TRY(dalloc(e, &a.va_vy, N));
+    SPC_TRY(dalloc(e, &a.va_cnt2, N));
+  }
   int *sys_of_p = nullptr, *sys_of_c = nullptr;
   SPC_TRY(dalloc(e, &sys_of_p, N));
   a.sys_of_p = sys_of_p;
@@ -307,6 +336,7 @@ inline int engine_init(Engine *e, int stepper, int precision, int pool_cap, int 
   SPC_TRY(dalloc(e, &e->part, (size_t)(1 << 11) * ((e->tile_cap + kScanGroup - 1) / kScanGroup)));
   SPC_TRY(dalloc(e, &e->d_sys, (size_t)sys_cap));
   SPC_TRY(dalloc(e, &e->d_ap, (size_t)sys_cap));
+  SPC_TRY(dalloc(e, &e->d_ap_all, (size_t)sys_cap));
   SPC_TRY(dalloc(e, &e->d_clamped, 1));
   SPC_TRY(dalloc(e, &e->aos, 12 * N));
   e->order_blocks = std::min(blocks_for((long long)N, 256), 1024);
@@ -491,9 +521,11 @@ inline SysDesc desc_of(const SysHost &h, int dense_p0, int c0) {
 }
 
 // 0: cell list, dense cells (cell-tile kernels); 1: cell list, sparse cells
-// (warp-per-cell kernel); 2: all pairs.
+// (warp-per-cell kernel); 2: vortex-arrays model (its own kernel, cell list or
+// all pairs); 3: all pairs.
 inline int system_class(const Engine *e, const SysHost &h) {
-  if (h.sc.allpairs) return 2;
+  if (h.sc.va) return 2;
+  if (h.sc.allpairs) return 3;
   return (double)h.n < e->sparse_below * (double)h.ncell ? 1 : 0;
 }
 
@@ -503,27 +535,30 @@ inline int engine_layout(Engine *e) {
   drop_graph(e);
   e->verlet_stale = true;  // slots and systems move: rebuild the rows
   std::vector<SysDesc> table;
-  std::vector<int> ap;
+  std::vector<int> ap, ap_all;
   int dense = 0, cells = 0;
   std::fill(e->slot_layout.begin(), e->slot_layout.end(), -1);
-  // cell-tile systems first, then warp-per-cell systems, then all-pairs ones,
-  // so that each neighbour kernel covers one contiguous range of cells
-  int ncell_tile = 0, ncell_warp = 0;
-  for (int cls = 0; cls < 3; ++cls) {
+  // cell-tile systems first, then warp-per-cell, vortex-arrays and all-pairs
+  // systems, so that each neighbour kernel covers one contiguous range of cells
+  int ncell_tile = 0, ncell_warp = 0, ncell_va = 0;
+  for (int cls = 0; cls < 4; ++cls) {
     for (int slot : e->order) {
       const SysHost &h = e->slots[slot];
       if (system_class(e, h) != cls) continue;
       e->slot_layout[slot] = (int)table.size();
       table.push_back(desc_of(h, dense, cells));
-      if (h.sc.allpairs) ap.push_back(cells);
+      if (cls == 3) ap.push_back(cells);
+      if (h.sc.allpairs) ap_all.push_back(cells);
       dense += h.n;
       cells += h.ncell;
       if (cls == 0) ncell_tile += h.ncell;
       if (cls == 1) ncell_warp += h.ncell;
+      if (cls == 2) ncell_va += h.ncell;
     }
   }
   e->ncell_tile = ncell_tile;
   e->ncell_warp = ncell_warp;
+  e->ncell_va = ncell_va;
   e->nsys = (int)table.size();
   e->n_active = dense;
   e->ncell_total = cells;
@@ -532,12 +567,15 @@ inline int engine_layout(Engine *e) {
   while (bits < 31 && (1u << bits) < (unsigned)std::max(cells, 2)) ++bits;
   e->sort_passes = (bits + 10) / 11;
   e->radix_bits = (bits + e->sort_passes - 1) / e->sort_passes;
-  e->has_cells = cells > (int)ap.size();
+  e->has_cells = ncell_tile + ncell_warp > 0;
+  e->n_ap_all = (int)ap_all.size();
   KArgs &a = e->a;
   a.nsys = e->nsys;
   a.n_active = e->n_active;
   a.ncell_total = e->ncell_total;
   a.ncell_tile = e->ncell_tile;
+  a.va_c0 = e->ncell_tile + e->ncell_warp;
+  a.va_c1 = a.va_c0 + e->ncell_va;
   a.n_ap = (int)ap.size();
   a.hist_len = (1 << e->radix_bits) * e->ntiles;
   if (e->nsys > 0) {
@@ -546,6 +584,9 @@ inline int engine_layout(Engine *e) {
     if (!ap.empty())
       SPC_CUDA(e, cudaMemcpyAsync(e->d_ap, ap.data(), ap.size() * sizeof(int), cudaMemcpyHostToDevice,
                                   e->stream));
+    if (!ap_all.empty())
+      SPC_CUDA(e, cudaMemcpyAsync(e->d_ap_all, ap_all.data(), ap_all.size() * sizeof(int),
+                                  cudaMemcpyHostToDevice, e->stream));
     const int g = std::max(e->n_active, e->ncell_total);
     k_layout_maps<<<blocks_for(g, 256), 256, 0, e->stream>>>(e->d_sys, e->nsys, e->n_active, e->ncell_total,
                                                              (int *)a.sys_of_p, (int *)a.sys_of_c);
@@ -644,6 +685,23 @@ inline int eval_cells(Engine *e, KArgs &a, int rk_form, int kq, double kcdt, boo
 template <int PREC, int KIND>
 int launch_pass_t(Engine *e, const KArgs &a, int epi) {
   cudaStream_t st = e->stream;
+  if constexpr (KIND == kKindNb) {
+    // diagnostics count neighbours within rho for every model: the all-pairs
+    // kernel takes every all-pairs system, the cell kernel every cell list
+    KArgs b = a;
+    b.ap_cells = e->d_ap_all;
+    b.n_ap = e->n_ap_all;
+    if (b.n_ap > 0) {
+      k_allpairs_pass<PREC, KIND><<<std::min(b.n_ap, 152 * 16), kAllPairsThreads, 0, st>>>(b, epi);
+      SPC_LAUNCHED(e);
+    }
+    if (e->ncell_total > e->n_ap_all) {
+      k_cell_pass<PREC, KIND><<<std::min(blocks_for(e->ncell_total, kPassWarps), 152 * 64), kPassThreads, 0,
+                                st>>>(b, epi);
+      SPC_LAUNCHED(e);
+    }
+    return SPC_OK;
+  }
   if (a.n_ap > 0) {
     k_allpairs_pass<PREC, KIND><<<std::min(a.n_ap, 152 * 16), kAllPairsThreads, 0, st>>>(a, epi);
     SPC_LAUNCHED(e);
@@ -655,12 +713,14 @@ int launch_pass_t(Engine *e, const KArgs &a, int epi) {
       return SPC_OK;
     }
   }
-  if (e->has_cells) {
-    if constexpr (KIND == kKindNb) {
-      k_cell_pass<PREC, KIND><<<std::min(blocks_for(e->ncell_total, kPassWarps), 152 * 64), kPassThreads, 0,
-                                st>>>(a, epi);
+  if constexpr (PREC == kPrecFP64 && KIND != kKindNb) {
+    if (e->ncell_va > 0) {
+      k_va_pass<KIND><<<std::min(e->ncell_va, 152 * 64), kVAThreads, 0, st>>>(a, epi);
       SPC_LAUNCHED(e);
-    } else {
+    }
+  }
+  if (e->has_cells) {
+    {
       if (e->ncell_tile > 0) {
         const int grid = std::min(e->ncell_tile, 152 * 256);
         if constexpr (PREC == kPrecFP32C)

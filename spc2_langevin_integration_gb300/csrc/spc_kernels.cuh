@@ -67,7 +67,8 @@ struct KArgs {
   int nsys;
   int n_active;                      // dense particles
   int ncell_total;
-  int ncell_tile;                    // cells [0, ncell_tile): cell-tile kernels; the rest: warp kernel
+  int ncell_tile;                    // cells [0, ncell_tile): cell-tile kernels
+  int va_c0, va_c1;                  // [ncell_tile, va_c0): warp kernel; [va_c0, va_c1): vortex arrays
   const int *sys_of_p;               // dense index -> system
   const int *sys_of_c;               // global cell -> system
   // state pool (structure of arrays)
@@ -87,6 +88,8 @@ struct KArgs {
   double *dphi_s;                    // SRK pass 1 phase rate, cell order
   float *dphi_f;                     // same, float (FP32C)
   int *cnt_s;                        // n_i, cell order
+  double *va_vx, *va_vy;             // vortex arrays: pass-1 velocity components, cell order
+  int *va_cnt2;                      // vortex arrays: cohesion partners, cell order
   uint32_t *nbmask;                  // FP32C: pass-1 neighbour bitmasks [word][n_active], or null
   uint32_t *hist;                    // radix histogram table (zeroed by k_gather)
   int hist_len;

@@ -85,7 +85,7 @@ __global__ void __launch_bounds__(kWarpPassThreads, 8) k_warp_fp32c(KArgs a, int
   WarpStage32<KIND> &sm = stage_all[w];
   const int n_all = a.n_active;
   const int stride = gridDim.x * kWarpPassWarps;
-  for (int c = a.ncell_tile + blockIdx.x * kWarpPassWarps + w; c < a.ncell_total; c += stride) {
+  for (int c = a.ncell_tile + blockIdx.x * kWarpPassWarps + w; c < a.va_c0; c += stride) {
     const int cb = a.cell_start[c], ce = a.cell_start[c + 1];
     if (cb == ce) continue;
     const SysDesc &sd = a.sys[a.sys_of_c[c]];
@@ -227,7 +227,7 @@ __global__ void __launch_bounds__(kWarpPassThreads) k_warp_fp64(KArgs a, int epi
   WarpStage64<KIND> &sm = stage_all[w];
   const uint32_t lt_mask = (1u << lane) - 1u;
   const int stride = gridDim.x * kWarpPassWarps;
-  for (int c = a.ncell_tile + blockIdx.x * kWarpPassWarps + w; c < a.ncell_total; c += stride) {
+  for (int c = a.ncell_tile + blockIdx.x * kWarpPassWarps + w; c < a.va_c0; c += stride) {
     const int cb = a.cell_start[c], ce = a.cell_start[c + 1];
     if (cb == ce) continue;
     const SysDesc &sd = a.sys[a.sys_of_c[c]];

@@ -20,8 +20,23 @@ def init_state(n, L, seed):
 
 
 def golden_cases():
+    """The ChimeraSystem fixtures (vector and shared-window classes)."""
     return sorted(os.path.splitext(os.path.basename(p))[0]
-                  for p in glob.glob(os.path.join(GOLDEN, "*.npz")))
+                  for p in glob.glob(os.path.join(GOLDEN, "*.npz"))
+                  if not os.path.basename(p).startswith("va_"))
+
+
+def va_golden_cases():
+    """The VortexArraysSystemPtr fixtures."""
+    return sorted(os.path.splitext(os.path.basename(p))[0]
+                  for p in glob.glob(os.path.join(GOLDEN, "va_*.npz")))
+
+
+VA_KEYS = ("velocity", "mu_plus", "mu_minus", "xi_a", "xi_r", "D_phi", "kappa", "rho")
+
+
+def va_params(g):
+    return {k: float(g[k]) for k in VA_KEYS}
 
 
 def load_golden(name):

@@ -6,7 +6,7 @@ inputs with injected normals, and stores inputs and outputs as .npz.  The
 fixtures pin the C restatement (tests/test_oracle.py) and the GPU path
 (tests/test_gpu_parity.py) without the reference being present.
 
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py [case ...]
 """
 from __future__ import annotations
 
@@ -87,9 +87,58 @@ def make_case(name, n, L, prm, family, stepper, nsteps, seed, dt=0.01):
     return traj.shape
 
 
+# VortexArraysSystemPtr: the reference's vortex-array configuration
+# (SimulationEnginePtr.cpp:131-139) in a unit box: velocity 0.1, mu+- 100,
+# xi_a 0.04, xi_r 0.02, D 0.01, kappa 20, rho 0.2
+VA_PRM = dict(velocity=0.1, mu_plus=100.0, mu_minus=100.0, xi_a=0.04, xi_r=0.02, D_phi=0.01,
+              kappa=20.0, rho=0.2)
+# name: (n, L, stepper, nsteps, seed)
+VA_CASES = {
+    "va_srk_n1024": (1024, 1.0, pyref.STEP_SRK, 30, 7),
+    "va_rk4_n512": (512, 1.0, pyref.STEP_RK4, 20, 8),
+    "va_eulerptr_n512": (512, 1.0, pyref.STEP_EULER, 20, 9),
+    "va_allpairs_srk_n150": (150, 0.6, pyref.STEP_SRK, 20, 10),  # rho > L/4
+}
+
+
+def make_va_case(name, n, L, stepper, nsteps, seed, dt=0.01):
+    rng = np.random.default_rng(2000 + seed)
+    state0 = init_state(n, L, seed)
+    m = {pyref.STEP_EULER: 1, pyref.STEP_SRK: 2, pyref.STEP_RK4: 0}[stepper]
+    noise = rng.standard_normal(nsteps * n * m)
+    # the SRK-Ptr constructor draws N frequencies first (unused by this model)
+    feed = np.concatenate([np.zeros(n), noise]) if stepper == pyref.STEP_SRK else noise
+    va = [VA_PRM[k] for k in ("mu_plus", "mu_minus", "xi_a", "xi_r", "kappa")]
+    common = dict(family=pyref.FAMILY_VA, v0=VA_PRM["velocity"], rho=VA_PRM["rho"],
+                  D_phi=VA_PRM["D_phi"], dt=dt, va=va)
+    traj = pyref.run_reference(n, L, mode=pyref.MODE_RUN, stepper=stepper, nsteps=nsteps,
+                               record_every=10, state=state0,
+                               noise=feed if feed.size else None, **common)
+    traj = traj.reshape(-1, 3 * n)
+    k_prev = rng.normal(0.0, 0.05, 3 * n)
+    k_next_init = rng.normal(0.0, 1.0, 3 * n)
+    rhs_rk = pyref.run_reference(n, L, mode=pyref.MODE_RHS_RK, k_coef=0.5, state=state0,
+                                 k_prev=k_prev, k_next_init=k_next_init, **common)
+    srk = pyref.run_reference(n, L, mode=pyref.MODE_RHS_SRK, state=state0, **common)
+    out = dict(n=n, L=L, dt=dt, family=pyref.FAMILY_VA, stepper=stepper, nsteps=nsteps,
+               record_every=10, state0=state0, noise=noise, trajectory=traj, k_prev=k_prev,
+               k_next_init=k_next_init, k_coef=0.5, rhs_rk=rhs_rk, srk_derivative=srk[:3 * n],
+               srk_additional=srk[3 * n:], **VA_PRM)
+    np.savez_compressed(os.path.join(HERE, name + ".npz"), **out)
+    return traj.shape
+
+
 def main():
+    which = sys.argv[1:]
     for name, (n, L, prm, family, stepper, nsteps, seed) in CASES.items():
+        if which and name not in which:
+            continue
         shape = make_case(name, n, L, prm, family, stepper, nsteps, seed)
+        print(name, shape)
+    for name, (n, L, stepper, nsteps, seed) in VA_CASES.items():
+        if which and name not in which:
+            continue
+        shape = make_va_case(name, n, L, stepper, nsteps, seed)
         print(name, shape)
 
 
