@@ -389,6 +389,62 @@ def run_large(precision, steps):
                          "candidates_ms_per_step": dict(zip(names, ms)), "tuning_s": tune_s}}
 
 
+VA = dict(name="vortex_arrays_srk_n51200_L8", n=51200, L=8.0, velocity=0.1, mu_plus=100.0,
+          mu_minus=100.0, xi_a=0.04, xi_r=0.02, D_phi=0.01, kappa=20.0, rho=0.2, dt=0.01, seed=3)
+
+
+def va_inputs(w):
+    rng = np.random.default_rng(w["seed"])
+    n, L = w["n"], w["L"]
+    st = np.empty(3 * n)
+    st[0::3] = rng.uniform(0.0, L, n)
+    st[1::3] = rng.uniform(0.0, L, n)
+    st[2::3] = rng.uniform(-np.pi, np.pi, n)
+    return st
+
+
+def run_va(steps, cpu=True):
+    """The vortex-arrays model (VortexArraysSystemPtr) with the reference's
+    vortex-array parameters (SimulationEnginePtr.cpp:131-139, box side 1 ->
+    velocity 0.1, mu+- 100, xi_a 0.04, xi_r 0.02, D 0.01, kappa 20, rho 0.2) at
+    density 800 (N = 51,200 in L = 8), SRK-Ptr stepper, plain FP64: graph
+    replays of `steps` steps timed with CUDA events; the oracle port on one host
+    core for 2 steps beside it."""
+    import torch
+    from spc2_langevin_integration_gb300 import abi
+    w = VA
+    st = va_inputs(w)
+    prm = {k: w[k] for k in ("velocity", "mu_plus", "mu_minus", "xi_a", "xi_r", "D_phi", "kappa",
+                             "rho")}
+    out = {}
+    with abi.System(w["n"], abi.make_va_params(L=w["L"], stepper=abi.STEPPER_SRK, seed=w["seed"],
+                                               **prm)) as s:
+        s.upload_state(st)
+        stream = torch.cuda.ExternalStream(s.stream)
+        s.step(w["dt"], steps, graph=True)  # capture + warm
+        s.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        s.step(w["dt"], steps, graph=True)
+        e1.record(stream)
+        s.synchronize()
+        ms = e0.elapsed_time(e1)
+        out = {"value": w["n"] * steps / (ms / 1e3), "unit": "particle-steps/s", "steps": steps,
+               "ms_per_step": ms / steps, "profile_ms": s.profile_steps(w["dt"], 3),
+               "gpu_launches_per_replay": s.graph_nodes()}
+    if cpu:
+        from oracle import pyoracle as po
+        o = po.OracleVortexArrays(w["n"], w["L"], **prm)
+        st2 = st.copy()
+        noise = np.random.default_rng(7).standard_normal(2 * w["n"] * 2)
+        t0 = time.perf_counter()
+        o.run(po.SRK, st2, 0.0, w["dt"], 2, noise)
+        dt_cpu = time.perf_counter() - t0
+        out["cpu_baseline"] = {"value": w["n"] * 2 / dt_cpu, "unit": "particle-steps/s", "cores": 1,
+                               "kind": "port", "sample": f"N={w['n']}, 2 SRK steps, 1 thread"}
+    return out
+
+
 def dist_setup(args):
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -505,7 +561,9 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--ncu-case", choices=["fp32c", "fp64", "ensemble_fp32c", "ensemble_fp64"],
+    ap.add_argument("--drift-series", default=None,
+                    help="--workload drift: also write the sampled series to this JSON file")
+    ap.add_argument("--ncu-case", choices=["fp32c", "fp64", "ensemble_fp32c", "ensemble_fp64", "va"],
                     default=None,
                     help="run a few plain (ungraphed) steps of the workload (or of an ensemble of "
                          "--ensemble-systems systems) for an ncu capture")
@@ -520,11 +578,12 @@ def main():
     ap.add_argument("--skin", type=float, default=None)
     ap.add_argument("--cell-list", action="store_true",
                     help="--ncu-case fp32c/fp64: the cell-list passes instead of the Verlet rows")
-    ap.add_argument("--workload", choices=["vortex", "ensemble", "serve", "drift", "large"],
+    ap.add_argument("--workload", choices=["vortex", "ensemble", "serve", "drift", "large", "va"],
                     default="vortex",
                     help="vortex: the headline single-system line; ensemble: 512 systems in one "
                          "batch; serve: the Poisson request stream; drift: FP32C vs FP64 order "
-                         "parameters over 10^4 steps; large: Chimera RK4, N=2^22, L=64")
+                         "parameters over 10^4 steps; large: Chimera RK4, N=2^22, L=64; va: the "
+                         "vortex-arrays model, N=51,200, L=8")
     ap.add_argument("--sparse-below", type=float, default=None,
                     help="ensemble: neighbour-kernel tuning (mean particles per cell below "
                          "which a system runs the warp-per-cell passes)")
@@ -574,6 +633,10 @@ def main():
         if dist is not None:
             dist.destroy_process_group()
         return
+    if args.workload == "va":
+        print(json.dumps({"metric": "particle-steps/s", "workload": VA["name"], "config": VA,
+                          "dtype": "f64", "fp64": run_va(100, cpu=not args.no_cpu_baseline)}))
+        return
     if args.workload == "large":
         from spc2_langevin_integration_gb300 import abi
         out = {"metric": "particle-steps/s", "workload": LARGE["name"], "config": LARGE,
@@ -586,9 +649,7 @@ def main():
         return
     if args.workload == "drift":
         out = {"metric": "order-parameter drift, FP32C vs FP64", "workload": "drift"}
-        out.update(run_drift(steps=args.drift_steps,
-                             out_path=os.path.join(ROOT, "gpurun_out", "drift_series.json")
-                             if os.path.isdir(os.path.join(ROOT, "gpurun_out")) else None))
+        out.update(run_drift(steps=args.drift_steps, out_path=args.drift_series))
         print(json.dumps(out))
         return
     if args.workload == "serve":
@@ -597,6 +658,17 @@ def main():
         for name, prec in (("fp32c", abi.PRECISION_FP32C), ("fp64", abi.PRECISION_FP64)):
             out[name] = run_serving(prec, args.serve_duration, args.serve_rate)
         print(json.dumps(out))
+        return
+    if args.ncu_case == "va":
+        from spc2_langevin_integration_gb300 import abi
+        w = VA
+        prm = {k: w[k] for k in ("velocity", "mu_plus", "mu_minus", "xi_a", "xi_r", "D_phi",
+                                 "kappa", "rho")}
+        with abi.System(w["n"], abi.make_va_params(L=w["L"], stepper=abi.STEPPER_SRK,
+                                                   seed=w["seed"], **prm)) as s:
+            s.upload_state(va_inputs(w))
+            s.step(w["dt"], 3)
+            s.synchronize()
         return
     if args.ncu_case and args.ncu_case.startswith("ensemble"):
         from spc2_langevin_integration_gb300 import abi

@@ -4,14 +4,19 @@
 // caller gets the reference's trajectory from the GPU path.
 //
 // usage: SPC_REF_N=<N> SPC_REF_L=<L> spc_dropin_driver <input.bin> <output.bin>
-// (mode 0 = run, family 0 = vector classes, family 1 + SRK = vortex with the
-//  first N injected values as frequencies; modes 1/2 = one EvaluateRhs.)
+// (mode 0 = run the engine loop, modes 1/2 = one EvaluateRhs of either form;
+//  family 0 = vector classes, family 1 = shared-window classes, whose SRK
+//  stepper takes the first N injected values as its natural frequencies,
+//  family 2 = VortexArraysSystemPtr with the shared-window steppers, whose
+//  five extra parameters follow the noise block and whose SRK stepper skips
+//  the first N injected values, the frequencies it draws and never uses.)
 // With SPC_OUTPUT_DIR set, a run also writes the reference's observer files
 // there (a frame and a summary line after every step, as the engine loop does).
 #include <cstdint>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <stdexcept>
 #include <vector>
 
 #include "spc_dropin.hpp"
@@ -56,12 +61,14 @@ int main(int argc, char **argv) {
   read_exact(in, &n_noise, 8);
   std::vector<Real> noise((size_t)n_noise);
   if (n_noise) read_exact(in, noise.data(), (size_t)n_noise * 8);
+  double va[5] = {0, 0, 0, 0, 0};  // mu_plus, mu_minus, xi_a, xi_r, kappa
+  if (h.family == 2) read_exact(in, va, sizeof(va));
   std::fclose(in);
   FILE *out = std::fopen(argv[2], "wb");
   if (!out) return 2;
   auto dump = [&](const Real *p, size_t n) { std::fwrite(p, 8, n, out); };
   try {
-    Thread thread(argc, argv);
+    ThreadSharedMemory thread(argc, argv);  // a Thread for the vector classes
     PeriodicBoundaryConditions pbc_config(&thread, kL, kL);
     BinaryObserver *observer = nullptr;
     if (std::getenv("SPC_OUTPUT_DIR") && h.mode == 0)
@@ -72,21 +79,53 @@ int main(int argc, char **argv) {
       observer->SaveSystemState(s, t);
       observer->SaveSummaryStatistics(s, t);
     };
-    if (h.family == 1 && h.stepper == 1 && h.mode == 0) {
-      std::vector<Real> omega(noise.begin(), noise.begin() + kN);
-      std::vector<Real> rest(noise.begin() + kN, noise.end());
-      VortexArraysSystem system(&thread, h.v0, h.sigma, h.rho, h.D_phi, h.rho_0, pbc_config, omega);
-      system.InjectNoise(rest);
-      StochasticRungeKuttaStepper stepper(&thread);
+    // the shared-window engine loop (SimulationEnginePtr.cpp:106-115)
+    auto run_ptr = [&](auto &system) {
+      if (h.mode == 1) {
+        system.EvaluateRhs(state.data(), k_prev, k_next, h.k_coef, h.dt);
+        dump(k_next.data(), n3);
+        return;
+      }
+      if (h.mode == 2) {
+        std::vector<Real> derivative(n3, 0.0);
+        std::vector<std::vector<Real>> additional(kN, std::vector<Real>(2, 0.0));
+        system.EvaluateRhs(state.data(), derivative, additional, h.dt);
+        dump(derivative.data(), n3);
+        for (int i = 0; i < kN; ++i) dump(additional[i].data(), 2);
+        return;
+      }
+      StochasticEulerStepperPtr euler(&thread);
+      StochasticRungeKuttaStepperPtr srk(&thread);
+      RungeKutta4StepperPtr rk4(&thread);
+      std::vector<Real> rest = noise;
+      if (h.stepper == 1) {
+        if ((int)noise.size() < kN) throw std::runtime_error("spc: SRK needs N frequencies first");
+        if (h.family == 1) srk.SetFrequencies(std::vector<Real>(noise.begin(), noise.begin() + kN));
+        rest.assign(noise.begin() + kN, noise.end());
+      }
+      if (!rest.empty()) system.InjectNoise(rest);
       Real t = h.t0;
       for (int k = 1; k <= h.nsteps; ++k) {
         t += h.dt;
-        stepper.DoStep(system, state, t, h.dt);
+        if (h.stepper == 0)
+          euler.DoStep(system, state.data(), t, h.dt);
+        else if (h.stepper == 1)
+          srk.DoStep(system, state.data(), t, h.dt);
+        else
+          rk4.DoStep(system, state.data(), t, h.dt);
         pbc_config.ApplyPeriodicBoundaryConditions(state);
-        thread.SynchronizeVector(state);
+        thread.SynchronizeVectorThroughoutClusters(state.data());
         observe(state, t);
         if ((h.record_every > 0 && k % h.record_every == 0) || k == h.nsteps) dump(state.data(), n3);
       }
+    };
+    if (h.family == 1) {
+      ChimeraSystemPtr system(&thread, h.v0, h.sigma, h.rho, h.alpha,
+                              h.D_phi, h.rho_0, pbc_config);
+      run_ptr(system);
+    } else if (h.family == 2) {
+      VortexArraysSystemPtr system(&thread, h.v0, va[0], va[1], va[2], va[3], h.D_phi, va[4], h.rho, pbc_config);
+      run_ptr(system);
     } else if (h.family == 0) {
       ChimeraSystem chimera_system(&thread, h.v0, h.sigma, h.rho, h.alpha, h.D_phi, h.rho_0, pbc_config);
       if (h.mode == 1) {

@@ -1,6 +1,7 @@
 // Drop-in classes (spc_dropin.hpp) forwarding to the C-ABI.
 #include "spc_dropin.hpp"
 
+#include <algorithm>
 #include <cmath>
 #include <numeric>
 
@@ -59,7 +60,7 @@ void SpcSystemBase::Check(int rc, spc_handle *h) const {
 spc_handle *SpcSystemBase::Handle(int stepper) {
   if (!handles_[stepper]) {
     spc_params p{};
-    p.model = model_;
+    p.model = ModelFor(stepper);
     p.stepper = stepper;
     p.neighbour = neighbour_;
     p.precision = precision_;
@@ -72,12 +73,59 @@ spc_handle *SpcSystemBase::Handle(int stepper) {
     p.rho_0 = rho_0_;
     p.skin = skin_;
     p.seed = seed_;
+    p.mu_plus = mu_plus_;
+    p.mu_minus = mu_minus_;
+    p.xi_a = xi_a_;
+    p.xi_r = xi_r_;
+    p.kappa = kappa_;
     spc_handle *h = nullptr;
     Check(spc_create(&p, kN, &h), nullptr);
     handles_[stepper] = h;
-    if (model_ == SPC_MODEL_VORTEX) Check(spc_upload_omega(h, frequencies_.data()), h);
+    if (p.model == SPC_MODEL_VORTEX) {
+      if ((int)frequencies_.size() != kN) frequencies_.assign((size_t)kN, 0.0);
+      Check(spc_upload_omega(h, frequencies_.data()), h);
+    }
+  } else if (frequencies_dirty_ && ModelFor(stepper) == SPC_MODEL_VORTEX) {
+    Check(spc_upload_omega(handles_[stepper], frequencies_.data()), handles_[stepper]);
   }
+  if (ModelFor(stepper) == SPC_MODEL_VORTEX) frequencies_dirty_ = false;
   return handles_[stepper];
+}
+
+void SpcSystemBase::UseFrequencies(const std::vector<Real> &frequencies) {
+  if ((int)frequencies.size() != kN) throw std::runtime_error("spc: need N frequencies");
+  if (frequencies != frequencies_) {
+    frequencies_ = frequencies;
+    frequencies_dirty_ = true;
+  }
+}
+
+void SpcSystemBase::AdvanceRaw(int stepper, Real *const state, Real &t, Real dt, int nsteps) {
+  std::vector<Real> v(state, state + (size_t)kS * kN);
+  Advance(stepper, v, t, dt, nsteps);
+  std::copy(v.begin(), v.end(), state);
+}
+
+void SpcSystemBase::RhsRk(const Real *state, const Real *k_prev, Real *k_next, Real k_coef, Real dt) {
+  spc_handle *h = Handle(SPC_STEPPER_RK4);
+  Sync(h, std::vector<Real>(state, state + (size_t)kS * kN));
+  Check(spc_rhs_rk(h, k_prev, k_coef, dt, k_next), h);
+}
+
+void SpcSystemBase::RhsSrk(const Real *state, Real *derivative,
+                           std::vector<std::vector<Real>> &additional_derivative) {
+  spc_handle *h = Handle(SPC_STEPPER_RK4);
+  Sync(h, std::vector<Real>(state, state + (size_t)kS * kN));
+  std::vector<Real> d(kS * (size_t)kN), a(2 * (size_t)kN);
+  Check(spc_rhs_srk(h, d.data(), a.data()), h);
+  // the steppers pass zero-filled buffers (StochasticRungeKuttaStepper.hpp:36-39)
+  for (int i = 0; i < kN; ++i) {
+    derivative[kS * i] = d[kS * i];
+    derivative[kS * i + 1] = d[kS * i + 1];
+    derivative[kS * i + 2] += d[kS * i + 2];
+    additional_derivative[i][0] += a[2 * i];
+    additional_derivative[i][1] += a[2 * i + 1];
+  }
 }
 
 void SpcSystemBase::Sync(spc_handle *h, const std::vector<Real> &state) {
@@ -113,26 +161,13 @@ ChimeraSystem::ChimeraSystem(Thread *thread, Real v_0, Real sigma, Real rho, Rea
 
 void ChimeraSystem::EvaluateRhs(std::vector<Real> &system_state, const std::vector<Real> &k_prev,
                                 std::vector<Real> &k_next, Real k_coef, Real dt) {
-  spc_handle *h = Handle(SPC_STEPPER_RK4);
-  Sync(h, system_state);
-  Check(spc_rhs_rk(h, k_prev.data(), k_coef, dt, k_next.data()), h);
+  RhsRk(system_state.data(), k_prev.data(), k_next.data(), k_coef, dt);
 }
 
 void ChimeraSystem::EvaluateRhs(std::vector<Real> &system_state, std::vector<Real> &derivative,
                                 std::vector<std::vector<Real>> &additional_derivative, Real dt) {
   (void)dt;
-  spc_handle *h = Handle(SPC_STEPPER_RK4);
-  Sync(h, system_state);
-  std::vector<Real> d(kS * (size_t)kN), a(2 * (size_t)kN);
-  Check(spc_rhs_srk(h, d.data(), a.data()), h);
-  // the steppers pass zero-filled buffers (StochasticRungeKuttaStepper.hpp:36-39)
-  for (int i = 0; i < kN; ++i) {
-    derivative[kS * i] = d[kS * i];
-    derivative[kS * i + 1] = d[kS * i + 1];
-    derivative[kS * i + 2] += d[kS * i + 2];
-    additional_derivative[i][0] += a[2 * i];
-    additional_derivative[i][1] += a[2 * i + 1];
-  }
+  RhsSrk(system_state.data(), derivative.data(), additional_derivative);
 }
 
 void ChimeraSystem::AddNoise(const std::vector<Real> &, std::vector<Real> &derivative, Real) {
@@ -171,4 +206,75 @@ void StochasticRungeKuttaStepper::DoStep(VortexArraysSystem &system,
 void RungeKutta4Stepper::DoStep(ChimeraSystem &chimera_system, std::vector<Real> &system_state,
                                 Real t, Real dt) {
   chimera_system.Advance(SPC_STEPPER_RK4, system_state, t, dt, 1);
+}
+
+// ---------------------------------------------------------------------------
+// shared-window classes
+ChimeraSystemPtr::ChimeraSystemPtr(ThreadSharedMemory *thread, Real v_0, Real sigma, Real rho, Real alpha,
+                                   Real D_phi, Real rho_0, PeriodicBoundaryConditions &pbc_config)
+    : SpcSystemBase(thread, SPC_MODEL_CHIMERA, v_0, sigma, rho, alpha, D_phi, rho_0, pbc_config) {}
+
+void ChimeraSystemPtr::EvaluateRhs(const Real *const system_state, const std::vector<Real> &k_prev,
+                                   std::vector<Real> &k_next, Real k_coef, Real dt) {
+  RhsRk(system_state, k_prev.data(), k_next.data(), k_coef, dt);
+}
+
+void ChimeraSystemPtr::EvaluateRhs(const Real *const system_state, std::vector<Real> &derivative,
+                                   std::vector<std::vector<Real>> &additional_derivative, Real) {
+  RhsSrk(system_state, derivative.data(), additional_derivative);
+}
+
+VortexArraysSystemPtr::VortexArraysSystemPtr(ThreadSharedMemory *thread, Real velocity, Real mu_plus,
+                                             Real mu_minus, Real xi_a, Real xi_r, Real D_phi, Real kappa,
+                                             Real rho, PeriodicBoundaryConditions &pbc_config)
+    : SpcSystemBase(thread, SPC_MODEL_VORTEX_ARRAYS, velocity, 0.0, rho, 0.0, D_phi, 1.0, pbc_config) {
+  mu_plus_ = mu_plus;
+  mu_minus_ = mu_minus;
+  xi_a_ = xi_a;
+  xi_r_ = xi_r;
+  kappa_ = kappa;
+}
+
+void VortexArraysSystemPtr::EvaluateRhs(const Real *const system_state, const std::vector<Real> &k_prev,
+                                        std::vector<Real> &k_next, Real k_coef, Real dt) {
+  RhsRk(system_state, k_prev.data(), k_next.data(), k_coef, dt);
+}
+
+void VortexArraysSystemPtr::EvaluateRhs(const Real *const system_state, std::vector<Real> &derivative,
+                                        std::vector<std::vector<Real>> &additional_derivative, Real) {
+  RhsSrk(system_state, derivative.data(), additional_derivative);
+}
+
+void StochasticEulerStepperPtr::DoStep(ChimeraSystemPtr &system, Real *const system_state, Real t, Real dt) {
+  system.AdvanceRaw(SPC_STEPPER_EULER_PTR, system_state, t, dt, 1);
+}
+
+void StochasticEulerStepperPtr::DoStep(VortexArraysSystemPtr &system, Real *const system_state, Real t,
+                                       Real dt) {
+  system.AdvanceRaw(SPC_STEPPER_EULER_PTR, system_state, t, dt, 1);
+}
+
+void StochasticRungeKuttaStepperPtr::SetFrequencies(const std::vector<Real> &frequencies) {
+  if ((int)frequencies.size() != kN) throw std::runtime_error("spc: need N frequencies");
+  frequencies_ = frequencies;
+}
+
+void StochasticRungeKuttaStepperPtr::DoStep(ChimeraSystemPtr &system, Real *const system_state, Real t,
+                                            Real dt) {
+  system.UseFrequencies(frequencies_);
+  system.AdvanceRaw(SPC_STEPPER_SRK, system_state, t, dt, 1);
+}
+
+void StochasticRungeKuttaStepperPtr::DoStep(VortexArraysSystemPtr &system, Real *const system_state, Real t,
+                                            Real dt) {
+  system.AdvanceRaw(SPC_STEPPER_SRK, system_state, t, dt, 1);
+}
+
+void RungeKutta4StepperPtr::DoStep(ChimeraSystemPtr &system, Real *const system_state, Real t, Real dt) {
+  system.AdvanceRaw(SPC_STEPPER_RK4, system_state, t, dt, 1);
+}
+
+void RungeKutta4StepperPtr::DoStep(VortexArraysSystemPtr &system, Real *const system_state, Real t,
+                                   Real dt) {
+  system.AdvanceRaw(SPC_STEPPER_RK4, system_state, t, dt, 1);
 }

@@ -73,7 +73,23 @@ class PeriodicBoundaryConditions {
   Real x_size_, y_size_, x_rsize_, y_rsize_;
 };
 
-// Shared machinery of the two systems: one library handle per stepper kind,
+// Parallelization/ThreadSharedMemory.hpp:14-60: one rank on one shared-memory
+// node; the shared windows of the reference live on the device here.
+class ThreadSharedMemory : public Thread {
+ public:
+  ThreadSharedMemory(int argc, char **argv) : Thread(argc, argv) {}
+  int GetRootRank() { return 0; }
+  int GetSharedRootRank() { return 0; }
+  bool IsSharedRoot() { return true; }
+  using Thread::BroadcastVector;
+  using Thread::SynchronizeVector;
+  void SynchronizeVector(Real *const, long) {}
+  void SynchronizeVectorThroughoutClusters(Real *const) {}
+  void SynchronizeVectorThroughoutClusters(int *const) {}
+  void BroadcastVector(Real *const, long) {}
+};
+
+// Shared machinery of the systems: one library handle per stepper kind,
 // created on first use, plus the host/device coherence of the state vector.
 class SpcSystemBase {
  public:
@@ -95,11 +111,20 @@ class SpcSystemBase {
   void InjectNoise(const std::vector<Real> &normals) { injected_ = normals; inject_pending_ = true; }
   // nsteps steps of stepper kind `stepper` with one upload and one download.
   void Advance(int stepper, std::vector<Real> &state, Real &t, Real dt, int nsteps);
+  // the same on a raw 3N state (the shared-window classes' Real * state)
+  void AdvanceRaw(int stepper, Real *const state, Real &t, Real dt, int nsteps);
+  // natural frequencies for the stochastic Runge-Kutta handle (re-uploaded
+  // when they change)
+  void UseFrequencies(const std::vector<Real> &frequencies);
   spc_handle *Handle(int stepper);
 
  protected:
+  // the library model of the handle for stepper kind `stepper`
+  virtual int ModelFor(int stepper) const { (void)stepper; return model_; }
   void Sync(spc_handle *h, const std::vector<Real> &state);
   void Check(int rc, spc_handle *h) const;
+  void RhsRk(const Real *state, const Real *k_prev, Real *k_next, Real k_coef, Real dt);
+  void RhsSrk(const Real *state, Real *derivative, std::vector<std::vector<Real>> &additional);
 
   Thread *thread_;
   PeriodicBoundaryConditions &pbc_config_;
@@ -110,6 +135,8 @@ class SpcSystemBase {
   Real skin_ = 0.05;
   uint64_t seed_ = 0;
   std::vector<Real> frequencies_;
+  bool frequencies_dirty_ = false;
+  Real mu_plus_ = 0.0, mu_minus_ = 0.0, xi_a_ = 0.0, xi_r_ = 0.0, kappa_ = 0.0;  // vortex arrays
   spc_handle *handles_[4] = {nullptr, nullptr, nullptr, nullptr};
   std::vector<Real> shadow_[4];  // what each handle's device state holds
   std::vector<Real> injected_;
@@ -139,6 +166,39 @@ class VortexArraysSystem : public SpcSystemBase {
  public:
   VortexArraysSystem(Thread *thread, Real v_0, Real sigma, Real rho, Real D_phi, Real rho_0,
                      PeriodicBoundaryConditions &pbc_config, const std::vector<Real> &frequencies);
+};
+
+// DynamicalSystems/ChimeraSystemPtr.hpp:12-80: the alignment system of the
+// shared-window classes.  With the stochastic Runge-Kutta stepper it takes the
+// stepper's natural frequencies into the phase drift
+// (StochasticRungeKuttaStepperPtr.hpp:65).
+class ChimeraSystemPtr : public SpcSystemBase {
+ public:
+  ChimeraSystemPtr(ThreadSharedMemory *thread, Real v_0, Real sigma, Real rho, Real alpha, Real D_phi,
+                   Real rho_0, PeriodicBoundaryConditions &pbc_config);
+  void EvaluateRhs(const Real *const system_state, const std::vector<Real> &k_prev,
+                   std::vector<Real> &k_next, Real k_coef, Real dt);
+  void EvaluateRhs(const Real *const system_state, std::vector<Real> &derivative,
+                   std::vector<std::vector<Real>> &additional_derivative, Real dt);
+  bool last_coefficient_ = false;
+
+ protected:
+  int ModelFor(int stepper) const override {
+    return stepper == SPC_STEPPER_SRK ? SPC_MODEL_VORTEX : SPC_MODEL_CHIMERA;
+  }
+};
+
+// DynamicalSystems/VortexArraysSystemPtr.hpp:14-95: the vortex-arrays model.
+class VortexArraysSystemPtr : public SpcSystemBase {
+ public:
+  VortexArraysSystemPtr(ThreadSharedMemory *thread, Real velocity, Real mu_plus, Real mu_minus,
+                        Real xi_a, Real xi_r, Real D_phi, Real kappa, Real rho,
+                        PeriodicBoundaryConditions &pbc_config);
+  void EvaluateRhs(const Real *const system_state, const std::vector<Real> &k_prev,
+                   std::vector<Real> &k_next, Real k_coef, Real dt);
+  void EvaluateRhs(const Real *const system_state, std::vector<Real> &derivative,
+                   std::vector<std::vector<Real>> &additional_derivative, Real dt);
+  bool last_coefficient_ = false;
 };
 
 // Steppers/StochasticEulerStepper.hpp:15-47
@@ -171,4 +231,42 @@ class RungeKutta4Stepper {
 
  private:
   Thread *thread_;
+};
+
+// Steppers/StochasticEulerStepperPtr.hpp:14-80
+class StochasticEulerStepperPtr {
+ public:
+  explicit StochasticEulerStepperPtr(ThreadSharedMemory *thread) : thread_(thread) {}
+  void DoStep(ChimeraSystemPtr &system, Real *const system_state, Real t, Real dt);
+  void DoStep(VortexArraysSystemPtr &system, Real *const system_state, Real t, Real dt);
+
+ private:
+  ThreadSharedMemory *thread_;
+};
+
+// Steppers/StochasticRungeKuttaStepperPtr.hpp:21-100.  The reference's
+// constructor draws the natural frequencies from N(0, 0), i.e. all zero
+// (:29-34); SetFrequencies (no reference counterpart) gives other ones.
+class StochasticRungeKuttaStepperPtr {
+ public:
+  explicit StochasticRungeKuttaStepperPtr(ThreadSharedMemory *thread)
+      : thread_(thread), frequencies_((size_t)kN, 0.0) {}
+  void SetFrequencies(const std::vector<Real> &frequencies);
+  void DoStep(ChimeraSystemPtr &system, Real *const system_state, Real t, Real dt);
+  void DoStep(VortexArraysSystemPtr &system, Real *const system_state, Real t, Real dt);
+
+ private:
+  ThreadSharedMemory *thread_;
+  std::vector<Real> frequencies_;
+};
+
+// Steppers/RungeKutta4StepperPtr.hpp:14-33 (k buffers persist on the device)
+class RungeKutta4StepperPtr {
+ public:
+  explicit RungeKutta4StepperPtr(ThreadSharedMemory *thread) : thread_(thread) {}
+  void DoStep(ChimeraSystemPtr &system, Real *const system_state, Real t, Real dt);
+  void DoStep(VortexArraysSystemPtr &system, Real *const system_state, Real t, Real dt);
+
+ private:
+  ThreadSharedMemory *thread_;
 };

@@ -1,9 +1,11 @@
 """The C++ drop-in (host/spc_dropin.hpp, host/spc_observer.hpp) as a
-reference-style program uses it: the engine loop of SimulationEngine.cpp:149-161
-written against the reference's class names (host/dropin_driver.cpp), fed the
-golden inputs, must reproduce the reference's golden trajectories and
-right-hand sides; with SPC_OUTPUT_DIR set, its observer files must be the
-bytes the reference's observer writes for those states."""
+reference-style program uses it: the engine loops of SimulationEngine.cpp:149-161
+and SimulationEnginePtr.cpp:106-115 written against the reference's class names
+(host/dropin_driver.cpp) for the vector classes, the shared-window classes and
+VortexArraysSystemPtr, fed the golden inputs, must reproduce the reference's
+golden trajectories and right-hand sides; with SPC_OUTPUT_DIR set, its
+observer files must be the bytes the reference's observer writes for those
+states."""
 import os
 
 import numpy as np
@@ -12,45 +14,54 @@ import pytest
 from oracle import pyref
 from spc2_langevin_integration_gb300 import observer as obs
 from spc2_langevin_integration_gb300.host import build_host
-from tests._helpers import golden_cases, load_golden, periodic_diff
+from tests._helpers import golden_cases, load_golden, periodic_diff, va_golden_cases, va_params
 
 pytestmark = pytest.mark.gpu
 
 TRAJ_TOL = 1e-9
 RHS_TOL = 1e-12
+VA_RHS_TOL = 1e-11  # of each array's largest magnitude, as for the vortex-arrays C-ABI tests
 
 
 def _run(g, mode, extra_env=None):
     n, L = int(g["n"]), float(g["L"])
-    kw = dict(mode=mode, family=int(g["family"]), stepper=int(g["stepper"]),
+    fam, stepper = int(g["family"]), int(g["stepper"])
+    kw = dict(mode=mode, family=fam, stepper=stepper,
               nsteps=int(g["nsteps"]), record_every=int(g["record_every"]),
-              v0=float(g["v0"]), sigma=float(g["sigma"]), rho=float(g["rho"]),
-              alpha=float(g["alpha"]), D_phi=float(g["D_phi"]), dt=float(g["dt"]),
+              D_phi=float(g["D_phi"]), rho=float(g["rho"]), dt=float(g["dt"]),
               k_coef=float(g["k_coef"]), state=g["state0"], k_prev=g["k_prev"],
               k_next_init=g["k_next_init"])
     noise = g["noise"]
-    if "omega" in g:
-        noise = np.concatenate([g["omega"], noise])
+    if fam == pyref.FAMILY_VA:
+        vp = va_params(g)
+        kw.update(v0=vp["velocity"], va=[vp[k] for k in ("mu_plus", "mu_minus", "xi_a", "xi_r", "kappa")])
+        if stepper == pyref.STEP_SRK:
+            noise = np.concatenate([np.zeros(n), noise])  # the unused frequency draw
+    else:
+        kw.update(v0=float(g["v0"]), sigma=float(g["sigma"]), alpha=float(g["alpha"]))
+        if "omega" in g:
+            noise = np.concatenate([g["omega"], noise])
+    if mode != 0:
+        noise = None  # one right-hand side draws no normals
     return pyref.run_reference(n, L, noise=noise, binary=build_host.build_driver(),
                                extra_env=extra_env, **kw)
 
 
-def _runnable(name):
-    g = load_golden(name)
-    # the driver runs the vector classes and the vortex SRK-Ptr form
-    return int(g["family"]) == 0 or (int(g["family"]) == 1 and int(g["stepper"]) == 1)
-
-
-@pytest.mark.parametrize("name", [c for c in golden_cases() if _runnable(c)])
-def test_dropin_engine_loop_matches_reference_golden(name, tmp_path):
+def _trajectory(name, extra_env=None):
     g = load_golden(name)
     n, L = int(g["n"]), float(g["L"])
-    out = _run(g, 0, extra_env={"SPC_OUTPUT_DIR": str(tmp_path)})
-    frames = out.reshape(-1, 3 * n)
+    frames = _run(g, 0, extra_env=extra_env).reshape(-1, 3 * n)
     ref = np.asarray(g["trajectory"])
     assert frames.shape == ref.shape
     for got, want in zip(frames, ref):
         assert np.abs(periodic_diff(got, want, L)).max() <= TRAJ_TOL
+    return g, frames
+
+
+@pytest.mark.parametrize("name", golden_cases())
+def test_dropin_engine_loop_matches_reference_golden(name, tmp_path):
+    g, frames = _trajectory(name, extra_env={"SPC_OUTPUT_DIR": str(tmp_path)})
+    n = int(g["n"])
     # observer files: one frame and one summary line after every step; the
     # recorded frames must be the float32 images of the driver's states
     bins = [f for f in os.listdir(tmp_path) if f.endswith(".bin")]
@@ -71,6 +82,33 @@ def test_dropin_engine_loop_matches_reference_golden(name, tmp_path):
             assert tf == float(np.float32(t))
             assert np.array_equal(fr, st.astype(np.float32))
             assert lines[k - 1] + "\n" == obs.summary_line(t, st)
+
+
+@pytest.mark.parametrize("name", va_golden_cases())
+def test_dropin_vortex_arrays_engine_loop_matches_reference_golden(name):
+    # VortexArraysSystemPtr driven by StochasticEulerStepperPtr,
+    # StochasticRungeKuttaStepperPtr and RungeKutta4StepperPtr
+    _trajectory(name)
+
+
+def _close(got, want, tol):
+    return np.abs(got - want).max() <= tol * max(np.abs(want).max(), 1.0)
+
+
+@pytest.mark.parametrize("name", [c for c in golden_cases() if load_golden(c)["family"] == 1]
+                         + va_golden_cases())
+def test_dropin_ptr_rhs_matches_reference_golden(name):
+    # both EvaluateRhs forms of ChimeraSystemPtr / VortexArraysSystemPtr on a
+    # raw state pointer
+    g = load_golden(name)
+    n = int(g["n"])
+    tol = VA_RHS_TOL if int(g["family"]) == pyref.FAMILY_VA else RHS_TOL * 10
+    assert _close(_run(g, 1), g["rhs_rk"], tol)
+    out = _run(g, 2)
+    d, a = out[:3 * n], out[3 * n:]
+    assert _close(d, g["srk_derivative"], tol)
+    assert _close(a[0::2], g["srk_additional"][0::2], tol)
+    assert _close(a[1::2], g["srk_additional"][1::2], tol)
 
 
 @pytest.mark.parametrize("name", [c for c in golden_cases() if load_golden(c)["family"] == 0])
