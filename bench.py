@@ -445,6 +445,69 @@ def run_va(steps, cpu=True):
     return out
 
 
+def run_observed(precision, nsteps=2000, every=10):
+    """The engine loop with an observer (a frame of the state every `every`
+    steps) on the headline workload, two ways, each from a resident state:
+      * per-step: one spc_step + state download per step, the host round trip
+        the unchanged DoStep API imposes on a reference-style loop;
+      * device loop: one spc_run call, chunks of steps as graph replays with
+        snapshots of the observed steps copied back while later steps run.
+    Both deliver the same frames (checked) to a consumer that reduces each to
+    its global order parameter on the host (numpy, ~1 ms per frame at this N);
+    device_loop_light hands the frames to a consumer that keeps only the step
+    index, which shows the loop's own cost.  particle-steps/s from wall time."""
+    from spc2_langevin_integration_gb300 import abi
+    w = WORKLOAD
+    st, omega = init_inputs(w)
+    prm = workload_params(abi, w, precision)
+    prm.neighbour = abi.NEIGHBOUR_CELL
+
+    def consume(state):
+        ph = state[2::3]
+        return complex(np.cos(ph).mean(), np.sin(ph).mean())
+
+    out = {}
+    frames = {}
+    pattern = [1] + [0] * (every - 1)
+    warm = 2 * every * max(1, 64 // every)  # two chunks of the device loop
+    for mode in ("per_step", "device_loop", "device_loop_light"):
+        with abi.System(w["n"], prm) as s:
+            s.upload_state(st)
+            s.upload_omega(omega)
+            if mode != "per_step":  # captures the chunk graphs outside the timed run
+                s.run(w["dt"], warm, every, pattern, lambda *a: False)
+            else:
+                s.step(w["dt"], warm)
+            s.synchronize()
+            got = []
+            t0 = time.perf_counter()
+            if mode == "per_step":
+                for k in range(1, nsteps + 1):
+                    s.step(w["dt"], 1)
+                    state = s.download_state()
+                    if k % every == 0:
+                        got.append(consume(state))
+            elif mode == "device_loop":
+                s.run(w["dt"], nsteps, every, pattern,
+                      lambda k, t, state: got.append(consume(state)) and False)
+                s.synchronize()
+            else:  # the loop's own cost: the consumer keeps only the step index
+                s.run(w["dt"], nsteps, every, pattern, lambda k, t, state: got.append(k) and False)
+                s.synchronize()
+            wall = time.perf_counter() - t0
+            frames[mode] = got
+            out[mode] = {"value": w["n"] * nsteps / wall, "unit": "particle-steps/s", "wall_s": wall,
+                         "frames": len(got)}
+            if mode != "per_step":
+                nodes, gsteps = s.run_graph_nodes()
+                out[mode]["graph"] = {"kernel_nodes": nodes, "steps": gsteps}
+    out["same_frames"] = frames["per_step"] == frames["device_loop"]
+    out["device_loop_over_per_step"] = out["device_loop"]["value"] / out["per_step"]["value"]
+    out["config"] = {"workload": w["name"], "steps": nsteps, "frame_every": every,
+                     "neighbour": "cell", "precision": "fp32c" if precision else "fp64"}
+    return out
+
+
 def dist_setup(args):
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -578,12 +641,14 @@ def main():
     ap.add_argument("--skin", type=float, default=None)
     ap.add_argument("--cell-list", action="store_true",
                     help="--ncu-case fp32c/fp64: the cell-list passes instead of the Verlet rows")
-    ap.add_argument("--workload", choices=["vortex", "ensemble", "serve", "drift", "large", "va"],
+    ap.add_argument("--workload",
+                    choices=["vortex", "ensemble", "serve", "drift", "large", "va", "observed"],
                     default="vortex",
                     help="vortex: the headline single-system line; ensemble: 512 systems in one "
                          "batch; serve: the Poisson request stream; drift: FP32C vs FP64 order "
                          "parameters over 10^4 steps; large: Chimera RK4, N=2^22, L=64; va: the "
-                         "vortex-arrays model, N=51,200, L=8")
+                         "vortex-arrays model, N=51,200, L=8; observed: the headline workload "
+                         "with a frame every 10 steps, per-step loop vs the device loop")
     ap.add_argument("--sparse-below", type=float, default=None,
                     help="ensemble: neighbour-kernel tuning (mean particles per cell below "
                          "which a system runs the warp-per-cell passes)")
@@ -650,6 +715,13 @@ def main():
     if args.workload == "drift":
         out = {"metric": "order-parameter drift, FP32C vs FP64", "workload": "drift"}
         out.update(run_drift(steps=args.drift_steps, out_path=args.drift_series))
+        print(json.dumps(out))
+        return
+    if args.workload == "observed":
+        from spc2_langevin_integration_gb300 import abi
+        out = {"metric": "particle-steps/s with an observer", "workload": "observed"}
+        out["fp32c"] = run_observed(abi.PRECISION_FP32C)
+        out["fp64"] = run_observed(abi.PRECISION_FP64, nsteps=100)
         print(json.dumps(out))
         return
     if args.workload == "serve":

@@ -127,6 +127,26 @@ int spc_step(spc_handle *h, double *t_inout, double dt, int32_t nsteps);
  * (fixed-length step loops; requires Philox noise). */
 int spc_step_graph(spc_handle *h, double *t_inout, double dt, int32_t nsteps);
 
+/* The engine loop with its observers, on the device
+ * (SimulationEngine.cpp:149-161, SimulationEnginePtr.cpp:106-115): nsteps
+ * steps from *t_inout, and after the k-th of them (k = 1..nsteps) a snapshot
+ * of the state when observe[k % period] is nonzero.  A snapshot holds 3N
+ * doubles (AoS), exactly what spc_download_state returns after that step.
+ * fn(user, k, t_k, state) is called for every snapshot in order of k, with t_k
+ * = *t_inout plus dt added k times (SimulationEngine.cpp:151), from the
+ * calling thread while the device runs later steps; the pointer is valid
+ * during the call only.  A nonzero return from fn stops the run: no later
+ * snapshot is delivered, the steps already enqueued (at most one chunk of
+ * about 64 steps) complete, and *steps_done (if not NULL) says how many steps
+ * the state advanced; *t_inout is the time after them.  Chunks run as CUDA
+ * graph replays under Philox noise and eagerly with injected noise; their
+ * snapshots reach the host in one copy per chunk on a second stream.  fn may
+ * be NULL (no snapshots; observe is then ignored).  fn must not call into
+ * this handle. */
+typedef int (*spc_observe_fn)(void *user, int64_t step, double t, const double *aos3n);
+int spc_run(spc_handle *h, double *t_inout, double dt, int64_t nsteps, int32_t period,
+            const uint8_t *observe, spc_observe_fn fn, void *user, int64_t *steps_done);
+
 /* Step counter used as the Philox counter (the number of steps taken). */
 int spc_get_step_counter(const spc_handle *h, uint64_t *out);
 int spc_set_step_counter(spc_handle *h, uint64_t step);
@@ -216,6 +236,8 @@ int spc_autotune(const spc_params *p, int32_t n, const double *aos3n, const doub
 /* Nodes (kernel launches) of the CUDA graph the last spc_step_graph call
  * captured or replayed: every replay launches exactly this many kernels. */
 int spc_graph_nodes(const spc_handle *h, int64_t *nodes);
+/* Nodes of spc_run's captured chunk graph (0 if none) and its steps. */
+int spc_run_graph_nodes(const spc_handle *h, int64_t *nodes, int32_t *steps);
 
 /* Synchronise the handle's stream; the stream itself (a cudaStream_t) for
  * callers that time or order work around the library. */

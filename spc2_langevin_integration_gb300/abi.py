@@ -134,10 +134,17 @@ def lib() -> C.CDLL:
                                C.c_int32, C.POINTER(Params), dp, dp, C.c_int32,
                                C.POINTER(C.c_int32)]
     L.spc_graph_nodes.argtypes = [H, C.POINTER(C.c_int64)]
+    L.spc_run.argtypes = [H, dp, C.c_double, C.c_int64, C.c_int32, C.c_void_p, OBSERVE_FN,
+                          C.c_void_p, C.POINTER(C.c_int64)]
+    L.spc_run_graph_nodes.argtypes = [H, C.POINTER(C.c_int64), C.POINTER(C.c_int32)]
     L.spc_alloc_pinned.argtypes = [C.c_size_t, C.POINTER(C.c_void_p)]
     L.spc_free_pinned.argtypes = [C.c_void_p]
     _lib = L
     return L
+
+
+# int (*)(void *user, int64_t step, double t, const double *aos3n)
+OBSERVE_FN = C.CFUNCTYPE(C.c_int, C.c_void_p, C.c_int64, C.c_double, C.POINTER(C.c_double))
 
 
 def _ptr(a: np.ndarray) -> C.c_void_p:
@@ -231,6 +238,44 @@ class System:
         self._check(f(self.h, C.byref(t), dt, int(nsteps)), self.h)
         self.t = t.value
         return self.t
+
+    def run(self, dt: float, nsteps: int, period: int = 1, observe=None, fn=None) -> int:
+        """The engine loop with its observers on the device (spc_run): after
+        step k (1-based) with observe[k % period] set, fn(k, t, state) gets a
+        copy of the AoS state; a true return from fn stops the run.  Returns
+        the number of steps taken."""
+        t = C.c_double(self.t)
+        done = C.c_int64()
+        obs = None
+        cb = OBSERVE_FN()
+        errors = []
+        if fn is not None:
+            mask = np.ones(period, np.uint8) if observe is None else np.asarray(observe, np.uint8)
+            if mask.size != period:
+                raise ValueError(f"observe needs {period} entries")
+            obs = np.ascontiguousarray(mask)
+            n3 = 3 * self.n
+
+            def tramp(_user, step, tt, state):
+                try:
+                    return 1 if fn(int(step), float(tt), np.ctypeslib.as_array(state, (n3,)).copy()) else 0
+                except BaseException as e:  # raised again after the C call returns
+                    errors.append(e)
+                    return 1
+            cb = OBSERVE_FN(tramp)
+        rc = self._L.spc_run(self.h, C.byref(t), float(dt), int(nsteps), int(period),
+                             _ptr(obs) if obs is not None else None, cb, None, C.byref(done))
+        self.t = t.value
+        if errors:
+            raise errors[0]
+        self._check(rc, self.h)
+        return done.value
+
+    def run_graph_nodes(self) -> tuple[int, int]:
+        """(kernel nodes, steps) of spc_run's captured chunk graph."""
+        v, st = C.c_int64(), C.c_int32()
+        self._check(self._L.spc_run_graph_nodes(self.h, C.byref(v), C.byref(st)), self.h)
+        return v.value, st.value
 
     @property
     def step_counter(self) -> int:

@@ -50,6 +50,108 @@ int check_ready(spc_handle *h) {
   return SPC_OK;
 }
 
+// ---------------------------------------------------------------------------
+// observed run loop (spc_run)
+
+// Ring buffers of `doubles` each (device + pinned host), the copy stream and
+// its events, created or grown on demand.
+int run_pipe_reserve(Engine *e, size_t doubles) {
+  Engine::RunPipe &r = e->run;
+  if (!r.copy) {
+    SPC_CUDA(e, cudaStreamCreateWithFlags(&r.copy, cudaStreamNonBlocking));
+    for (int b = 0; b < 2; ++b) {
+      SPC_CUDA(e, cudaEventCreateWithFlags(&r.computed[b], cudaEventDisableTiming));
+      SPC_CUDA(e, cudaEventCreateWithFlags(&r.copied[b], cudaEventDisableTiming));
+    }
+  }
+  doubles = std::max<size_t>(doubles, 1);
+  if (r.ring_doubles >= doubles) return SPC_OK;
+  SPC_CUDA(e, cudaStreamSynchronize(e->stream));
+  SPC_CUDA(e, cudaStreamSynchronize(r.copy));
+  drop_graph(e);  // the captured chunks write the old rings
+  for (int b = 0; b < 2; ++b) {
+    if (r.d_ring[b]) {
+      auto it = std::find(e->allocs.begin(), e->allocs.end(), (void *)r.d_ring[b]);
+      if (it != e->allocs.end()) e->allocs.erase(it);
+      cudaFree(r.d_ring[b]);
+      r.d_ring[b] = nullptr;
+    }
+    if (r.h_ring[b]) cudaFreeHost(r.h_ring[b]);
+    r.h_ring[b] = nullptr;
+  }
+  r.ring_doubles = 0;
+  for (int b = 0; b < 2; ++b) {
+    SPC_TRY(dalloc(e, &r.d_ring[b], doubles));
+    cudaError_t ce = cudaHostAlloc((void **)&r.h_ring[b], doubles * 8, cudaHostAllocDefault);
+    if (ce != cudaSuccess) {
+      r.h_ring[b] = nullptr;
+      return fail(e, SPC_ERR_NOMEM, "cudaHostAlloc(%zu bytes): %s", doubles * 8, cudaGetErrorString(ce));
+    }
+  }
+  r.ring_doubles = doubles;
+  return SPC_OK;
+}
+
+// Enqueue one chunk of len steps, with a snapshot into ring b after every
+// step whose pattern entry is set.
+int run_enqueue_chunk(spc_handle *h, double dt, int len, const uint8_t *pat, int b,
+                      const double *noise, long long per_step) {
+  Engine *e = &h->e;
+  const SysHost &sh = e->slots[h->slot];
+  const size_t snap = 3 * (size_t)h->n;
+  k_begin_call<<<blocks_for(e->nsys, 128), 128, 0, e->stream>>>(e->d_sys, e->nsys, len);
+  SPC_LAUNCHED(e);
+  int k = 0;
+  for (int s = 0; s < len; ++s) {
+    SPC_TRY(enqueue_step(e, dt, s, noise ? noise + (long long)s * per_step : nullptr));
+    if (pat[s]) {
+      k_soa_to_aos<<<blocks_for(h->n, 256), 256, 0, e->stream>>>(
+          e->a.x + sh.pool_p0, e->a.y + sh.pool_p0, e->a.phi + sh.pool_p0, h->n,
+          e->run.d_ring[b] + (size_t)k * snap);
+      SPC_LAUNCHED(e);
+      ++k;
+    }
+  }
+  k_end_call<<<blocks_for(e->nsys, 128), 128, 0, e->stream>>>(e->d_sys, e->nsys);
+  SPC_LAUNCHED(e);
+  return SPC_OK;
+}
+
+// Capture the two chunk graphs (one per ring) for chunks of G steps.
+int run_capture(spc_handle *h, double dt, int G, const std::vector<uint8_t> &pat) {
+  Engine *e = &h->e;
+  Engine::RunPipe &r = e->run;
+  if (r.graph[0] && r.graph[1] && r.steps == G && r.dt == dt && r.pattern == pat) return SPC_OK;
+  for (cudaGraphExec_t &g : r.graph)
+    if (g) {
+      cudaGraphExecDestroy(g);
+      g = nullptr;
+    }
+  for (int b = 0; b < 2; ++b) {
+    cudaGraph_t g = nullptr;
+    SPC_CUDA(e, cudaStreamBeginCapture(e->stream, cudaStreamCaptureModeThreadLocal));
+    int rc = run_enqueue_chunk(h, dt, G, pat.data(), b, nullptr, 0);
+    cudaError_t ce = cudaStreamEndCapture(e->stream, &g);
+    if (rc != SPC_OK) {
+      if (g) cudaGraphDestroy(g);
+      return rc;
+    }
+    if (ce != cudaSuccess) return fail(e, SPC_ERR_CUDA, "graph capture: %s", cudaGetErrorString(ce));
+    r.graph_nodes = 0;
+    cudaGraphGetNodes(g, nullptr, &r.graph_nodes);
+    ce = cudaGraphInstantiate(&r.graph[b], g, 0);
+    cudaGraphDestroy(g);
+    if (ce != cudaSuccess) {
+      r.graph[b] = nullptr;
+      return fail(e, SPC_ERR_CUDA, "graph instantiate: %s", cudaGetErrorString(ce));
+    }
+  }
+  r.steps = G;
+  r.dt = dt;
+  r.pattern = pat;
+  return SPC_OK;
+}
+
 bool batch_slot_ok(spc_batch *b, int slot) {
   return slot >= 0 && slot < b->e.sys_cap && b->e.slots[slot].used;
 }
@@ -204,6 +306,125 @@ int spc_step_graph(spc_handle *h, double *t_inout, double dt, int32_t nsteps) {
   for (int s = 0; s < nsteps; ++s) t += dt;
   *t_inout = t;
   return SPC_OK;
+}
+
+int spc_run(spc_handle *h, double *t_inout, double dt, int64_t nsteps, int32_t period,
+            const uint8_t *observe, spc_observe_fn fn, void *user, int64_t *steps_done) {
+  if (steps_done) *steps_done = 0;
+  if (!h || !t_inout) return hfail(h, SPC_ERR_INVALID, "NULL argument");
+  if (nsteps < 0) return hfail(h, SPC_ERR_INVALID, "nsteps must be >= 0");
+  if (period < 1) return hfail(h, SPC_ERR_INVALID, "period must be >= 1");
+  if (fn && !observe) return hfail(h, SPC_ERR_INVALID, "observe is NULL");
+  SPC_TRY(check_ready(h));
+  Engine *e = &h->e;
+  SPC_TRY(engine_set_device(e));
+  const long long per_step = (long long)noise_per_particle(h->p.stepper) * h->n;
+  const bool inject = e->injecting && per_step > 0;
+  if (inject && e->noise_cursor + per_step * nsteps > e->noise_count)
+    return fail(e, SPC_ERR_NOISE, "injected noise: %lld normals left, %lld needed",
+                e->noise_count - e->noise_cursor, per_step * (long long)nsteps);
+  if (nsteps == 0) return SPC_OK;
+  // chunks of G = m periods (about 64 steps) whose snapshots fit rings of 512 MB
+  const size_t snap = 3 * (size_t)h->n;
+  int obs_per_period = 0;
+  if (fn)
+    for (int j = 0; j < period; ++j) obs_per_period += observe[j] != 0;
+  long long m = std::max(1, 64 / period);
+  const size_t ring_cap = ((size_t)512 << 20) / 8;
+  while (m > 1 && (size_t)(obs_per_period * m) * snap > ring_cap) --m;
+  const long long G = std::min<long long>(period * m, nsteps);
+  std::vector<uint8_t> full((size_t)G);
+  int obs_chunk = 0;
+  for (long long s = 0; s < G; ++s) {
+    full[(size_t)s] = fn && observe[(s + 1) % period] ? 1 : 0;
+    obs_chunk += full[(size_t)s];
+  }
+  SPC_TRY(run_pipe_reserve(e, (size_t)obs_chunk * snap));
+  SPC_TRY(engine_layout(e));
+  SPC_TRY(verlet_prepare(e));
+  const bool use_graph = !inject && G <= 1024;
+  if (use_graph) SPC_TRY(run_capture(h, dt, (int)G, full));
+  Engine::RunPipe &r = e->run;
+  struct Chunk {
+    long long first, len;
+    int b, nobs;
+  };
+  bool have_prev = false, stop = false;
+  Chunk prev{};
+  long long done = 0;
+  double t_cb = *t_inout;
+  int rc = SPC_OK;
+  std::vector<uint8_t> pat;
+  for (int c = 0; rc == SPC_OK; ++c) {
+    Chunk cur{};
+    const bool more = done < nsteps && !stop;
+    if (more) {
+      cur.first = done;
+      cur.len = std::min<long long>(G, nsteps - done);
+      cur.b = c & 1;
+      pat.assign((size_t)cur.len, 0);
+      cur.nobs = 0;
+      for (long long s = 0; s < cur.len; ++s) {
+        pat[(size_t)s] = fn && observe[(done + s + 1) % period] ? 1 : 0;
+        cur.nobs += pat[(size_t)s];
+      }
+      // the ring's previous copy (chunk c - 2) completed before its callbacks
+      const double *noise = inject ? e->d_noise + e->noise_cursor : nullptr;
+      if (use_graph && cur.len == G) {
+        const cudaError_t ce = cudaGraphLaunch(r.graph[cur.b], e->stream);
+        if (ce != cudaSuccess) rc = fail(e, SPC_ERR_CUDA, "graph launch: %s", cudaGetErrorString(ce));
+      } else {
+        rc = run_enqueue_chunk(h, dt, (int)cur.len, pat.data(), cur.b, noise, per_step);
+      }
+      if (rc != SPC_OK) break;
+      mirror_call(e, (int)cur.len);
+      if (inject) e->noise_cursor += per_step * cur.len;
+      if (cur.nobs > 0) {
+        cudaError_t ce = cudaEventRecord(r.computed[cur.b], e->stream);
+        if (ce == cudaSuccess) ce = cudaStreamWaitEvent(r.copy, r.computed[cur.b], 0);
+        if (ce == cudaSuccess)
+          ce = cudaMemcpyAsync(r.h_ring[cur.b], r.d_ring[cur.b], (size_t)cur.nobs * snap * 8,
+                               cudaMemcpyDeviceToHost, r.copy);
+        if (ce == cudaSuccess) ce = cudaEventRecord(r.copied[cur.b], r.copy);
+        if (ce != cudaSuccess) {
+          rc = fail(e, SPC_ERR_CUDA, "snapshot copy: %s", cudaGetErrorString(ce));
+          break;
+        }
+      }
+      done += cur.len;
+    }
+    if (have_prev) {
+      // the previous chunk's snapshots, while the device runs this one
+      if (prev.nobs > 0) {
+        const cudaError_t ce = cudaEventSynchronize(r.copied[prev.b]);
+        if (ce != cudaSuccess) {
+          rc = fail(e, SPC_ERR_CUDA, "snapshot copy: %s", cudaGetErrorString(ce));
+          break;
+        }
+      }
+      int k = 0;
+      for (long long s = 0; s < prev.len; ++s) {
+        t_cb += dt;
+        const long long step = prev.first + s + 1;
+        if (fn && observe[step % period]) {
+          if (!stop && fn(user, step, t_cb, r.h_ring[prev.b] + (size_t)k * snap) != 0) stop = true;
+          ++k;
+        }
+      }
+    }
+    if (!more) break;
+    prev = cur;
+    have_prev = true;
+  }
+  // the state has advanced by every enqueued step
+  cudaError_t ce = cudaStreamSynchronize(e->stream);
+  if (ce == cudaSuccess && r.copy) ce = cudaStreamSynchronize(r.copy);
+  if (rc == SPC_OK && ce != cudaSuccess) rc = fail(e, SPC_ERR_CUDA, "run: %s", cudaGetErrorString(ce));
+  double t = *t_inout;
+  for (long long s = 0; s < done; ++s) t += dt;  // SimulationEngine.cpp:151
+  *t_inout = t;
+  if (steps_done) *steps_done = done;
+  return rc;
 }
 
 int spc_get_step_counter(const spc_handle *h, uint64_t *out) {
@@ -409,6 +630,14 @@ int spc_synchronize(spc_handle *h) {
 }
 
 void *spc_stream(spc_handle *h) { return h ? (void *)h->e.stream : nullptr; }
+
+int spc_run_graph_nodes(const spc_handle *h, int64_t *nodes, int32_t *steps) {
+  if (!h || !nodes) return fail(nullptr, SPC_ERR_INVALID, "NULL argument");
+  const bool have = h->e.run.graph[0] != nullptr;
+  *nodes = have ? (int64_t)h->e.run.graph_nodes : 0;
+  if (steps) *steps = have ? h->e.run.steps : 0;
+  return SPC_OK;
+}
 
 int spc_graph_nodes(const spc_handle *h, int64_t *nodes) {
   if (!h || !nodes) return fail(nullptr, SPC_ERR_INVALID, "NULL argument");

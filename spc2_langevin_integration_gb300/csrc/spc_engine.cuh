@@ -211,6 +211,19 @@ struct Engine {
   int *vrowlen = nullptr, *vsys = nullptr, *vcell = nullptr, *vflags = nullptr;
   double *vxb = nullptr, *vyb = nullptr;
   unsigned long long *vrebuilds = nullptr;
+  // observed run loop (spc_run): two snapshot rings (device and pinned host),
+  // a copy stream, and one captured chunk graph per ring
+  struct RunPipe {
+    cudaStream_t copy = nullptr;
+    cudaEvent_t computed[2] = {}, copied[2] = {};
+    double *d_ring[2] = {}, *h_ring[2] = {};
+    size_t ring_doubles = 0;
+    cudaGraphExec_t graph[2] = {};
+    size_t graph_nodes = 0;
+    int steps = 0;
+    double dt = 0.0;
+    std::vector<uint8_t> pattern;  // observe after chunk step s (0-based) iff pattern[s]
+  } run;
 };
 
 inline int fail(Engine *e, int code, const char *fmt, ...) {
@@ -406,13 +419,34 @@ inline int verlet_prepare(Engine *e) {
   return SPC_OK;
 }
 
+inline void drop_graph(Engine *e) {
+  if (e->graph) {
+    cudaGraphExecDestroy(e->graph);
+    e->graph = nullptr;
+  }
+  for (cudaGraphExec_t &g : e->run.graph)
+    if (g) {
+      cudaGraphExecDestroy(g);
+      g = nullptr;
+    }
+}
+
 inline void engine_free(Engine *e) {
   if (!e || e->view) return;
   cudaSetDevice(e->device);
   if (e->stream) cudaStreamSynchronize(e->stream);
-  if (e->graph) cudaGraphExecDestroy(e->graph);
+  if (e->run.copy) cudaStreamSynchronize(e->run.copy);
+  drop_graph(e);
   for (cudaEvent_t ev : e->prof_ev)
     if (ev) cudaEventDestroy(ev);
+  for (int b = 0; b < 2; ++b) {
+    if (e->run.computed[b]) cudaEventDestroy(e->run.computed[b]);
+    if (e->run.copied[b]) cudaEventDestroy(e->run.copied[b]);
+    if (e->run.h_ring[b]) cudaFreeHost(e->run.h_ring[b]);
+    e->run.h_ring[b] = nullptr;
+  }
+  if (e->run.copy) cudaStreamDestroy(e->run.copy);
+  e->run.copy = nullptr;
   for (void *p : e->allocs) cudaFree(p);
   e->allocs.clear();
   if (e->stream) cudaStreamDestroy(e->stream);
@@ -447,13 +481,6 @@ inline void pool_give(Engine *e, int at, int n) {
       merged.push_back(r);
   }
   fr.swap(merged);
-}
-
-inline void drop_graph(Engine *e) {
-  if (e->graph) {
-    cudaGraphExecDestroy(e->graph);
-    e->graph = nullptr;
-  }
 }
 
 // Admit a system: its state goes to a pool range; returns the slot.

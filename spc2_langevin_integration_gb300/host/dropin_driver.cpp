@@ -12,6 +12,9 @@
 //  the first N injected values, the frequencies it draws and never uses.)
 // With SPC_OUTPUT_DIR set, a run also writes the reference's observer files
 // there (a frame and a summary line after every step, as the engine loop does).
+// With SPC_DEVICE_LOOP=1 a run is one RunObserved call (the loop on the
+// device, states delivered at the observer's and the recording cadence)
+// instead of one DoStep per step; the outputs must not change.
 #include <cstdint>
 #include <cstdio>
 #include <cstdlib>
@@ -79,6 +82,14 @@ int main(int argc, char **argv) {
       observer->SaveSystemState(s, t);
       observer->SaveSummaryStatistics(s, t);
     };
+    const bool device_loop = std::getenv("SPC_DEVICE_LOOP") && std::atoi(std::getenv("SPC_DEVICE_LOOP")) != 0;
+    // the whole loop in one call: records every record_every-th state and the last
+    auto run_device = [&](SpcSystemBase &system, int kind) {
+      Real t = h.t0;
+      RunObserved(system, kind, state, t, h.dt, h.nsteps, observer, h.record_every,
+                  [&](long, Real, const std::vector<Real> &s) { dump(s.data(), n3); });
+      if (h.record_every <= 0 || h.nsteps % h.record_every != 0) dump(state.data(), n3);
+    };
     // the shared-window engine loop (SimulationEnginePtr.cpp:106-115)
     auto run_ptr = [&](auto &system) {
       if (h.mode == 1) {
@@ -104,6 +115,12 @@ int main(int argc, char **argv) {
         rest.assign(noise.begin() + kN, noise.end());
       }
       if (!rest.empty()) system.InjectNoise(rest);
+      if (device_loop) {
+        if (h.stepper == 1 && h.family == 1)
+          system.UseFrequencies(std::vector<Real>(noise.begin(), noise.begin() + kN));
+        run_device(system, h.stepper == 0 ? SPC_STEPPER_EULER_PTR : h.stepper == 1 ? SPC_STEPPER_SRK : SPC_STEPPER_RK4);
+        return;
+      }
       Real t = h.t0;
       for (int k = 1; k <= h.nsteps; ++k) {
         t += h.dt;
@@ -143,7 +160,10 @@ int main(int argc, char **argv) {
         StochasticRungeKuttaStepper srk(&thread);
         RungeKutta4Stepper rk4(&thread);
         Real t = h.t0;
-        for (int k = 1; k <= h.nsteps; ++k) {
+        if (device_loop)
+          run_device(chimera_system,
+                     h.stepper == 0 ? SPC_STEPPER_EULER : h.stepper == 1 ? SPC_STEPPER_SRK : SPC_STEPPER_RK4);
+        for (int k = 1; k <= h.nsteps && !device_loop; ++k) {
           t += h.dt;
           if (h.stepper == 0)
             euler.DoStep(chimera_system, state, t, h.dt);

@@ -2,6 +2,7 @@
 #include "spc_dropin.hpp"
 
 #include <algorithm>
+#include <exception>
 #include <cmath>
 #include <numeric>
 
@@ -152,6 +153,48 @@ void SpcSystemBase::Advance(int stepper, std::vector<Real> &state, Real &t, Real
   while (handles_[k] != h) ++k;
   shadow_[k] = state;
   t = tt;
+}
+
+namespace {
+struct RunCall {
+  const SpcSystemBase::StateFn *fn;
+  std::exception_ptr error;
+};
+
+int run_trampoline(void *user, int64_t step, double t, const double *aos3n) {
+  RunCall *c = static_cast<RunCall *>(user);
+  try {
+    return (*c->fn)((long)step, t, aos3n) ? 1 : 0;
+  } catch (...) {  // never unwind through the C library
+    c->error = std::current_exception();
+    return 1;
+  }
+}
+}  // namespace
+
+long SpcSystemBase::Run(int stepper, std::vector<Real> &state, Real &t, Real dt, long nsteps, int period,
+                        const std::vector<uint8_t> &observe, const StateFn &on_state) {
+  if ((int)state.size() != kS * kN) throw std::runtime_error("spc: state size is not 3N");
+  if (on_state && (int)observe.size() != period) throw std::runtime_error("spc: observe needs period entries");
+  spc_handle *h = Handle(stepper);
+  Sync(h, state);
+  if (inject_pending_) {
+    Check(spc_inject_noise(h, injected_.data(), (int64_t)injected_.size()), h);
+    inject_pending_ = false;
+  }
+  RunCall call{&on_state, nullptr};
+  double tt = t;
+  int64_t done = 0;
+  const int rc = spc_run(h, &tt, dt, nsteps, period, on_state ? observe.data() : nullptr,
+                         on_state ? run_trampoline : nullptr, &call, &done);
+  if (call.error) std::rethrow_exception(call.error);
+  Check(rc, h);
+  Check(spc_download_state(h, state.data()), h);
+  int k = 0;
+  while (handles_[k] != h) ++k;
+  shadow_[k] = state;
+  t = tt;
+  return (long)done;
 }
 
 // ---------------------------------------------------------------------------

@@ -25,6 +25,7 @@
 #include <cstdint>
 #include <stdexcept>
 #include <string>
+#include <functional>
 #include <vector>
 
 #include "../../include/spc_gb300.h"
@@ -113,6 +114,13 @@ class SpcSystemBase {
   void Advance(int stepper, std::vector<Real> &state, Real &t, Real dt, int nsteps);
   // the same on a raw 3N state (the shared-window classes' Real * state)
   void AdvanceRaw(int stepper, Real *const state, Real &t, Real dt, int nsteps);
+  // nsteps steps of the engine loop on the device (spc_run): after step k
+  // (1-based) with observe[k % period] set, on_state(k, t_k, state) sees the
+  // 3N state of that step while the device runs on; a true return stops the
+  // run.  state and t end as after the steps taken, which are returned.
+  using StateFn = std::function<bool(long, Real, const Real *)>;
+  long Run(int stepper, std::vector<Real> &state, Real &t, Real dt, long nsteps, int period,
+           const std::vector<uint8_t> &observe, const StateFn &on_state);
   // natural frequencies for the stochastic Runge-Kutta handle (re-uploaded
   // when they change)
   void UseFrequencies(const std::vector<Real> &frequencies);

@@ -3,6 +3,7 @@
 
 #include <cmath>
 #include <complex>
+#include <numeric>
 #include <cstdio>
 #include <cstdlib>
 #include <sstream>
@@ -86,4 +87,54 @@ void InitializeSystemStateFromFile(const std::string &file_name, std::vector<Rea
   if ((size_t)f.gcount() != buf.size() * sizeof(float))
     throw std::runtime_error(file_name + ": fewer than 3N float32 values");
   system_state.assign(buf.begin(), buf.end());
+}
+
+bool BinaryObserver::StateWrittenAt(long j) const {
+  const long T = output_time_threshold_[0];
+  return thread_->IsRoot() && ((output_time_counter_[0] + j - 1) % T + T) % T == 0;
+}
+
+bool BinaryObserver::SummaryWrittenAt(long j) const {
+  const long T = output_time_threshold_[1];
+  return thread_->IsRoot() && ((output_time_counter_[1] + j - 1) % T + T) % T == 0;
+}
+
+void BinaryObserver::SkipCalls(long n) {
+  output_time_counter_[0] += (int)n;
+  output_time_counter_[1] += (int)n;
+}
+
+long BinaryObserver::CadencePeriod() const {
+  const long a = output_time_threshold_[0], b = output_time_threshold_[1];
+  return a / std::gcd(a, b) * b;
+}
+
+void RunObserved(SpcSystemBase &system, int stepper, std::vector<Real> &state, Real &t, Real dt, long nsteps,
+                 BinaryObserver *observer, long every,
+                 const std::function<void(long, Real, const std::vector<Real> &)> &on_state) {
+  long period = observer ? observer->CadencePeriod() : 1;
+  if (every > 0) period = period / std::gcd(period, every) * every;
+  if (period > (1L << 20)) throw std::runtime_error("RunObserved: observer cadence period too long");
+  // step k is observed when k % period == j: j stands for step j (or period)
+  std::vector<uint8_t> observe((size_t)period, 0);
+  for (long j = 0; j < period; ++j) {
+    const long k = j == 0 ? period : j;
+    observe[(size_t)j] = (observer && (observer->StateWrittenAt(k) || observer->SummaryWrittenAt(k))) ||
+                         (every > 0 && k % every == 0);
+  }
+  std::vector<Real> snapshot;
+  long last = 0;
+  auto fn = [&](long k, Real tk, const Real *s) {
+    snapshot.assign(s, s + (size_t)kS * kN);
+    if (observer) {
+      observer->SkipCalls(k - last - 1);
+      observer->SaveSystemState(snapshot, tk);
+      observer->SaveSummaryStatistics(snapshot, tk);
+    }
+    if (every > 0 && k % every == 0 && on_state) on_state(k, tk, snapshot);
+    last = k;
+    return false;
+  };
+  const long done = system.Run(stepper, state, t, dt, nsteps, (int)period, observe, fn);
+  if (observer) observer->SkipCalls(done - last);
 }

@@ -19,6 +19,7 @@
 #pragma once
 
 #include <fstream>
+#include <functional>
 #include <string>
 #include <vector>
 
@@ -36,6 +37,13 @@ class BinaryObserver {
   // write every `state_every`-th / `summary_every`-th call (the reference's
   // output_time_threshold_, 1 and 1 there)
   void SetOutputThresholds(int state_every, int summary_every);
+  // the device loop (RunObserved): whether the j-th next call (j >= 1) of
+  // SaveSystemState / SaveSummaryStatistics writes, and n calls of each that
+  // write nothing (the counters advance as if the engine had called them)
+  bool StateWrittenAt(long j) const;
+  bool SummaryWrittenAt(long j) const;
+  void SkipCalls(long n);
+  long CadencePeriod() const;  // lcm of the two thresholds
   const std::string &SimulationFileName() const { return simulation_file_name_; }
   const std::string &SummaryStatisticsFileName() const { return summary_statistics_file_name_; }
 
@@ -49,3 +57,13 @@ class BinaryObserver {
 };
 
 void InitializeSystemStateFromFile(const std::string &file_name, std::vector<Real> &system_state);
+
+// The engine loop of SimulationEngine::RunSimulation (SimulationEngine.cpp:149-161)
+// for nsteps steps of stepper kind `stepper`, run on the device by spc_run:
+// the observer writes exactly the frames and summary lines its counters ask
+// for, from snapshots of those steps, while the device runs the next steps.
+// With every > 0, on_state also sees the state after every every-th step.
+// state and t end as after the last step.
+void RunObserved(SpcSystemBase &system, int stepper, std::vector<Real> &state, Real &t, Real dt, long nsteps,
+                 BinaryObserver *observer, long every = 0,
+                 const std::function<void(long, Real, const std::vector<Real> &)> &on_state = nullptr);

@@ -123,3 +123,24 @@ def test_dropin_rhs_matches_reference_golden(name):
     d, a = out[:3 * n], out[3 * n:]
     assert np.all(np.abs(d - g["srk_derivative"]) <= RHS_TOL * np.maximum(np.abs(g["srk_derivative"]), 1.0) * 10)
     assert np.all(np.abs(a - g["srk_additional"]) <= RHS_TOL * np.maximum(np.abs(g["srk_additional"]), 1.0) * 10)
+
+
+@pytest.mark.parametrize("name", golden_cases() + va_golden_cases())
+def test_dropin_device_loop_matches_per_step_loop(name, tmp_path):
+    # RunObserved (the engine loop on the device, spc_run) against one DoStep
+    # per step: the same recorded states, bit for bit, and byte-identical
+    # observer files; both within the golden tolerance of the reference
+    g = load_golden(name)
+    d_step, d_loop = tmp_path / "step", tmp_path / "loop"
+    d_step.mkdir()
+    d_loop.mkdir()
+    per_step = _run(g, 0, extra_env={"SPC_OUTPUT_DIR": str(d_step)})
+    loop = _run(g, 0, extra_env={"SPC_OUTPUT_DIR": str(d_loop), "SPC_DEVICE_LOOP": "1"})
+    assert np.array_equal(per_step, loop)
+    n, L = int(g["n"]), float(g["L"])
+    for got, want in zip(loop.reshape(-1, 3 * n), np.asarray(g["trajectory"])):
+        assert np.abs(periodic_diff(got, want, L)).max() <= TRAJ_TOL
+    files = sorted(os.listdir(d_step))
+    assert files == sorted(os.listdir(d_loop)) and len(files) == 2
+    for f in files:
+        assert open(d_step / f, "rb").read() == open(d_loop / f, "rb").read(), f
