@@ -554,7 +554,7 @@ def tune_form(abi, w, precision, rank=0):
 
 
 def run_form(abi, torch, w, precision, steps, warmup, rank, dist, params=None, sparse_below=None,
-             e2e=True):
+             e2e=True, tile_split=None):
     """Device-timed graph replays of the workload; then (e2e) the same through
     the C-ABI with host buffers, and a per-phase profile."""
     n = w["n"]
@@ -563,6 +563,8 @@ def run_form(abi, torch, w, precision, steps, warmup, rank, dist, params=None, s
     s = abi.System(n, p)
     if sparse_below is not None and p.neighbour == abi.NEIGHBOUR_CELL:
         s.set_tuning(abi.TUNE_SPARSE_BELOW, sparse_below)
+    if tile_split is not None:
+        s.set_tuning(abi.TUNE_TILE_SPLIT, tile_split)
     s.upload_state(st)
     s.upload_omega(omega)
     stream = torch.cuda.ExternalStream(s.stream)
@@ -639,6 +641,8 @@ def main():
                          "--skin (no autotune): the command for a launch list of the timed region")
     ap.add_argument("--neighbour", choices=["cell", "verlet"], default="cell")
     ap.add_argument("--skin", type=float, default=None)
+    ap.add_argument("--tile-split", type=int, default=None,
+                    help="--form: CTAs per cell of the cell-tile passes (0: the default, 1)")
     ap.add_argument("--cell-list", action="store_true",
                     help="--ncu-case fp32c/fp64: the cell-list passes instead of the Verlet rows")
     ap.add_argument("--workload",
@@ -817,9 +821,10 @@ def main():
         if args.skin is not None:
             p.skin = args.skin
         ms, e2e_ms, prof, _, launches = run_form(abi, torch, w, prec, args.steps, args.warmup,
-                                                 rank, dist, p)
+                                                 rank, dist, p, tile_split=args.tile_split)
         if rank == 0:
             print(json.dumps({"form": args.form, "neighbour": args.neighbour, "skin": p.skin,
+                              "tile_split": args.tile_split,
                               "value": n_total * SIM_STEPS_PER_BENCH_STEP * args.steps / (ms / 1e3),
                               "ms_per_bench_step": ms / args.steps, "profile_ms": prof,
                               "gpu_launches": launches}))

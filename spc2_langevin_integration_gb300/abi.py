@@ -21,6 +21,7 @@ PRECISION_FP64, PRECISION_FP32C = 0, 1
 FLAG_EXACT_ALL = 0x1
 TUNE_SPARSE_BELOW = 1
 TUNE_VERLET_ROW_LIMIT = 2
+TUNE_TILE_SPLIT = 3
 
 SPC_OK = 0
 ERRORS = {

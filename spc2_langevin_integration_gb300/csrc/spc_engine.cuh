@@ -187,6 +187,8 @@ struct Engine {
   // tuning: cell-list systems with fewer than sparse_below particles per cell
   // (on average) run the warp-per-cell passes
   double sparse_below = kSparseBelowDefault;
+  // tuning: CTAs per cell of the cell-tile kernels (0: chosen per layout)
+  int tile_split_tune = 0;
   std::vector<int> slot_layout;  // slot -> layout index (-1 if inactive)
   // noise injection (single-system handles)
   double *d_noise = nullptr;
@@ -419,6 +421,12 @@ inline int verlet_prepare(Engine *e) {
   return SPC_OK;
 }
 
+// CTAs per cell of the cell-tile kernels: one unless tuned.  Splitting the
+// 64-particle cells of a one-wave system (1024 cells) into 2-4 CTAs to even
+// out the SMs' ends of pass measured 3-4% slower on GB300 (each CTA stages the
+// whole stencil; the idle SM time at the end of a pass did not shrink).
+inline int tile_split_for(int tune) { return tune > 0 ? tune : 1; }
+
 inline void drop_graph(Engine *e) {
   if (e->graph) {
     cudaGraphExecDestroy(e->graph);
@@ -601,6 +609,7 @@ inline int engine_layout(Engine *e) {
   a.n_active = e->n_active;
   a.ncell_total = e->ncell_total;
   a.ncell_tile = e->ncell_tile;
+  a.tile_split = tile_split_for(e->tile_split_tune);
   a.va_c0 = e->ncell_tile + e->ncell_warp;
   a.va_c1 = a.va_c0 + e->ncell_va;
   a.n_ap = (int)ap.size();
@@ -749,7 +758,7 @@ int launch_pass_t(Engine *e, const KArgs &a, int epi) {
   if (e->has_cells) {
     {
       if (e->ncell_tile > 0) {
-        const int grid = std::min(e->ncell_tile, 152 * 256);
+        const int grid = std::min(e->ncell_tile * std::max(a.tile_split, 1), 152 * 256);
         if constexpr (PREC == kPrecFP32C)
           k_tile_fp32c<KIND><<<grid, kTileThreads32, 0, st>>>(a, epi);
         else
@@ -891,6 +900,15 @@ inline int engine_set_tuning(Engine *e, int key, double value) {
     drop_graph(e);
     return SPC_OK;
   }
+  if (key == SPC_TUNE_TILE_SPLIT) {
+    if (!(value >= 0.0) || !(value <= 8.0) || value != std::floor(value))
+      return fail(e, SPC_ERR_INVALID, "tile split must be an integer in [0, 8]");
+    if ((int)value != e->tile_split_tune) {
+      e->tile_split_tune = (int)value;
+      e->dirty = true;
+    }
+    return SPC_OK;
+  }
   if (key == SPC_TUNE_SPARSE_BELOW) {
     if (!(value >= 0.0) || !std::isfinite(value)) return fail(e, SPC_ERR_INVALID, "sparse_below must be >= 0");
     if (value != e->sparse_below) {
@@ -909,6 +927,10 @@ inline int engine_get_tuning(const Engine *e, int key, double *value) {
   }
   if (key == SPC_TUNE_SPARSE_BELOW) {
     *value = e->sparse_below;
+    return SPC_OK;
+  }
+  if (key == SPC_TUNE_TILE_SPLIT) {  // the split in effect
+    *value = (double)tile_split_for(e->tile_split_tune);
     return SPC_OK;
   }
   return fail(nullptr, SPC_ERR_INVALID, "unknown tuning key %d", key);

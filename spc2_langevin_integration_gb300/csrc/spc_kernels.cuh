@@ -68,6 +68,7 @@ struct KArgs {
   int n_active;                      // dense particles
   int ncell_total;
   int ncell_tile;                    // cells [0, ncell_tile): cell-tile kernels
+  int tile_split;                    // cell-tile kernels: CTAs per cell (0 or 1: one)
   int va_c0, va_c1;                  // [ncell_tile, va_c0): warp kernel; [va_c0, va_c1): vortex arrays
   const int *sys_of_p;               // dense index -> system
   const int *sys_of_c;               // global cell -> system

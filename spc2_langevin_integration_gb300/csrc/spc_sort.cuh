@@ -46,39 +46,13 @@ __global__ void __launch_bounds__(kSortThreads)
   for (int d = threadIdx.x; d < R; d += blockDim.x) hist[(size_t)blockIdx.x * R + d] = h[d];
 }
 
-// In-place exclusive scan of the tile-major table hist[tile][digit] in
-// digit-major order (all tiles of digit 0, then of digit 1, ...), which gives
-// each (tile, digit) its first output position.  One block: each thread owns
-// digits d = t, t + 1024; it sums its digits over the tiles (independent,
-// coalesced loads), the block scans the digit totals with warp shuffles, and
-// the thread writes its digits' running prefixes back.
-__global__ void __launch_bounds__(kScanThreads)
-    k_scan_digits(uint32_t *__restrict__ hist, int ntiles, int bits, const int *gate) {
-  if (gate && *gate == 0) return;
-  __shared__ uint32_t wsum[kScanThreads / kWarp];
-  const int R = 1 << bits;
+// For many tiles the scan runs in three steps over groups of kScanGroup tiles
+// (below); the register path of k_scan_digits takes at most kScanGroup tiles.
+constexpr int kScanGroup = 32;
+
+// Block-wide exclusive scan of one value per thread (kScanThreads threads).
+__device__ __forceinline__ uint32_t block_exclusive_scan(uint32_t mine, uint32_t *wsum) {
   const int t = threadIdx.x, lane = t % kWarp, w = t / kWarp;
-  constexpr int kPer = 2;  // up to 2048 digits
-  uint32_t tot[kPer];
-#pragma unroll
-  for (int k = 0; k < kPer; ++k) {
-    const int d = t * kPer + k;
-    uint32_t s = 0;
-    if (d < R) {
-      // eight independent loads in flight per iteration (tiles are <= 32 here)
-      int tile = 0;
-      for (; tile + 8 <= ntiles; tile += 8) {
-        uint32_t v[8];
-#pragma unroll
-        for (int u = 0; u < 8; ++u) v[u] = hist[(size_t)(tile + u) * R + d];
-#pragma unroll
-        for (int u = 0; u < 8; ++u) s += v[u];
-      }
-      for (; tile < ntiles; ++tile) s += hist[(size_t)tile * R + d];
-    }
-    tot[k] = s;
-  }
-  const uint32_t mine = tot[0] + tot[1];
   uint32_t incl = mine;
 #pragma unroll
   for (int off = 1; off < kWarp; off <<= 1) {
@@ -98,7 +72,65 @@ __global__ void __launch_bounds__(kScanThreads)
     wsum[lane] = si - s;
   }
   __syncthreads();
-  uint32_t run = wsum[w] + (incl - mine);
+  return wsum[w] + (incl - mine);
+}
+
+// In-place exclusive scan of the tile-major table hist[tile][digit] in
+// digit-major order (all tiles of digit 0, then of digit 1, ...), which gives
+// each (tile, digit) its first output position.  One block of 1024 threads.
+// Up to 1024 digits and kScanGroup tiles each thread owns one digit: it loads
+// the digit's counts of every tile at once (coalesced across threads, all in
+// flight), keeps them in registers, and writes the running prefixes back
+// after the block scan of the digit totals.  Otherwise (2048 digits, or the
+// sums of more than kScanGroup groups) each thread owns two consecutive
+// digits and reads their counts twice, eight loads in flight.
+__global__ void __launch_bounds__(kScanThreads)
+    k_scan_digits(uint32_t *__restrict__ hist, int ntiles, int bits, const int *gate) {
+  if (gate && *gate == 0) return;
+  __shared__ uint32_t wsum[kScanThreads / kWarp];
+  const int R = 1 << bits;
+  const int t = threadIdx.x;
+  if (R <= kScanThreads && ntiles <= kScanGroup) {
+    const bool own = t < R;
+    uint32_t v[kScanGroup];
+    uint32_t mine = 0;
+#pragma unroll
+    for (int tile = 0; tile < kScanGroup; ++tile)
+      v[tile] = (own && tile < ntiles) ? hist[(size_t)tile * R + t] : 0u;
+#pragma unroll
+    for (int tile = 0; tile < kScanGroup; ++tile) mine += v[tile];
+    uint32_t run = block_exclusive_scan(mine, wsum);
+#pragma unroll
+    for (int tile = 0; tile < kScanGroup; ++tile) {
+      if (own && tile < ntiles) {
+        hist[(size_t)tile * R + t] = run;
+        run += v[tile];
+      }
+    }
+    return;
+  }
+  constexpr int kPer = 2;  // up to 2048 digits
+  uint32_t tot[kPer];
+#pragma unroll
+  for (int k = 0; k < kPer; ++k) {
+    const int d = t * kPer + k;
+    uint32_t s = 0;
+    if (d < R) {
+      // eight independent loads in flight per iteration
+      int tile = 0;
+      for (; tile + 8 <= ntiles; tile += 8) {
+        uint32_t v[8];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) v[u] = hist[(size_t)(tile + u) * R + d];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) s += v[u];
+      }
+      for (; tile < ntiles; ++tile) s += hist[(size_t)tile * R + d];
+    }
+    tot[k] = s;
+  }
+  const uint32_t mine = tot[0] + tot[1];
+  uint32_t run = block_exclusive_scan(mine, wsum);
 #pragma unroll
   for (int k = 0; k < kPer; ++k) {
     const int d = t * kPer + k;
@@ -128,8 +160,6 @@ __global__ void __launch_bounds__(kScanThreads)
 // per-(group, digit) sums, a one-block digit-major scan of those sums (the
 // same k_scan_digits with groups in place of tiles), and per-(group, digit)
 // running prefixes written back over the group's tiles.
-constexpr int kScanGroup = 32;
-
 __global__ void k_scan_group_sums(const uint32_t *__restrict__ hist, int ntiles, int bits,
                                   uint32_t *__restrict__ part, const int *gate) {
   if (gate && *gate == 0) return;

@@ -75,10 +75,39 @@ __device__ __forceinline__ float shift_y(int q, float cell_f) { return (float)(q
 // ---------------------------------------------------------------------------
 // FP32C passes.  Pass 1 (KIND == kKindSin) also records, for cells whose
 // candidate list fits one staging round, each particle's neighbour set as a
-// bitmask over that list (word w of particle p at nbmask[w * n + p]); pass 2
-// (kKindCos2) then walks only the set bits instead of re-testing every
-// candidate.  Cells with more candidates run the filter in pass 2 as well.
+// bitmask over that list; pass 2 (kKindCos2) then walks only the set bits
+// instead of re-testing every candidate.  Cells with more candidates run the
+// filter in pass 2 as well.  Four consecutive words of a particle share one
+// 16-byte group (word w of particle p at nbmask[((w / 4) * n + p) * 4 + w % 4]),
+// so pass 2 fetches the masks of four candidate blocks with one load.
 constexpr int kMaskWords = kTileCap / 32;
+static_assert(kMaskWords % 4 == 0, "mask words come in groups of four");
+
+__device__ __forceinline__ size_t tile_mask_at(int w, int p, int n) {
+  return ((size_t)(w >> 2) * n + p) * 4 + (w & 3);
+}
+
+// Work item `item` of the cell-tile kernels: cell c = item / K and part
+// item % K of its particles, K = a.tile_split CTAs per cell.  Parts are
+// multiples of 32 particles, so a warp chunk never straddles two CTAs.  c0 is
+// the cell's first particle (the own cell's stencil entry starts there).
+struct TileItem {
+  int c, c0, cb, ce;
+};
+
+__device__ __forceinline__ int tile_items(const KArgs &a) { return a.ncell_tile * max(a.tile_split, 1); }
+
+__device__ __forceinline__ bool tile_item(const KArgs &a, int item, TileItem &t) {
+  const int K = max(a.tile_split, 1);
+  t.c = item / K;
+  const int h = item - t.c * K;
+  t.c0 = a.cell_start[t.c];
+  const int c1 = a.cell_start[t.c + 1];
+  const int per = ((c1 - t.c0 + K - 1) / K + 31) & ~31;
+  t.cb = t.c0 + h * per;
+  t.ce = min(c1, t.cb + per);
+  return t.cb < t.ce;
+}
 
 // Per-part results of one 128-particle group: each part's compensated sums
 // (sum minus compensation) and counts; pass 1 has one sum, pass 2 two.
@@ -98,41 +127,47 @@ __device__ __forceinline__ int split_point(int rcnt, int part, int S) {
   return part >= S ? rcnt : ((rcnt * part / S) & ~31);
 }
 
+// Float prefilter offset d^2 - mid of a candidate at (dx, dy), in two fused
+// multiply-adds.  A pair is inside when off < -band, outside when off > band,
+// and undecided (left to the reference's FP64 test) otherwise: one value for
+// all three, so the float-inside and undecided sets are disjoint.  Float
+// error is ~1e-7 rho^2, far inside the band of 3e-5 rho^2.
+__device__ __forceinline__ float cutoff_offset(float dx, float dy, float nmid) {
+  return fmaf(dx, dx, fmaf(dy, dy, nmid));
+}
+
 // One block of 32 staged candidates against one particle (FP32C).  The block
 // is fully unrolled: bit t of *bits is candidate j0 + t.  SELF: the block may
 // contain the particle itself (staged index `self`).  Pairs the float test
-// cannot decide (within the band around rho^2) are left out here and reported
-// through *mn (the smallest |d2 - mid| seen).
+// cannot decide are left out here and reported through *mn (the smallest
+// |d^2 - mid| seen).  The block sums the inside candidates' cos phi_j and
+// sin phi_j (and, pass 2, the same weighted by the phase rate d_j); the
+// caller turns them into the alignment terms by angle addition once per block.
 template <int KIND, bool SELF>
 __device__ __forceinline__ void block32(const float4 *__restrict__ s_c4, const float *__restrict__ s_d,
-                                        int j0, int self, float fxi, float fyi, float ca, float sa,
-                                        float di, float lo2, float mid, float &b0, float &b1,
-                                        uint32_t &bits, float &mn) {
+                                        int j0, int self, float fxi, float fyi, float nmid, float nband,
+                                        float &sc_, float &ss_, float &sdc, float &sds, uint32_t &bits,
+                                        float &mn) {
 #pragma unroll
   for (int t = 0; t < kWarp; ++t) {
     const float4 cj = s_c4[j0 + t];
     const float dx = cj.x - fxi, dy = cj.y - fyi;
-    const float d2 = fmaf(dx, dx, dy * dy);
-    bool in = d2 < lo2;
-    float off = fabsf(d2 - mid);
+    float off = cutoff_offset(dx, dy, nmid);
+    bool in = off < nband;
     if (SELF) {
       in = in && (j0 + t != self);
       off = (j0 + t != self) ? off : 3.0e38f;
     }
-    mn = fminf(mn, off);
-    if constexpr (KIND == kKindSin) {
-      const float tv = fmaf(cj.w, ca, -cj.z * sa);
-      if (in) {
-        b0 += tv;
-        bits |= 1u << t;
+    mn = fminf(mn, fabsf(off));
+    if (in) {
+      sc_ += cj.z;
+      ss_ += cj.w;
+      if constexpr (KIND == kKindCos2) {
+        const float dj = s_d[j0 + t];
+        sdc = fmaf(dj, cj.z, sdc);
+        sds = fmaf(dj, cj.w, sds);
       }
-    } else {
-      const float tv = fmaf(cj.z, ca, cj.w * sa);
-      if (in) {
-        b0 += tv;
-        b1 = fmaf(s_d[j0 + t] - di, tv, b1);
-        bits |= 1u << t;
-      }
+      bits |= 1u << t;
     }
   }
 }
@@ -147,14 +182,16 @@ __global__ void __launch_bounds__(kTileThreads32, kTileMinBlocks32) k_tile_fp32c
   __shared__ int t_n[kTileThreads32];
   const int n_all = a.n_active;
   const int tid = threadIdx.x, w = tid / kWarp, lane = tid % kWarp;
-  for (int c = blockIdx.x; c < a.ncell_tile; c += gridDim.x) {
-    const int cb = a.cell_start[c], ce = a.cell_start[c + 1];
-    if (cb == ce) continue;
+  const int nitems = tile_items(a);
+  for (int item = blockIdx.x; item < nitems; item += gridDim.x) {
+    TileItem ti;
+    if (!tile_item(a, item, ti)) continue;
+    const int c = ti.c, c0 = ti.c0, cb = ti.cb, ce = ti.ce;
     const SysDesc &sd = a.sys[a.sys_of_c[c]];
     const SysConst &sc = sd.sc;
     if (sc.allpairs) continue;
     const float lo2 = sc.lo2, hi2 = sc.hi2;
-    const float band = 0.5f * (hi2 - lo2), mid = 0.5f * (hi2 + lo2);
+    const float band = 0.5f * (hi2 - lo2), nmid = -0.5f * (hi2 + lo2);
     const bool exact_all = sc.exact_all != 0;
     Stencil st;
     stencil_of(a, sd, c, st);
@@ -211,41 +248,67 @@ __global__ void __launch_bounds__(kTileThreads32, kTileMinBlocks32) k_tile_fp32c
             yi = a.sy[p];
           }
           // staged index of i itself (the own cell is stencil entry 4); its block
-          const int self = st.prefix[4] + (p - cb) - rlo;
+          const int self = st.prefix[4] + (p - c0) - rlo;
           const int jlo = split_point(rpad, part, S), jhi = split_point(rpad, part + 1, S);
           float S0 = 0.0f, C0 = 0.0f, S1 = 0.0f, C1 = 0.0f;
           int n = 0;
           if (KIND == kKindCos2 && masked) {
-            // pass 2 over the neighbour bitmask of pass 1 (same staged list)
-            uint32_t next = (valid && jlo < jhi) ? a.nbmask[(size_t)(jlo / kWarp) * n_all + p] : 0u;
+            // pass 2 over the neighbour bitmask of pass 1 (same staged list):
+            // one 16-byte group of four mask words in hand, the next in flight
+            const uint4 *m4 = reinterpret_cast<const uint4 *>(a.nbmask);
+            const uint4 none = make_uint4(0u, 0u, 0u, 0u);
+            const int w0 = jlo / kWarp, w1 = jhi / kWarp;
+            int g = w0 >> 2;
+            uint4 cur = (valid && w0 < w1) ? m4[(size_t)g * n_all + p] : none;
+            uint4 nxt = (valid && ((g + 1) << 2) < w1) ? m4[(size_t)(g + 1) * n_all + p] : none;
             for (int j0 = jlo; j0 < jhi; j0 += kWarp) {
-              const uint32_t bits = next;
-              if (j0 + kWarp < jhi)
-                next = valid ? a.nbmask[(size_t)((j0 + kWarp) / kWarp) * n_all + p] : 0u;
-              float b0 = 0.0f, b1 = 0.0f;
+              const int w = j0 / kWarp;
+              if ((w >> 2) != g) {
+                ++g;
+                cur = nxt;
+                nxt = (valid && ((g + 1) << 2) < w1) ? m4[(size_t)(g + 1) * n_all + p] : none;
+              }
+              const int sub = w & 3;
+              const uint32_t bits = sub == 0 ? cur.x : sub == 1 ? cur.y : sub == 2 ? cur.z : cur.w;
+              float sc_ = 0.0f, ss_ = 0.0f, sdc = 0.0f, sds = 0.0f;
 #pragma unroll
               for (int t = 0; t < kWarp; ++t) {
                 if ((bits >> t) & 1u) {
                   const float4 cj = s_c4[j0 + t];
-                  const float tv = fmaf(cj.z, ca, cj.w * sa);
-                  b0 += tv;
-                  b1 = fmaf(s_d[j0 + t] - di, tv, b1);
+                  const float dj = s_d[j0 + t];
+                  sc_ += cj.z;
+                  ss_ += cj.w;
+                  sdc = fmaf(dj, cj.z, sdc);
+                  sds = fmaf(dj, cj.w, sds);
                 }
               }
+              // sum cos(phi_j - phi_i - alpha) and sum (d_j - d_i) cos(...)
+              const float b0 = fmaf(sc_, ca, ss_ * sa);
+              const float b1 = fmaf(sdc, ca, fmaf(sds, sa, -di * b0));
               n += __popc(bits);
               kahan_add(S0, C0, b0);
               kahan_add(S1, C1, b1);
             }
           } else {
             for (int j0 = jlo; j0 < jhi; j0 += kWarp) {
-              float b0 = 0.0f, b1 = 0.0f, mn = 3.0e38f;
+              float sc_ = 0.0f, ss_ = 0.0f, sdc = 0.0f, sds = 0.0f, mn = 3.0e38f;
               uint32_t bits = 0u;
               const bool self_block = (unsigned)(self - j0) < (unsigned)kWarp;
               if (!exact_all) {
                 if (__any_sync(0xffffffffu, self_block))
-                  block32<KIND, true>(s_c4, s_d, j0, self, fxi, fyi, ca, sa, di, lo2, mid, b0, b1, bits, mn);
+                  block32<KIND, true>(s_c4, s_d, j0, self, fxi, fyi, nmid, -band, sc_, ss_, sdc, sds, bits, mn);
                 else
-                  block32<KIND, false>(s_c4, s_d, j0, self, fxi, fyi, ca, sa, di, lo2, mid, b0, b1, bits, mn);
+                  block32<KIND, false>(s_c4, s_d, j0, self, fxi, fyi, nmid, -band, sc_, ss_, sdc, sds, bits, mn);
+              }
+              // the block's alignment terms by angle addition:
+              // sin(phi_j - phi_i - alpha) = sin phi_j ca - cos phi_j sa,
+              // cos(phi_j - phi_i - alpha) = cos phi_j ca + sin phi_j sa
+              float b0, b1 = 0.0f;
+              if constexpr (KIND == kKindSin) {
+                b0 = fmaf(ss_, ca, -sc_ * sa);
+              } else {
+                b0 = fmaf(sc_, ca, ss_ * sa);
+                b1 = fmaf(sdc, ca, fmaf(sds, sa, -di * b0));
               }
               // pairs the float test cannot decide: the reference's FP64 test
               const bool amb = valid && (exact_all || mn <= band);
@@ -256,8 +319,7 @@ __global__ void __launch_bounds__(kTileThreads32, kTileMinBlocks32) k_tile_fp32c
                     if (j == self || j >= rcnt) continue;
                     const float4 cj = s_c4[j];
                     const float dx = cj.x - fxi, dy = cj.y - fyi;
-                    const float d2 = fmaf(dx, dx, dy * dy);
-                    if (!(exact_all || fabsf(d2 - mid) <= band)) continue;
+                    if (!(exact_all || fabsf(cutoff_offset(dx, dy, nmid)) <= band)) continue;
                     int q;
                     const int pj = slot_of(st, rlo + j, q);
                     if (!exact_within(sc, xi, yi, a.sx[pj], a.sy[pj])) continue;
@@ -276,7 +338,7 @@ __global__ void __launch_bounds__(kTileThreads32, kTileMinBlocks32) k_tile_fp32c
               kahan_add(S0, C0, b0);
               if constexpr (KIND == kKindCos2) kahan_add(S1, C1, b1);
               if (KIND == kKindSin && masked && valid)
-                a.nbmask[(size_t)(j0 / kWarp) * n_all + p] = bits;
+                a.nbmask[tile_mask_at(j0 / kWarp, p, n_all)] = bits;
             }
           }
           if (valid) {
@@ -329,9 +391,11 @@ __global__ void __launch_bounds__(kTileThreads64) k_tile_fp64(KArgs a, int epi) 
   __shared__ int s_p[kTileCap64];
   __shared__ uint16_t s_q[kQCap][kTileThreads64];
   const int tid = threadIdx.x;
-  for (int c = blockIdx.x; c < a.ncell_tile; c += gridDim.x) {
-    const int cb = a.cell_start[c], ce = a.cell_start[c + 1];
-    if (cb == ce) continue;
+  const int nitems = tile_items(a);
+  for (int item = blockIdx.x; item < nitems; item += gridDim.x) {
+    TileItem ti;
+    if (!tile_item(a, item, ti)) continue;
+    const int c = ti.c, c0 = ti.c0, cb = ti.cb, ce = ti.ce;
     const SysDesc &sd = a.sys[a.sys_of_c[c]];
     const SysConst &sc = sd.sc;
     if (sc.allpairs) continue;
@@ -370,7 +434,7 @@ __global__ void __launch_bounds__(kTileThreads64) k_tile_fp64(KArgs a, int epi) 
           }
           __syncthreads();
         }
-        const int self = st.prefix[4] + (p - cb) - rlo;
+        const int self = st.prefix[4] + (p - c0) - rlo;
         int qn = 0, qh = 0;
         auto eval = [&](int j) {
           const double dphi_ = dsub(dsub(s_phi[j], il.phi), sc.alpha);

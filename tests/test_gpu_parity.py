@@ -316,3 +316,53 @@ def test_tuning_knob_round_trip():
             s.set_tuning(abi.TUNE_SPARSE_BELOW, -1.0)
         with pytest.raises(abi.SpcError):
             s.set_tuning(99, 1.0)
+
+
+@pytest.mark.parametrize("stepper", [abi.STEPPER_SRK, abi.STEPPER_RK4])
+def test_tile_split_fp64_is_bitwise_and_fp32c_within_float(stepper):
+    # CTAs per cell of the cell-tile passes: each FP64 particle sum walks the
+    # whole candidate list in order whatever the split, so FP64 results are
+    # bitwise equal; FP32C splits the list into other parts (summation order)
+    n, L, dt = 8192, 1.0, 0.005
+    prm = dict(v0=0.02, sigma=2.0, rho=0.125, alpha=0.3, D_phi=0.01)  # ~128 per cell
+    st0 = init_state(n, L, 53)
+    for prec in (abi.PRECISION_FP64, abi.PRECISION_FP32C):
+        got = {}
+        for split in (1, 2, 4, 8):
+            with gpu(n, L, prm, stepper, precision=prec, kernel="tile") as s:
+                s.set_tuning(abi.TUNE_TILE_SPLIT, split)
+                s.upload_state(st0)
+                s.step(dt, 12)
+                got[split] = s.download_state()
+                assert s.get_tuning(abi.TUNE_TILE_SPLIT) == (split if split else 1)
+        for split in (2, 4, 8):
+            if prec == abi.PRECISION_FP64:
+                assert np.array_equal(got[split], got[1]), split
+            else:
+                assert np.abs(periodic_diff(got[split], got[1], L)).max() <= 1e-5, split
+
+
+def test_tile_split_rhs_matches_oracle():
+    # the split passes' SRK-form right-hand side against the oracle, at the
+    # plain form's tolerance (sparse cells: some particles are isolated)
+    n, L = 3000, 1.3
+    prm = dict(v0=0.01, sigma=1.0, rho=0.1, alpha=1.45, D_phi=0.005)
+    st0 = init_state(n, L, 54)
+    o = po.OracleSystem(n, L, **prm)
+    d_ref, a_ref, _ = o.rhs_srk(st0.copy())
+    for split in (1, 3):
+        with gpu(n, L, prm, abi.STEPPER_SRK, kernel="tile") as s:
+            s.set_tuning(abi.TUNE_TILE_SPLIT, split)
+            s.upload_state(st0)
+            d, a = s.rhs_srk()
+        assert np.abs(d - d_ref).max() <= RHS_TOL * max(np.abs(d_ref).max(), 1.0), split
+        assert np.abs(a - a_ref).max() <= RHS_TOL * max(np.abs(a_ref).max(), 1.0), split
+
+
+def test_tile_split_knob_validation():
+    with gpu(256, 1.0, PRM0, abi.STEPPER_EULER) as s:
+        for bad in (-1.0, 9.0, 1.5):
+            with pytest.raises(abi.SpcError):
+                s.set_tuning(abi.TUNE_TILE_SPLIT, bad)
+        s.set_tuning(abi.TUNE_TILE_SPLIT, 3)
+        assert s.get_tuning(abi.TUNE_TILE_SPLIT) == 3.0
