@@ -242,6 +242,15 @@ struct Acc<kPrecFP32C> {
   __device__ void init() { s0 = c0 = s1 = c1 = 0.0f; n = 0; }
 };
 
+// Float prefilter offset d^2 - mid of a candidate at (dx, dy), in two fused
+// multiply-adds.  A pair is inside when off < -band, outside when off > band,
+// and undecided (left to the reference's FP64 test) otherwise: one value for
+// all three, so the float-inside and undecided sets are disjoint.  Float
+// error is ~1e-7 rho^2, far inside the band of 3e-5 rho^2.
+__device__ __forceinline__ float cutoff_offset(float dx, float dy, float nmid) {
+  return fmaf(dx, dx, fmaf(dy, dy, nmid));
+}
+
 __device__ __forceinline__ void kahan_add(float &sum, float &comp, float v) {
   const float y = v - comp;
   const float t = sum + y;

@@ -127,15 +127,6 @@ __device__ __forceinline__ int split_point(int rcnt, int part, int S) {
   return part >= S ? rcnt : ((rcnt * part / S) & ~31);
 }
 
-// Float prefilter offset d^2 - mid of a candidate at (dx, dy), in two fused
-// multiply-adds.  A pair is inside when off < -band, outside when off > band,
-// and undecided (left to the reference's FP64 test) otherwise: one value for
-// all three, so the float-inside and undecided sets are disjoint.  Float
-// error is ~1e-7 rho^2, far inside the band of 3e-5 rho^2.
-__device__ __forceinline__ float cutoff_offset(float dx, float dy, float nmid) {
-  return fmaf(dx, dx, fmaf(dy, dy, nmid));
-}
-
 // One block of 32 staged candidates against one particle (FP32C).  The block
 // is fully unrolled: bit t of *bits is candidate j0 + t.  SELF: the block may
 // contain the particle itself (staged index `self`).  Pairs the float test

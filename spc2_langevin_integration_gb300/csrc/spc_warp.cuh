@@ -15,10 +15,12 @@
 // FP32C (k_warp_fp32c): the lanes are (particle, candidate group) pairs.  A
 // chunk of g_n particles gets G = 32 / g_n groups; lane l works on particle
 // l % g_n against the candidates j = group, group + G, ... of the staged list,
-// so all lanes are busy even for cells of a few particles.  Each lane keeps a
-// Kahan sum; the groups of one particle are combined in group order through
-// shared memory.  Pass 1 stores each lane's accepted-candidate bits, pass 2
-// walks only those bits.
+// so all lanes are busy even for cells of a few particles.  Each lane sums
+// its accepted candidates' cos phi_j and sin phi_j per word of 32 candidates,
+// turns them into the alignment terms by angle addition, and adds each word's
+// term to a Kahan sum; the groups of one particle are combined in group order
+// through shared memory.  Pass 1 stores each lane's accepted-candidate bits,
+// pass 2 walks only those bits.
 //
 // FP64 (k_warp_fp64): for each particle i in turn the 32 lanes test 32
 // candidates at a time; a ballot gives the neighbour word, the accepted
@@ -92,7 +94,7 @@ __global__ void __launch_bounds__(kWarpPassThreads, 8) k_warp_fp32c(KArgs a, int
     const SysConst &sc = sd.sc;
     if (sc.allpairs) continue;
     const float lo2 = sc.lo2, hi2 = sc.hi2;
-    const float band = 0.5f * (hi2 - lo2), mid = 0.5f * (hi2 + lo2);
+    const float band = 0.5f * (hi2 - lo2), nmid = -0.5f * (hi2 + lo2);
     const bool exact_all = sc.exact_all != 0;
     Stencil st;
     stencil_of(a, sd, c, st);
@@ -132,26 +134,34 @@ __global__ void __launch_bounds__(kWarpPassThreads, 8) k_warp_fp32c(KArgs a, int
               for (int wd = 0; wd < W; ++wd) {
                 uint32_t bits = a.nbmask[(size_t)(g * W + wd) * n_all + pp];
                 pn += __popc(bits);
+                float bc = 0.0f, bs = 0.0f, bdc = 0.0f, bds = 0.0f;
                 while (bits) {
                   const int t = __ffs(bits) - 1;
                   bits &= bits - 1u;
                   const int j = g + (wd * kWarp + t) * G;
                   const float4 cj = sm.c4[j];
-                  const float tv = fmaf(cj.z, cai, cj.w * sai);  // cos(phi_j - phi_i - alpha)
-                  kahan_add(ps0, pc0, tv);
-                  kahan_add(ps1, pc1, (sm.df[j] - dfi) * tv);
+                  const float dj = sm.df[j];
+                  bc += cj.z;
+                  bs += cj.w;
+                  bdc = fmaf(dj, cj.z, bdc);
+                  bds = fmaf(dj, cj.w, bds);
                 }
+                // sum cos(phi_j - phi_i - alpha) and sum (d_j - d_i) cos(...)
+                const float b0 = fmaf(bc, cai, bs * sai);
+                kahan_add(ps0, pc0, b0);
+                kahan_add(ps1, pc1, fmaf(bdc, cai, fmaf(bds, sai, -dfi * b0)));
               }
             }
           } else {
             uint32_t bits = 0u;
             int k = 0;
+            float bc = 0.0f, bs = 0.0f, bdc = 0.0f, bds = 0.0f;  // this word's sums
             for (int j = g; j < rcnt; j += G, ++k) {
               const float4 cj = sm.c4[j];
               const float dx = cj.x - fxi, dy = cj.y - fyi;
-              const float d2 = fmaf(dx, dx, dy * dy);
-              bool in = !exact_all && d2 < lo2;
-              if (exact_all || fabsf(d2 - mid) <= band) {  // rare: the reference's FP64 test
+              const float off = cutoff_offset(dx, dy, nmid);
+              bool in = !exact_all && off < -band;
+              if (exact_all || fabsf(off) <= band) {  // rare: the reference's FP64 test
                 int q;
                 const int pj = slot_of(st, rlo + j, q);
                 in = exact_within(sc, a.sx[pp], a.sy[pp], a.sx[pj], a.sy[pj]);
@@ -159,15 +169,25 @@ __global__ void __launch_bounds__(kWarpPassThreads, 8) k_warp_fp32c(KArgs a, int
               in = in && j != self;
               if (in) {
                 bits |= 1u << (k & (kWarp - 1));
-                if constexpr (KIND == kKindSin) {
-                  kahan_add(ps0, pc0, fmaf(cj.w, cai, -cj.z * sai));  // sin(phi_j - phi_i - alpha)
-                } else {
-                  const float tv = fmaf(cj.z, cai, cj.w * sai);
-                  kahan_add(ps0, pc0, tv);
-                  kahan_add(ps1, pc1, (sm.df[j] - dfi) * tv);
+                bc += cj.z;
+                bs += cj.w;
+                if constexpr (KIND == kKindCos2) {
+                  const float dj = sm.df[j];
+                  bdc = fmaf(dj, cj.z, bdc);
+                  bds = fmaf(dj, cj.w, bds);
                 }
               }
               if ((k & (kWarp - 1)) == kWarp - 1 || j + G >= rcnt) {
+                // the word's alignment terms by angle addition (sin / cos of
+                // phi_j - phi_i - alpha from cos phi_j, sin phi_j)
+                if constexpr (KIND == kKindSin) {
+                  kahan_add(ps0, pc0, fmaf(bs, cai, -bc * sai));
+                } else {
+                  const float b0 = fmaf(bc, cai, bs * sai);
+                  kahan_add(ps0, pc0, b0);
+                  kahan_add(ps1, pc1, fmaf(bdc, cai, fmaf(bds, sai, -dfi * b0)));
+                }
+                bc = bs = bdc = bds = 0.0f;
                 pn += __popc(bits);
                 if (KIND == kKindSin && masked) a.nbmask[(size_t)(g * W + k / kWarp) * n_all + pp] = bits;
                 bits = 0u;
