@@ -659,7 +659,9 @@ def main():
     ap.add_argument("--compare-kernels", action="store_true",
                     help="ensemble: also time every system on the cell-tile passes")
     ap.add_argument("--drift-steps", type=int, default=10000)
-    ap.add_argument("--serve-duration", type=float, default=10.0)
+    ap.add_argument("--serve-duration", type=float, default=2.0,
+                    help="serve: seconds of the Poisson trace served (2 s: 384 requests, a few "
+                         "minutes of device time; the FP64 form takes most of it)")
     ap.add_argument("--serve-rate", type=float, default=200.0)
     args = ap.parse_args()
     if args.workload == "ensemble":

@@ -91,7 +91,7 @@ struct KArgs {
   int *cnt_s;                        // n_i, cell order
   double *va_vx, *va_vy;             // vortex arrays: pass-1 velocity components, cell order
   int *va_cnt2;                      // vortex arrays: cohesion partners, cell order
-  uint32_t *nbmask;                  // FP32C: pass-1 neighbour bitmasks [word][n_active], or null
+  uint32_t *nbmask;                  // FP32C: pass-1 neighbour bitmasks (mask_at), or null
   uint32_t *hist;                    // radix histogram table (zeroed by k_gather)
   int hist_len;
   const int *ap_cells;               // global cells of the all-pairs systems
@@ -241,6 +241,17 @@ struct Acc<kPrecFP32C> {
   int n;
   __device__ void init() { s0 = c0 = s1 = c1 = 0.0f; n = 0; }
 };
+
+// Word w (< 32) of the pass-1 neighbour bitmask of cell-order slot p among n
+// active particles.  Four consecutive words of a particle share one 16-byte
+// group.  The cell-tile and warp-per-cell kernels of one pass write the same
+// buffer for the particles of their own cells, so both must index it this way:
+// distinct (w, p) never share a word.  (The Verlet kernels keep a word-major
+// layout of their own; a Verlet engine holds one system and runs no other
+// neighbour kernel in the pass.)
+__device__ __forceinline__ size_t mask_at(int w, int p, int n) {
+  return ((size_t)(w >> 2) * n + p) * 4 + (w & 3);
+}
 
 // Float prefilter offset d^2 - mid of a candidate at (dx, dy), in two fused
 // multiply-adds.  A pair is inside when off < -band, outside when off > band,

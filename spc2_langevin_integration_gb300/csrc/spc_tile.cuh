@@ -77,15 +77,10 @@ __device__ __forceinline__ float shift_y(int q, float cell_f) { return (float)(q
 // candidate list fits one staging round, each particle's neighbour set as a
 // bitmask over that list; pass 2 (kKindCos2) then walks only the set bits
 // instead of re-testing every candidate.  Cells with more candidates run the
-// filter in pass 2 as well.  Four consecutive words of a particle share one
-// 16-byte group (word w of particle p at nbmask[((w / 4) * n + p) * 4 + w % 4]),
-// so pass 2 fetches the masks of four candidate blocks with one load.
+// filter in pass 2 as well.  The masks are laid out by mask_at, so pass 2
+// fetches the words of four candidate blocks with one 16-byte load.
 constexpr int kMaskWords = kTileCap / 32;
 static_assert(kMaskWords % 4 == 0, "mask words come in groups of four");
-
-__device__ __forceinline__ size_t tile_mask_at(int w, int p, int n) {
-  return ((size_t)(w >> 2) * n + p) * 4 + (w & 3);
-}
 
 // Work item `item` of the cell-tile kernels: cell c = item / K and part
 // item % K of its particles, K = a.tile_split CTAs per cell.  Parts are
@@ -329,7 +324,7 @@ __global__ void __launch_bounds__(kTileThreads32, kTileMinBlocks32) k_tile_fp32c
               kahan_add(S0, C0, b0);
               if constexpr (KIND == kKindCos2) kahan_add(S1, C1, b1);
               if (KIND == kKindSin && masked && valid)
-                a.nbmask[tile_mask_at(j0 / kWarp, p, n_all)] = bits;
+                a.nbmask[mask_at(j0 / kWarp, p, n_all)] = bits;
             }
           }
           if (valid) {

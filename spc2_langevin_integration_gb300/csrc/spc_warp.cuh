@@ -132,7 +132,7 @@ __global__ void __launch_bounds__(kWarpPassThreads, 8) k_warp_fp32c(KArgs a, int
           if (KIND == kKindCos2 && masked) {
             if constexpr (KIND == kKindCos2) {
               for (int wd = 0; wd < W; ++wd) {
-                uint32_t bits = a.nbmask[(size_t)(g * W + wd) * n_all + pp];
+                uint32_t bits = a.nbmask[mask_at(g * W + wd, pp, n_all)];
                 pn += __popc(bits);
                 float bc = 0.0f, bs = 0.0f, bdc = 0.0f, bds = 0.0f;
                 while (bits) {
@@ -189,13 +189,13 @@ __global__ void __launch_bounds__(kWarpPassThreads, 8) k_warp_fp32c(KArgs a, int
                 }
                 bc = bs = bdc = bds = 0.0f;
                 pn += __popc(bits);
-                if (KIND == kKindSin && masked) a.nbmask[(size_t)(g * W + k / kWarp) * n_all + pp] = bits;
+                if (KIND == kKindSin && masked) a.nbmask[mask_at(g * W + k / kWarp, pp, n_all)] = bits;
                 bits = 0u;
               }
             }
             // a group with fewer candidates than group 0 leaves its last words empty
             if (KIND == kKindSin && masked)
-              for (int wd = (k + kWarp - 1) / kWarp; wd < W; ++wd) a.nbmask[(size_t)(g * W + wd) * n_all + pp] = 0u;
+              for (int wd = (k + kWarp - 1) / kWarp; wd < W; ++wd) a.nbmask[mask_at(g * W + wd, pp, n_all)] = 0u;
           }
         }
         // combine the groups of each particle in group order on its owner lane

@@ -14,9 +14,12 @@ from tests._helpers import init_state, periodic_diff
 
 pytestmark = pytest.mark.gpu
 
-# (n, L, params, vortex): uneven sizes, one all-pairs system (rho > L/4)
+# (n, L, params, vortex): uneven sizes, one all-pairs system (rho > L/4), one
+# dense system (~64 per cell: cell-tile passes) beside sparse ones (~6-13 per
+# cell: warp-per-cell passes), so one pass runs both kernels over one mask buffer
 SYSTEMS = [
     (1500, 1.2, dict(v0=0.01, sigma=1.0, rho=0.1, alpha=1.45, D_phi=0.005), False),
+    (4096, 1.0, dict(v0=0.02, sigma=1.5, rho=0.125, alpha=0.5, D_phi=0.01), True),
     (400, 0.6, dict(v0=0.01, sigma=0.7, rho=0.07, alpha=1.3, D_phi=0.012), False),
     (3000, 1.8, dict(v0=0.02, sigma=2.0, rho=0.12, alpha=0.0, D_phi=0.01), True),
     (256, 0.5, dict(v0=0.01, sigma=1.5, rho=0.14, alpha=1.55, D_phi=0.002), False),  # all pairs
