@@ -271,8 +271,12 @@ int dalloc(Engine *e, T **ptr, size_t count) {
 // memory; the attribute is set with the device current (not a stream
 // operation, so never inside a capture).
 inline cudaError_t set_kernel_attributes() {
-  return cudaFuncSetAttribute(k_radix_scatter, cudaFuncAttributeMaxDynamicSharedMemorySize,
+  cudaError_t ce = cudaFuncSetAttribute(k_radix_scatter<1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        (int)scatter_smem_bytes(11));
+  if (ce == cudaSuccess)
+    ce = cudaFuncSetAttribute(k_radix_scatter<4>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                               (int)scatter_smem_bytes(11));
+  return ce;
 }
 
 inline int engine_set_device(Engine *e) {
@@ -700,8 +704,12 @@ inline int eval_cells(Engine *e, KArgs &a, int rk_form, int kq, double kcdt, boo
       k_scan_digits<<<1, kScanThreads, 0, st>>>(e->part, ng, bits, a.gate);
       k_scan_group_apply<<<grid, 256, 0, st>>>(e->hist, e->ntiles, bits, e->part, a.gate);
     }
-    k_radix_scatter<<<e->ntiles, kSortThreads, scatter_smem_bytes(bits), st>>>(kin, vin, kout, vout, n,
-                                                                               shift, bits, e->hist, a.gate);
+    if (e->ntiles < kScatterSplitBelow)
+      k_radix_scatter<4><<<e->ntiles * 4, kSortThreads, scatter_smem_bytes(bits), st>>>(
+          kin, vin, kout, vout, n, shift, bits, e->hist, a.gate);
+    else
+      k_radix_scatter<1><<<e->ntiles, kSortThreads, scatter_smem_bytes(bits), st>>>(
+          kin, vin, kout, vout, n, shift, bits, e->hist, a.gate);
     SPC_LAUNCHED(e);
     std::swap(kin, kout);
     std::swap(vin, vout);

@@ -189,26 +189,43 @@ __global__ void k_scan_group_apply(uint32_t *__restrict__ hist, int ntiles, int 
 }
 
 // Stable scatter of one digit pass; hist_scanned is the output of k_scan_digits.
+// Each sort tile (kSortTile keys, one row of the digit table) is scattered by
+// SUB CTAs of kSortTile / SUB keys, so that a small system still fills the
+// GPU (SUB = 4 below kScatterSplitBelow tiles, else 1): a CTA starts from its
+// tile's digit bases, adds the digit counts of the tile's earlier parts
+// (shared-memory atomics: counts do not depend on their order), and ranks its
+// own keys in element order, so the scatter is stable.
+constexpr int kScatterSplitBelow = 2 * 152;
+
+template <int SUB>
 __global__ void __launch_bounds__(kSortThreads)
     k_radix_scatter(const uint32_t *__restrict__ keys_in, const uint32_t *__restrict__ vals_in,
                     uint32_t *__restrict__ keys_out, uint32_t *__restrict__ vals_out, int n,
                     int shift, int bits, const uint32_t *__restrict__ hist_scanned, const int *gate) {
+  constexpr int kScatterKeys = kSortTile / SUB;
+  constexpr int kScatterItems = kScatterKeys / kSortThreads;
+  static_assert(kScatterItems * kSortThreads * SUB == kSortTile, "scatter parts tile the sort tile");
   if (gate && *gate == 0) return;
+  const int tile = blockIdx.x / SUB, part = blockIdx.x % SUB;
+  const int t0 = tile * kSortTile, p0 = t0 + part * kScatterKeys;
+  if (p0 >= n) return;  // a part past the end of the last tile
   extern __shared__ uint32_t smem_sort[];
   const int R = 1 << bits;
-  uint32_t *wcount = smem_sort;                      // [kSortWarps][R]
-  uint32_t *tile_base_of_digit = smem_sort + kSortWarps * R;
+  uint32_t *wcount = smem_sort;                         // [kSortWarps][R]
+  uint32_t *digit_base = smem_sort + kSortWarps * R;    // first output slot of each digit
   const int warp = threadIdx.x / kWarp, lane = threadIdx.x % kWarp;
   for (int d = threadIdx.x; d < kSortWarps * R; d += blockDim.x) smem_sort[d] = 0;
-  for (int d = threadIdx.x; d < R; d += blockDim.x)
-    tile_base_of_digit[d] = hist_scanned[(size_t)blockIdx.x * R + d];
+  for (int d = threadIdx.x; d < R; d += blockDim.x) digit_base[d] = hist_scanned[(size_t)tile * R + d];
+  __syncthreads();
+  for (int idx = t0 + threadIdx.x; idx < p0; idx += blockDim.x)  // the tile's earlier parts
+    atomicAdd(&digit_base[(keys_in[idx] >> shift) & (R - 1)], 1u);
   __syncthreads();
 
-  const int base = blockIdx.x * kSortTile + warp * (kSortItems * kWarp);
+  const int base = p0 + warp * (kScatterItems * kWarp);
   const unsigned lanes_below = (1u << lane) - 1u;
-  uint32_t key[kSortItems], val[kSortItems], rank[kSortItems];
+  uint32_t key[kScatterItems], val[kScatterItems], rank[kScatterItems];
 #pragma unroll
-  for (int it = 0; it < kSortItems; ++it) {
+  for (int it = 0; it < kScatterItems; ++it) {
     const int idx = base + it * kWarp + lane;
     const bool valid = idx < n;
     key[it] = valid ? keys_in[idx] : 0u;
@@ -236,10 +253,10 @@ __global__ void __launch_bounds__(kSortThreads)
   }
   __syncthreads();
 #pragma unroll
-  for (int it = 0; it < kSortItems; ++it) {
+  for (int it = 0; it < kScatterItems; ++it) {
     if (rank[it] == 0xffffffffu) continue;
     const uint32_t d = (key[it] >> shift) & (R - 1);
-    const uint32_t pos = tile_base_of_digit[d] + wcount[warp * R + d] + rank[it];
+    const uint32_t pos = digit_base[d] + wcount[warp * R + d] + rank[it];
     keys_out[pos] = key[it];
     vals_out[pos] = val[it];
   }

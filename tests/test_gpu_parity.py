@@ -366,3 +366,19 @@ def test_tile_split_knob_validation():
                 s.set_tuning(abi.TUNE_TILE_SPLIT, bad)
         s.set_tuning(abi.TUNE_TILE_SPLIT, 3)
         assert s.get_tuning(abi.TUNE_TILE_SPLIT) == 3.0
+
+
+@pytest.mark.parametrize("n,L,rho", [(20000, 8.0, 0.1), (3000, 3.0, 0.05)])
+def test_two_pass_sort_neighbour_lists_match_oracle(n, L, rho):
+    # more than 2048 cells: the radix sort takes two 8-bit passes, each
+    # scattered by several CTAs per sort tile (few tiles); the neighbour lists
+    # in the reference's visiting order must come out exactly
+    prm = dict(v0=0.01, sigma=1.0, rho=rho, alpha=1.45, D_phi=0.005)
+    st = init_state(n, L, 55)
+    assert abi.cells_of(L, rho) > 2048
+    with gpu(n, L, prm, abi.STEPPER_EULER) as s:
+        s.upload_state(st)
+        off, idx = s.neighbours()
+    o = po.OracleSystem(n, L, **prm)
+    off_ref, idx_ref = o.neighbour_lists(st)
+    assert np.array_equal(off, off_ref) and np.array_equal(idx, idx_ref)
