@@ -556,7 +556,14 @@ def tune_form(abi, w, precision, rank=0):
 def run_form(abi, torch, w, precision, steps, warmup, rank, dist, params=None, sparse_below=None,
              e2e=True, tile_split=None):
     """Device-timed graph replays of the workload; then (e2e) the same through
-    the C-ABI with host buffers, and a per-phase profile."""
+    the C-ABI with host buffers, and a per-phase profile.
+
+    The cost of a step grows as the vortex system clusters (denser cells, more
+    pairs), so every timed replay, device-timed and end-to-end alike, starts
+    from the same warm state: the state after the warm-up replays, kept in
+    pinned host memory.  Its upload is outside the CUDA events of the
+    device-timed replays and inside the end-to-end timing."""
+    import ctypes as C
     n = w["n"]
     st, omega = init_inputs(w, seed_offset=rank)
     p = params if params is not None else workload_params(abi, w, precision, rank)
@@ -573,12 +580,19 @@ def run_form(abi, torch, w, precision, steps, warmup, rank, dist, params=None, s
     for _ in range(warmup):
         s.step(dt, SIM_STEPS_PER_BENCH_STEP, graph=True)
     s.synchronize()
+    L = abi.lib()
+    ptrs = [C.c_void_p(), C.c_void_p()]
+    for q in ptrs:
+        L.spc_alloc_pinned(3 * n * 8, C.byref(q))
+    warm, host = [np.ctypeslib.as_array((C.c_double * (3 * n)).from_address(q.value)) for q in ptrs]
+    warm[:] = s.download_state()
     ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
           for _ in range(steps)]
     if dist is not None:
         dist.barrier()
     torch.cuda.synchronize()
     for k in range(steps):
+        s.upload_state(warm)
         flush.zero_()
         torch.cuda.synchronize()
         ev[k][0].record(stream)
@@ -590,31 +604,26 @@ def run_form(abi, torch, w, precision, steps, warmup, rank, dist, params=None, s
     ms = sum(a.elapsed_time(b) for a, b in ev)
     ms = reduce_max(dist, ms)
     launches = s.graph_nodes() * steps  # one graph replay per bench step
-    if not e2e:
-        prof = s.profile_steps(dt, 20)
-        s.close()
-        return ms, None, prof, None, launches
-    # e2e through the C-ABI with host buffers: pinned upload, 100 steps, download
-    import ctypes as C
-    L = abi.lib()
-    ptr = C.c_void_p()
-    L.spc_alloc_pinned(3 * n * 8, C.byref(ptr))
-    host = np.ctypeslib.as_array((C.c_double * (3 * n)).from_address(ptr.value))
-    host[:] = s.download_state()
-    e2e_ms = 0.0
-    for k in range(steps):
-        flush.zero_()
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        s.upload_state(host)
-        s.step(dt, SIM_STEPS_PER_BENCH_STEP, graph=True)
-        s.download_state(host)
-        e2e_ms += (time.perf_counter() - t0) * 1e3
-    e2e_ms = reduce_max(dist, e2e_ms)
+    e2e_ms, R = None, None
+    if e2e:
+        # e2e through the C-ABI with host buffers: pinned upload, 100 steps, download
+        e2e_ms = 0.0
+        for k in range(steps):
+            flush.zero_()
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            s.upload_state(warm)
+            s.step(dt, SIM_STEPS_PER_BENCH_STEP, graph=True)
+            s.download_state(host)
+            e2e_ms += (time.perf_counter() - t0) * 1e3
+        e2e_ms = reduce_max(dist, e2e_ms)
+    s.upload_state(warm)
     prof = s.profile_steps(dt, 20)
-    R = s.order_params()
-    del host
-    L.spc_free_pinned(ptr)
+    if e2e:
+        R = s.order_params()
+    del warm, host
+    for q in ptrs:
+        L.spc_free_pinned(q)
     s.close()
     return ms, e2e_ms, prof, R, launches
 
@@ -789,6 +798,10 @@ def main():
               "neighbour": "autotuned per precision (cell list or Verlet rows; see autotune)",
               "dt": w["dt"], "sim_steps_per_bench_step": SIM_STEPS_PER_BENCH_STEP,
               "l2": "flushed between bench steps (512 MB write, outside the timed events)",
+              "start_state": "every timed replay starts from the state after the warm-up "
+                             "replays (uploaded from pinned host memory: outside the CUDA events "
+                             "for value, inside the timing for e2e); a step's cost grows as the "
+                             "system clusters",
               "parallelism": f"replicas{world}"}
 
     if args.impl == "reference":
