@@ -252,6 +252,14 @@ void *spc_stream(spc_handle *h);
  * draw), for checking against the published known-answer vectors. */
 int spc_philox4x32_10(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]);
 
+/* Self-check of the FP64 kernels' division by a reused divisor (no reference
+ * counterpart): for i < n, a[i] / b[i] on the device both as the correctly
+ * rounded division and as the kernels' form (reciprocal rounded to nearest,
+ * then one fused multiply-add correction); *mismatches counts the pairs
+ * whose results differ in any bit (0 means the FP64 forms divide exactly as
+ * the reference writes it). */
+int spc_check_division(int64_t n, const double *a, const double *b, int64_t *mismatches);
+
 /* ---------------------------------------------------------------------------
  * Batches: many independent systems (each with its own N, box and
  * parameters) resident in one pool of device memory and advanced together,

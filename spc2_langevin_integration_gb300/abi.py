@@ -138,10 +138,27 @@ def lib() -> C.CDLL:
     L.spc_run.argtypes = [H, dp, C.c_double, C.c_int64, C.c_int32, C.c_void_p, OBSERVE_FN,
                           C.c_void_p, C.POINTER(C.c_int64)]
     L.spc_run_graph_nodes.argtypes = [H, C.POINTER(C.c_int64), C.POINTER(C.c_int32)]
+    L.spc_check_division.argtypes = [C.c_int64, C.c_void_p, C.c_void_p, C.POINTER(C.c_int64)]
     L.spc_alloc_pinned.argtypes = [C.c_size_t, C.POINTER(C.c_void_p)]
     L.spc_free_pinned.argtypes = [C.c_void_p]
     _lib = L
     return L
+
+
+def check_division(a, b) -> int:
+    """Pairs (a[i], b[i]) whose quotient differs in any bit between the
+    correctly rounded division and the FP64 kernels' reciprocal form, on the
+    device (spc_check_division)."""
+    a = np.ascontiguousarray(a, np.float64)
+    b = np.ascontiguousarray(b, np.float64)
+    if a.shape != b.shape:
+        raise ValueError("a and b differ in shape")
+    bad = C.c_int64()
+    L = lib()
+    rc = L.spc_check_division(a.size, _ptr(a), _ptr(b), C.byref(bad))
+    if rc != 0:
+        raise SpcError(rc, L.spc_last_error(None).decode())
+    return bad.value
 
 
 # int (*)(void *user, int64_t step, double t, const double *aos3n)

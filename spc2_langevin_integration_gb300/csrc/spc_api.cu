@@ -743,6 +743,32 @@ int spc_philox4x32_10(const uint32_t ctr[4], const uint32_t key[2], uint32_t out
   return SPC_OK;
 }
 
+int spc_check_division(int64_t n, const double *a, const double *b, int64_t *mismatches) {
+  if (!a || !b || !mismatches || n < 0) return fail(nullptr, SPC_ERR_INVALID, "bad argument");
+  *mismatches = 0;
+  if (n == 0) return SPC_OK;
+  double *da = nullptr, *db = nullptr;
+  unsigned long long *dbad = nullptr;
+  cudaError_t e = cudaMalloc(&da, (size_t)n * 8);
+  if (e == cudaSuccess) e = cudaMalloc(&db, (size_t)n * 8);
+  if (e == cudaSuccess) e = cudaMalloc(&dbad, 8);
+  if (e == cudaSuccess) e = cudaMemcpy(da, a, (size_t)n * 8, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(db, b, (size_t)n * 8, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemset(dbad, 0, 8);
+  if (e == cudaSuccess) {
+    k_check_division<<<152 * 8, 256>>>(n, da, db, dbad);
+    e = cudaGetLastError();
+  }
+  unsigned long long bad = 0;
+  if (e == cudaSuccess) e = cudaMemcpy(&bad, dbad, 8, cudaMemcpyDeviceToHost);
+  cudaFree(da);
+  cudaFree(db);
+  cudaFree(dbad);
+  if (e != cudaSuccess) return fail(nullptr, SPC_ERR_CUDA, "check_division: %s", cudaGetErrorString(e));
+  *mismatches = (int64_t)bad;
+  return SPC_OK;
+}
+
 int spc_alloc_pinned(size_t bytes, void **out) {
   if (!out) return fail(nullptr, SPC_ERR_INVALID, "NULL argument");
   cudaError_t e = cudaMallocHost(out, bytes);

@@ -16,6 +16,23 @@ __device__ __forceinline__ double dadd(double a, double b) { return __dadd_rn(a,
 __device__ __forceinline__ double dsub(double a, double b) { return __dsub_rn(a, b); }
 __device__ __forceinline__ double dmul(double a, double b) { return __dmul_rn(a, b); }
 __device__ __forceinline__ double ddiv(double a, double b) { return __ddiv_rn(a, b); }
+
+// a / b rounded to nearest, for a divisor b used many times, from its
+// reciprocal y = RN(1 / b) computed once: q = RN(a y) is within an ulp of
+// a / b, the remainder a - q b is exact in one fused multiply-add, and
+// RN(q + (a - q b) y) = RN(a / b) (the final correction step of
+// Newton-Raphson division, P. Markstein, "Computation of elementary functions
+// on the IBM RISC System/6000 processor", IBM J. Res. Dev. 34(1), 1990).
+// Bitwise equal to ddiv(a, b) for the finite nonzero divisors of these
+// kernels (spc_check_division checks it on the device); it replaces two
+// correctly rounded divisions per pair by a multiply and two fused
+// multiply-adds on the FP64 pipe.
+__device__ __forceinline__ double ddiv_by(double a, double b, double y) {
+  const double q = __dmul_rn(a, y);
+  const double r = __fma_rn(-q, b, a);
+  return __fma_rn(r, y, q);
+}
+__device__ __forceinline__ double drcp(double b) { return __drcp_rn(b); }
 __device__ __forceinline__ double dsqrt(double a) { return __dsqrt_rn(a); }
 
 // Per-system constants, the reference's ChimeraSystem / PeriodicBoundaryConditions
@@ -43,6 +60,9 @@ struct SysConst {
   int va;
   double mu_plus, mu_minus, xi_a, xi_r, kappa;
   float va_r2;    // float dr^2 above this: beyond rho and xi_r for certain
+  // vortex arrays: w = rho - xi_a and xi_a^2 as the model computes them, and
+  // the reciprocals of w, xi_a and xi_a^2 rounded to nearest (ddiv_by)
+  double va_w, va_xa2, va_rw, va_rxa, va_rxa2;
 };
 
 // PeriodicBoundaryConditions::ClassAEffectiveParticleDistance (PeriodicBoundaryConditions.cpp:22-35):

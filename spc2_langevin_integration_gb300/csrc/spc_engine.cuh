@@ -92,6 +92,12 @@ inline SysConst make_sysconst(const spc_params &p, int n) {
     sc.kappa = p.kappa;
     const double rm = std::max(p.rho, p.xi_r);
     sc.va_r2 = (float)(rm * rm * (1.0 + 3e-5));
+    // IEEE double arithmetic on the host: the same roundings as the device's
+    sc.va_w = p.rho - p.xi_a;
+    sc.va_xa2 = p.xi_a * p.xi_a;
+    sc.va_rw = 1.0 / sc.va_w;
+    sc.va_rxa = 1.0 / p.xi_a;
+    sc.va_rxa2 = 1.0 / sc.va_xa2;
   }
   // Verlet rows over a (2R+1)^2 stencil of rho-cells; needs 2R+1 distinct cells
   if (p.neighbour == SPC_NEIGHBOUR_VERLET && !sc.allpairs && !sc.va) {

@@ -277,6 +277,7 @@ struct ILane {
   double x, y;  // wrapped stage position
   double phi;   // stage phase
   double card;  // pass 2: n_i from pass 1 (double, as neighborhood_cardinality_)
+  double rcard; // pass 2: 1 / n_i rounded to nearest (ddiv_by)
   double dphi;  // pass 2: own phase rate
   float ca, sa; // FP32C: cos(phi + alpha), sin(phi + alpha)
   float dphif;
@@ -300,8 +301,8 @@ __device__ __forceinline__ void accept_pair(const KArgs &a, const SysDesc &sd, c
     if constexpr (PREC == kPrecFP64) {
       // ChimeraSystem.cpp:634-637
       const double c = cos(dsub(dsub(a.sphi[pj], il.phi), sc.alpha));
-      acc.s0 = dadd(acc.s0, ddiv(c, il.card));
-      acc.s1 = dadd(acc.s1, ddiv(dmul(dsub(a.dphi_s[pj], il.dphi), c), il.card));
+      acc.s0 = dadd(acc.s0, ddiv_by(c, il.card, il.rcard));
+      acc.s1 = dadd(acc.s1, ddiv_by(dmul(dsub(a.dphi_s[pj], il.dphi), c), il.card, il.rcard));
     } else {
       const float c = cjc * il.ca + cjs * il.sa;
       kahan_add(acc.s0, acc.c0, c);
@@ -530,6 +531,7 @@ __device__ __forceinline__ void load_i(const KArgs &a, const SysConst &sc, ILane
   }
   if constexpr (KIND == kKindCos2) {
     il.card = (double)a.cnt_s[p];
+    il.rcard = drcp(il.card);  // unused (and infinite) when n_i = 0: no pairs
     il.dphi = a.dphi_s[p];
     if constexpr (PREC == kPrecFP32C) il.dphif = a.dphi_f[p];
   } else {
@@ -736,6 +738,18 @@ __global__ void k_export_noise(uint64_t seed, uint32_t system_id, uint64_t first
   double *o = out + ((size_t)s * n + i) * m;
   o[0] = z0;
   if (m > 1) o[1] = z1;
+}
+
+// a[i] / b[i] as ddiv and as ddiv_by with the reciprocal; counts the pairs
+// whose results differ in any bit (spc_check_division).
+__global__ void k_check_division(long long n, const double *__restrict__ a, const double *__restrict__ b,
+                                 unsigned long long *bad) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x) {
+    const double x = a[i], d = b[i];
+    const double q0 = ddiv(x, d), q1 = ddiv_by(x, d, drcp(d));
+    if (__double_as_longlong(q0) != __double_as_longlong(q1)) atomicAdd(bad, 1ull);
+  }
 }
 
 __global__ void k_philox_kat(U4 c, uint32_t k0, uint32_t k1, uint32_t *out) {

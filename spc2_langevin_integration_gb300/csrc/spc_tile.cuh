@@ -401,7 +401,7 @@ __global__ void __launch_bounds__(kTileThreads64) k_tile_fp64(KArgs a, int epi) 
       if (!valid) {
         il.fx = il.fy = 3.0e30f;
         il.x = il.y = il.phi = il.dphi = 0.0;
-        il.card = 1.0;
+        il.card = il.rcard = 1.0;
       }
       Acc<kPrecFP64> acc;
       acc.init();
@@ -428,8 +428,8 @@ __global__ void __launch_bounds__(kTileThreads64) k_tile_fp64(KArgs a, int epi) 
             acc.s0 = dadd(acc.s0, sin(dphi_));  // ChimeraSystem.cpp:412
           } else {
             const double cc = cos(dphi_);      // ChimeraSystem.cpp:634-637
-            acc.s0 = dadd(acc.s0, ddiv(cc, il.card));
-            acc.s1 = dadd(acc.s1, ddiv(dmul(dsub(s_d[j], il.dphi), cc), il.card));
+            acc.s0 = dadd(acc.s0, ddiv_by(cc, il.card, il.rcard));
+            acc.s1 = dadd(acc.s1, ddiv_by(dmul(dsub(s_d[j], il.dphi), cc), il.card, il.rcard));
           }
         };
         for (int j0 = 0; j0 < rcnt; j0 += kWarp) {

@@ -23,22 +23,26 @@ namespace spc {
 constexpr int kVAThreads = 64;
 constexpr int kVACap = 512;  // candidates staged per round
 
-// AlignmentStrength (VortexArraysSystemPtr.cpp:737-749)
+// AlignmentStrength (VortexArraysSystemPtr.cpp:737-749); the divisions by
+// the constants xi_a^2 and w = rho - xi_a use their precomputed reciprocals
+// (ddiv_by: the same correctly rounded quotients)
 __device__ __forceinline__ double va_strength(const SysConst &sc, double r) {
-  if (r < sc.xi_a) return dmul(sc.mu_plus, dsub(1.0, ddiv(dmul(r, r), dmul(sc.xi_a, sc.xi_a))));
+  if (r < sc.xi_a) return dmul(sc.mu_plus, dsub(1.0, ddiv_by(dmul(r, r), sc.va_xa2, sc.va_rxa2)));
   if (r < sc.rho) {
-    const double w = dsub(sc.rho, sc.xi_a);
-    return ddiv(ddiv(dmul(dmul(dmul(-sc.mu_minus, 4.0), dsub(r, sc.xi_a)), dsub(sc.rho, r)), w), w);
+    const double w = sc.va_w, rw = sc.va_rw;
+    return ddiv_by(ddiv_by(dmul(dmul(dmul(-sc.mu_minus, 4.0), dsub(r, sc.xi_a)), dsub(sc.rho, r)), w, rw), w, rw);
   }
   return 0.0;
 }
 
 // AlignmentStrengthDerivative (VortexArraysSystemPtr.cpp:751-763)
 __device__ __forceinline__ double va_strength_derivative(const SysConst &sc, double r) {
-  if (r < sc.xi_a) return dmul(sc.mu_plus, ddiv(ddiv(dmul(-2.0, r), sc.xi_a), sc.xi_a));
+  if (r < sc.xi_a)
+    return dmul(sc.mu_plus, ddiv_by(ddiv_by(dmul(-2.0, r), sc.xi_a, sc.va_rxa), sc.xi_a, sc.va_rxa));
   if (r < sc.rho) {
-    const double w = dsub(sc.rho, sc.xi_a);
-    return ddiv(ddiv(dmul(dmul(-sc.mu_minus, 4.0), dadd(dadd(dmul(-2.0, r), sc.rho), sc.xi_a)), w), w);
+    const double w = sc.va_w, rw = sc.va_rw;
+    return ddiv_by(ddiv_by(dmul(dmul(-sc.mu_minus, 4.0), dadd(dadd(dmul(-2.0, r), sc.rho), sc.xi_a)), w, rw),
+                   w, rw);
   }
   return 0.0;
 }
@@ -180,7 +184,7 @@ __global__ void __launch_bounds__(kVAThreads) k_va_pass(KArgs a, int epi) {
       const bool valid = p < ce;
       double xi = 0.0, yi = 0.0, phii = 0.0;
       float fx = 0.0f, fy = 0.0f;
-      double vxi = 0.0, vyi = 0.0, ddi = 0.0, norm1 = 0.0, norm2 = 0.0;
+      double vxi = 0.0, vyi = 0.0, ddi = 0.0, norm1 = 0.0, norm2 = 0.0, rn1 = 1.0, rn2 = 1.0;
       if (valid) {
         xi = a.sx[p];
         yi = a.sy[p];
@@ -196,6 +200,8 @@ __global__ void __launch_bounds__(kVAThreads) k_va_pass(KArgs a, int epi) {
           ddi = a.dphi_s[p];
           norm1 = (double)a.cnt_s[p];   // neighborhood_cardinality_[i][0] + [i][1]
           norm2 = (double)a.va_cnt2[p]; // neighborhood_cardinality_[i][2]
+          rn1 = drcp(norm1);            // used only when norm1 > 0 (ddiv_by)
+          rn2 = drcp(norm2);
         }
       }
       const int self = (ap ? 0 : st.prefix[4]) + (p - cb);
@@ -253,24 +259,27 @@ __global__ void __launch_bounds__(kVAThreads) k_va_pass(KArgs a, int epi) {
             if ((dr <= sc.rho) && (norm1 > 0.0)) {
               const double cp = cos(dsub(phij, phii)), sp = sin(dsub(phij, phii));
               const double as = va_strength(sc, dr), asd = va_strength_derivative(sc, dr);
-              r.a0 = dadd(r.a0, ddiv(dmul(-as, cp), norm1));
-              const double gx = ddiv(dmul(dmul(dsub(sm.vx[j], vxi), asd), dx), dr);
-              const double gy = ddiv(dmul(dmul(dsub(sm.vy[j], vyi), asd), dy), dr);
-              const double t1 = ddiv(dmul(dadd(gx, gy), sp), norm1);
-              const double t2 = ddiv(dmul(dmul(dsub(sm.dd[j], ddi), as), cp), norm1);
-              const double t3 = ddiv(dmul(dmul(dmul(2.0, sc.D), sp), as), norm1);
+              // every quotient by norm1 or dr as ddiv would give it (ddiv_by)
+              const double rdr = drcp(dr);
+              r.a0 = dadd(r.a0, ddiv_by(dmul(-as, cp), norm1, rn1));
+              const double gx = ddiv_by(dmul(dmul(dsub(sm.vx[j], vxi), asd), dx), dr, rdr);
+              const double gy = ddiv_by(dmul(dmul(dsub(sm.vy[j], vyi), asd), dy), dr, rdr);
+              const double t1 = ddiv_by(dmul(dadd(gx, gy), sp), norm1, rn1);
+              const double t2 = ddiv_by(dmul(dmul(dsub(sm.dd[j], ddi), as), cp), norm1, rn1);
+              const double t3 = ddiv_by(dmul(dmul(dmul(2.0, sc.D), sp), as), norm1, rn1);
               r.a1 = dadd(r.a1, dsub(dadd(t1, t2), t3));
             }
             if ((dr <= sc.xi_r) && (norm2 > 0.0)) {
               const double th = atan2(dy, dx);
               const double cq = cos(dsub(th, phii)), sq = sin(dsub(th, phii));
-              r.a0 = dadd(r.a0, ddiv(dmul(sc.kappa, cq), norm2));
+              const double rdr = drcp(dr);
+              r.a0 = dadd(r.a0, ddiv_by(dmul(sc.kappa, cq), norm2, rn2));
               const double inner =
-                  dsub(dadd(ddiv(ddiv(dmul(dsub(sm.vx[j], vxi), -dy), dr), dr),
-                            ddiv(ddiv(dmul(dsub(sm.vy[j], vyi), dx), dr), dr)),
+                  dsub(dadd(ddiv_by(ddiv_by(dmul(dsub(sm.vx[j], vxi), -dy), dr, rdr), dr, rdr),
+                            ddiv_by(ddiv_by(dmul(dsub(sm.vy[j], vyi), dx), dr, rdr), dr, rdr)),
                        ddi);
-              const double u1 = ddiv(dmul(dmul(-sc.kappa, inner), cq), norm2);
-              const double u2 = ddiv(dmul(dmul(sc.kappa, sc.D), sq), norm2);
+              const double u1 = ddiv_by(dmul(dmul(-sc.kappa, inner), cq), norm2, rn2);
+              const double u2 = ddiv_by(dmul(dmul(sc.kappa, sc.D), sq), norm2, rn2);
               r.a1 = dadd(r.a1, dadd(u1, u2));
             }
           }

@@ -333,8 +333,8 @@ __global__ void __launch_bounds__(kVThreads) k_vtile(KArgs a, int epi) {
               acc.s0 = dadd(acc.s0, sin(dp));  // ChimeraSystem.cpp:412
             } else {
               const double cc = cos(dp);  // ChimeraSystem.cpp:634-637
-              acc.s0 = dadd(acc.s0, ddiv(cc, il.card));
-              acc.s1 = dadd(acc.s1, ddiv(dmul(dsub(sm.dd[j], il.dphi), cc), il.card));
+              acc.s0 = dadd(acc.s0, ddiv_by(cc, il.card, il.rcard));
+              acc.s1 = dadd(acc.s1, ddiv_by(dmul(dsub(sm.dd[j], il.dphi), cc), il.card, il.rcard));
             }
           }
           bits |= 1u << (k & (kWarp - 1));
@@ -413,8 +413,8 @@ __global__ void __launch_bounds__(kVThreads) k_vtile(KArgs a, int epi) {
                       acc.s0 = dadd(acc.s0, sin(dp));  // ChimeraSystem.cpp:412
                     } else {
                       const double cc = cos(dp);  // ChimeraSystem.cpp:634-637
-                      acc.s0 = dadd(acc.s0, ddiv(cc, il.card));
-                      acc.s1 = dadd(acc.s1, ddiv(dmul(dsub(sm.dd[j], il.dphi), cc), il.card));
+                      acc.s0 = dadd(acc.s0, ddiv_by(cc, il.card, il.rcard));
+                      acc.s1 = dadd(acc.s1, ddiv_by(dmul(dsub(sm.dd[j], il.dphi), cc), il.card, il.rcard));
                     }
                   }
                   bits |= 1u << (kk & (kWarp - 1));

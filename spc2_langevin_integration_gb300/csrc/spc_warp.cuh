@@ -66,7 +66,7 @@ __device__ __forceinline__ void stage_round(const KArgs &a, const SysConst &sc, 
 __device__ __forceinline__ void invalid_lane(ILane &il) {
   il.fx = il.fy = 3.0e30f;
   il.x = il.y = il.phi = il.dphi = 0.0;
-  il.card = 1.0;
+  il.card = il.rcard = 1.0;
   il.ca = il.sa = il.dphif = 0.0f;
 }
 
@@ -282,6 +282,7 @@ __global__ void __launch_bounds__(kWarpPassThreads) k_warp_fp64(KArgs a, int epi
           const int self = st.prefix[4] + (ib - cb) + i - rlo;  // staged index of i (may be outside)
           const double phii = __shfl_sync(FULL, il.phi, i);
           const double cardi = KIND == kKindCos2 ? __shfl_sync(FULL, il.card, i) : 1.0;
+          const double rcardi = KIND == kKindCos2 ? __shfl_sync(FULL, il.rcard, i) : 1.0;
           const double dphii = KIND == kKindCos2 ? __shfl_sync(FULL, il.dphi, i) : 0.0;
           int n_i = 0, nacc = 0;
           // evaluate the first cnt listed candidates (one per lane) and add
@@ -295,8 +296,8 @@ __global__ void __launch_bounds__(kWarpPassThreads) k_warp_fp64(KArgs a, int epi
                 v0 = sin(dp);  // ChimeraSystem.cpp:412
               } else {
                 const double cc = cos(dp);  // ChimeraSystem.cpp:634-637
-                v0 = ddiv(cc, cardi);
-                v1 = ddiv(dmul(dsub(sm.dd[jj], dphii), cc), cardi);
+                v0 = ddiv_by(cc, cardi, rcardi);
+                v1 = ddiv_by(dmul(dsub(sm.dd[jj], dphii), cc), cardi, rcardi);
               }
             }
             for (int k = 0; k < cnt; ++k) {

@@ -382,3 +382,24 @@ def test_two_pass_sort_neighbour_lists_match_oracle(n, L, rho):
     o = po.OracleSystem(n, L, **prm)
     off_ref, idx_ref = o.neighbour_lists(st)
     assert np.array_equal(off, off_ref) and np.array_equal(idx, idx_ref)
+
+
+def test_fp64_division_by_reciprocal_is_bitwise():
+    # the FP64 kernels divide by reused divisors (n_i, pair distances, the
+    # vortex-arrays constants) through a rounded reciprocal and one fused
+    # multiply-add correction; it must give every bit of the correctly
+    # rounded quotient
+    rng = np.random.default_rng(56)
+    m = 4_000_000
+    mant = 1.0 + rng.random(m)
+    a = np.ldexp(mant, rng.integers(-40, 40, m)) * rng.choice([-1.0, 1.0], m)
+    b = np.concatenate([
+        rng.integers(1, 5000, m // 4).astype(np.float64),              # neighbour counts
+        rng.uniform(1e-6, 0.3, m // 4),                                 # pair distances
+        np.ldexp(1.0 + rng.random(m // 4), rng.integers(-20, 20, m // 4)),
+        # significands near all ones
+        np.ldexp(2.0 - np.ldexp(rng.integers(1, 256, m // 4).astype(np.float64), -52),
+                 rng.integers(-8, 8, m // 4)),
+    ])
+    assert abi.check_division(a, b) == 0
+    assert abi.check_division(np.zeros(0), np.zeros(0)) == 0
