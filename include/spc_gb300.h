@@ -260,6 +260,13 @@ int spc_philox4x32_10(const uint32_t ctr[4], const uint32_t key[2], uint32_t out
  * the reference writes it). */
 int spc_check_division(int64_t n, const double *a, const double *b, int64_t *mismatches);
 
+/* Self-check of the FP64 Verlet passes' cosine cache (no reference
+ * counterpart): for i < n, sin(x[i]) and cos(x[i]) from separate launches
+ * against one sincos(x[i]); *mismatches counts the values whose results
+ * differ in any bit (0 means the cached cosine of the first pass is the
+ * cosine the second pass would compute). */
+int spc_check_sincos(int64_t n, const double *x, int64_t *mismatches);
+
 /* ---------------------------------------------------------------------------
  * Batches: many independent systems (each with its own N, box and
  * parameters) resident in one pool of device memory and advanced together,

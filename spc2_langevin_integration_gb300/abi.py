@@ -139,6 +139,7 @@ def lib() -> C.CDLL:
                           C.c_void_p, C.POINTER(C.c_int64)]
     L.spc_run_graph_nodes.argtypes = [H, C.POINTER(C.c_int64), C.POINTER(C.c_int32)]
     L.spc_check_division.argtypes = [C.c_int64, C.c_void_p, C.c_void_p, C.POINTER(C.c_int64)]
+    L.spc_check_sincos.argtypes = [C.c_int64, C.c_void_p, C.POINTER(C.c_int64)]
     L.spc_alloc_pinned.argtypes = [C.c_size_t, C.POINTER(C.c_void_p)]
     L.spc_free_pinned.argtypes = [C.c_void_p]
     _lib = L
@@ -156,6 +157,18 @@ def check_division(a, b) -> int:
     bad = C.c_int64()
     L = lib()
     rc = L.spc_check_division(a.size, _ptr(a), _ptr(b), C.byref(bad))
+    if rc != 0:
+        raise SpcError(rc, L.spc_last_error(None).decode())
+    return bad.value
+
+
+def check_sincos(x) -> int:
+    """Values whose sin / cos from separate launches differ in any bit from
+    one sincos, on the device (spc_check_sincos)."""
+    x = np.ascontiguousarray(x, np.float64)
+    bad = C.c_int64()
+    L = lib()
+    rc = L.spc_check_sincos(x.size, _ptr(x), C.byref(bad))
     if rc != 0:
         raise SpcError(rc, L.spc_last_error(None).decode())
     return bad.value

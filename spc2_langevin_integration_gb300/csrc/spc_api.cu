@@ -769,6 +769,35 @@ int spc_check_division(int64_t n, const double *a, const double *b, int64_t *mis
   return SPC_OK;
 }
 
+int spc_check_sincos(int64_t n, const double *x, int64_t *mismatches) {
+  if (!x || !mismatches || n < 0) return fail(nullptr, SPC_ERR_INVALID, "bad argument");
+  *mismatches = 0;
+  if (n == 0) return SPC_OK;
+  double *dx = nullptr, *ds = nullptr, *dc = nullptr;
+  unsigned long long *dbad = nullptr;
+  cudaError_t e = cudaMalloc(&dx, (size_t)n * 8);
+  if (e == cudaSuccess) e = cudaMalloc(&ds, (size_t)n * 8);
+  if (e == cudaSuccess) e = cudaMalloc(&dc, (size_t)n * 8);
+  if (e == cudaSuccess) e = cudaMalloc(&dbad, 8);
+  if (e == cudaSuccess) e = cudaMemcpy(dx, x, (size_t)n * 8, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemset(dbad, 0, 8);
+  if (e == cudaSuccess) {
+    k_sin_only<<<152 * 8, 256>>>(n, dx, ds);
+    k_cos_only<<<152 * 8, 256>>>(n, dx, dc);
+    k_sincos_cmp<<<152 * 8, 256>>>(n, dx, ds, dc, dbad);
+    e = cudaGetLastError();
+  }
+  unsigned long long bad = 0;
+  if (e == cudaSuccess) e = cudaMemcpy(&bad, dbad, 8, cudaMemcpyDeviceToHost);
+  cudaFree(dx);
+  cudaFree(ds);
+  cudaFree(dc);
+  cudaFree(dbad);
+  if (e != cudaSuccess) return fail(nullptr, SPC_ERR_CUDA, "check_sincos: %s", cudaGetErrorString(e));
+  *mismatches = (int64_t)bad;
+  return SPC_OK;
+}
+
 int spc_alloc_pinned(size_t bytes, void **out) {
   if (!out) return fail(nullptr, SPC_ERR_INVALID, "NULL argument");
   cudaError_t e = cudaMallocHost(out, bytes);

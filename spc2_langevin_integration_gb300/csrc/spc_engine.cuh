@@ -403,6 +403,13 @@ inline int engine_init_verlet(Engine *e, int cap) {
   SPC_TRY(dalloc(e, &e->vyb, N));
   SPC_TRY(dalloc(e, &e->vflags, 2));
   SPC_TRY(dalloc(e, &e->vrebuilds, 1));
+  // FP64 SRK: the first pass keeps each accepted row entry's cosine for the
+  // second (sincos gives the cosine bit for bit; spc_check_sincos), within a
+  // budget of 4 GB; above it the second pass evaluates the cosine itself
+  double *vcos = nullptr;
+  if (e->precision == SPC_PRECISION_FP64 && e->stepper == SPC_STEPPER_SRK &&
+      (size_t)cap * N * sizeof(double) <= ((size_t)4 << 30))
+    SPC_TRY(dalloc(e, &vcos, (size_t)cap * N));
   cudaStream_t st = e->stream;
   SPC_CUDA(e, cudaMemsetAsync(e->vrowlen, 0, N * 4, st));
   SPC_CUDA(e, cudaMemsetAsync(e->vsys, 0, N * 4, st));
@@ -418,6 +425,7 @@ inline int engine_init_verlet(Engine *e, int cap) {
   a.vyb = e->vyb;
   a.vflags = e->vflags;
   a.vrebuilds = e->vrebuilds;
+  a.vcos = vcos;
   e->verlet_stale = true;
   return SPC_OK;
 }

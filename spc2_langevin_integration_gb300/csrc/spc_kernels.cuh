@@ -112,6 +112,7 @@ struct KArgs {
   const int *gate;                   // binning kernels return at once when *gate == 0
   int *vsys, *vcell;                 // build: system and cell of each cell-order slot
   uint16_t *vrows;                   // row entry k of slot v at vrows[((k / 8) * n_active + v) * 8 + k % 8]
+  double *vcos;                      // FP64 SRK: cos of row entry k's phase difference at vcos[k * n_active + v], or null
   int *vrowlen;                      // entries of each row, -1: overflow (scan the stencil)
   int vcap;                          // row limit of the current build
   double *vxb, *vyb;                 // stage positions at the build
@@ -749,6 +750,30 @@ __global__ void k_check_division(long long n, const double *__restrict__ a, cons
     const double x = a[i], d = b[i];
     const double q0 = ddiv(x, d), q1 = ddiv_by(x, d, drcp(d));
     if (__double_as_longlong(q0) != __double_as_longlong(q1)) atomicAdd(bad, 1ull);
+  }
+}
+
+// sin and cos of x[i] from separate launches (nothing to merge) and from one
+// sincos, for spc_check_sincos.
+__global__ void k_sin_only(long long n, const double *__restrict__ x, double *__restrict__ s) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x)
+    s[i] = sin(x[i]);
+}
+__global__ void k_cos_only(long long n, const double *__restrict__ x, double *__restrict__ c) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x)
+    c[i] = cos(x[i]);
+}
+__global__ void k_sincos_cmp(long long n, const double *__restrict__ x, const double *__restrict__ s,
+                             const double *__restrict__ c, unsigned long long *bad) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x) {
+    double sn, cn;
+    sincos(x[i], &sn, &cn);
+    if (__double_as_longlong(sn) != __double_as_longlong(s[i]) ||
+        __double_as_longlong(cn) != __double_as_longlong(c[i]))
+      atomicAdd(bad, 1ull);
   }
 }
 

@@ -329,10 +329,19 @@ __global__ void __launch_bounds__(kVThreads) k_vtile(KArgs a, int epi) {
             }
           } else {
             const double dp = dsub(dsub(sm.phi[j], il.phi), sc.alpha);
+            // row entries only: k is then the entry's position in the row
+            double *vc = (a.vcos && rows) ? a.vcos + (size_t)k * n_all + v : nullptr;
             if constexpr (KIND == kKindSin) {
-              acc.s0 = dadd(acc.s0, sin(dp));  // ChimeraSystem.cpp:412
+              double sn, cn;
+              if (vc) {  // keep the cosine for the second pass
+                sincos(dp, &sn, &cn);
+                *vc = cn;
+              } else {
+                sn = sin(dp);
+              }
+              acc.s0 = dadd(acc.s0, sn);  // ChimeraSystem.cpp:412
             } else {
-              const double cc = cos(dp);  // ChimeraSystem.cpp:634-637
+              const double cc = vc ? *vc : cos(dp);  // ChimeraSystem.cpp:634-637
               acc.s0 = dadd(acc.s0, ddiv_by(cc, il.card, il.rcard));
               acc.s1 = dadd(acc.s1, ddiv_by(dmul(dsub(sm.dd[j], il.dphi), cc), il.card, il.rcard));
             }
@@ -409,10 +418,18 @@ __global__ void __launch_bounds__(kVThreads) k_vtile(KArgs a, int epi) {
                     }
                   } else {
                     const double dp = dsub(dsub(sm.phi[j], il.phi), sc.alpha);
+                    double *vc = a.vcos ? a.vcos + (size_t)kk * n_all + v : nullptr;
                     if constexpr (KIND == kKindSin) {
-                      acc.s0 = dadd(acc.s0, sin(dp));  // ChimeraSystem.cpp:412
+                      double sn, cn;
+                      if (vc) {  // keep the cosine for the second pass
+                        sincos(dp, &sn, &cn);
+                        *vc = cn;
+                      } else {
+                        sn = sin(dp);
+                      }
+                      acc.s0 = dadd(acc.s0, sn);  // ChimeraSystem.cpp:412
                     } else {
-                      const double cc = cos(dp);  // ChimeraSystem.cpp:634-637
+                      const double cc = vc ? *vc : cos(dp);  // ChimeraSystem.cpp:634-637
                       acc.s0 = dadd(acc.s0, ddiv_by(cc, il.card, il.rcard));
                       acc.s1 = dadd(acc.s1, ddiv_by(dmul(dsub(sm.dd[j], il.dphi), cc), il.card, il.rcard));
                     }

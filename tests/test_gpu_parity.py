@@ -403,3 +403,14 @@ def test_fp64_division_by_reciprocal_is_bitwise():
     ])
     assert abi.check_division(a, b) == 0
     assert abi.check_division(np.zeros(0), np.zeros(0)) == 0
+
+
+def test_sincos_cosine_is_bitwise_the_cosine():
+    # the FP64 Verlet SRK first pass keeps sincos's cosine of each accepted
+    # pair for the second pass; it must be the cosine the second pass would
+    # compute (test_row_overflow_fallback_is_bitwise_fp64 checks the passes)
+    rng = np.random.default_rng(57)
+    m = 2_000_000
+    x = np.concatenate([rng.uniform(-7, 7, m), rng.uniform(-1e3, 1e3, m), rng.normal(0, 50, m),
+                        np.ldexp(rng.random(m), rng.integers(-30, 30, m)) * rng.choice([-1.0, 1.0], m)])
+    assert abi.check_sincos(x) == 0
