@@ -390,6 +390,18 @@ inline int engine_init(Engine *e, int stepper, int precision, int pool_cap, int 
 
 // Verlet buffers for rows of up to `cap` entries (cap <= 1024, so that the
 // FP32C pass-1 bits of a row fit the 32 mask words of a particle).
+// Vortex-arrays SRK single systems: room for the first pass's records of
+// `cap` pairs within rho per particle (32 B each), within a budget of 4 GB;
+// beyond it (or beyond cap pairs) the second pass recomputes them.
+inline int engine_init_va_cache(Engine *e, int cap) {
+  const size_t N = (size_t)e->pool_cap;
+  cap = std::max(32, cap);
+  if ((size_t)cap * N * 4 * sizeof(double) > ((size_t)4 << 30)) return SPC_OK;
+  SPC_TRY(dalloc(e, &e->a.vacache, (size_t)cap * N * 4));
+  e->a.vacap = cap;
+  return SPC_OK;
+}
+
 inline int engine_init_verlet(Engine *e, int cap) {
   const size_t N = (size_t)e->pool_cap;
   cap = std::max(32, std::min(cap, kMaskWords * kWarp));

@@ -113,6 +113,11 @@ struct KArgs {
   int *vsys, *vcell;                 // build: system and cell of each cell-order slot
   uint16_t *vrows;                   // row entry k of slot v at vrows[((k / 8) * n_active + v) * 8 + k % 8]
   double *vcos;                      // FP64 SRK: cos of row entry k's phase difference at vcos[k * n_active + v], or null
+  // vortex-arrays SRK (single systems): the first pass's record of slot p's
+  // k-th pair within rho (k < vacap): strength, its derivative, sin and cos of
+  // the phase difference at vacache[(k * n_active + p) * 4 + 0..3], or null
+  double *vacache;
+  int vacap;
   int *vrowlen;                      // entries of each row, -1: overflow (scan the stencil)
   int vcap;                          // row limit of the current build
   double *vxb, *vyb;                 // stage positions at the build

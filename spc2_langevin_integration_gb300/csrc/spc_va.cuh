@@ -161,6 +161,7 @@ template <int KIND>
 __global__ void __launch_bounds__(kVAThreads) k_va_pass(KArgs a, int epi) {
   __shared__ VAStage<KIND> sm;
   const int tid = threadIdx.x;
+  const int n_all = a.n_active;
   for (int c = a.va_c0 + blockIdx.x; c < a.va_c1; c += gridDim.x) {
     const int cb = a.cell_start[c], ce = a.cell_start[c + 1];
     if (cb == ce) continue;
@@ -206,6 +207,7 @@ __global__ void __launch_bounds__(kVAThreads) k_va_pass(KArgs a, int epi) {
       }
       const int self = (ap ? 0 : st.prefix[4]) + (p - cb);
       VAAcc r{0.0, 0.0, 0.0, 0, 0, 0, 0.0, 0.0};
+      int kr = 0;  // pairs within rho so far: the index of this particle's pair records
       for (int rr = 0; rr < rounds; ++rr) {
         const int rlo = rr * kVACap, rcnt = min(kVACap, total - rlo);
         if (rounds > 1 || ig == cb) {
@@ -241,14 +243,34 @@ __global__ void __launch_bounds__(kVAThreads) k_va_pass(KArgs a, int epi) {
           const double dy = min_image_1d(dsub(a.sy[pj], yi), sc.rL, sc.L);
           const double dr = dsqrt(dadd(dmul(dx, dx), dmul(dy, dy)));
           const double phij = sm.phi[j];
+          // a pair within rho has a record for the second SRK pass (single
+          // systems): the same strength, derivative, sin and cos bit for bit
+          const bool rho_pair = dr <= sc.rho;
+          double *rec = (rho_pair && a.vacache && kr < a.vacap) ? a.vacache + ((size_t)kr * n_all + p) * 4 : nullptr;
+          kr += rho_pair ? 1 : 0;
           if constexpr (KIND == kKindSin) {
             // VortexArraysSystemPtr.cpp:475-488
-            if (dr <= sc.xi_a) {
-              r.align = dadd(r.align, dmul(va_strength(sc, dr), sin(dsub(phij, phii))));
-              ++r.c0;
-            } else if (dr <= sc.rho) {
-              r.anti = dadd(r.anti, dmul(va_strength(sc, dr), sin(dsub(phij, phii))));
-              ++r.c1;
+            if (dr <= sc.xi_a || rho_pair) {
+              double as, sn;
+              if (rec) {
+                double cn;
+                sincos(dsub(phij, phii), &sn, &cn);  // the bits of sin and cos
+                as = va_strength(sc, dr);
+                rec[0] = as;
+                rec[1] = va_strength_derivative(sc, dr);
+                rec[2] = sn;
+                rec[3] = cn;
+              } else {
+                as = va_strength(sc, dr);
+                sn = sin(dsub(phij, phii));
+              }
+              if (dr <= sc.xi_a) {
+                r.align = dadd(r.align, dmul(as, sn));
+                ++r.c0;
+              } else {
+                r.anti = dadd(r.anti, dmul(as, sn));
+                ++r.c1;
+              }
             }
             if (dr <= sc.xi_r) {
               r.coh = dadd(r.coh, dmul(-sc.kappa, sin(dsub(atan2(dy, dx), phii))));
@@ -256,9 +278,19 @@ __global__ void __launch_bounds__(kVAThreads) k_va_pass(KArgs a, int epi) {
             }
           } else {
             // VortexArraysSystemPtr.cpp:706-728
-            if ((dr <= sc.rho) && (norm1 > 0.0)) {
-              const double cp = cos(dsub(phij, phii)), sp = sin(dsub(phij, phii));
-              const double as = va_strength(sc, dr), asd = va_strength_derivative(sc, dr);
+            if (rho_pair && (norm1 > 0.0)) {
+              double cp, sp, as, asd;
+              if (rec) {  // the first pass's values
+                as = rec[0];
+                asd = rec[1];
+                sp = rec[2];
+                cp = rec[3];
+              } else {
+                cp = cos(dsub(phij, phii));
+                sp = sin(dsub(phij, phii));
+                as = va_strength(sc, dr);
+                asd = va_strength_derivative(sc, dr);
+              }
               // every quotient by norm1 or dr as ddiv would give it (ddiv_by)
               const double rdr = drcp(dr);
               r.a0 = dadd(r.a0, ddiv_by(dmul(-as, cp), norm1, rn1));
