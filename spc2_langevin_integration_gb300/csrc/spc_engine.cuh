@@ -402,6 +402,18 @@ inline int engine_init_va_cache(Engine *e, int cap) {
   return SPC_OK;
 }
 
+// Cell-tile FP64 SRK single systems: room for the first pass's cosines of
+// `cap` accepted pairs per particle (8 B each), within a budget of 4 GB;
+// beyond it (or beyond cap pairs) the second pass evaluates them.
+inline int engine_init_tile_cos(Engine *e, int cap) {
+  const size_t N = (size_t)e->pool_cap;
+  cap = std::max(32, cap);
+  if ((size_t)cap * N * sizeof(double) > ((size_t)4 << 30)) return SPC_OK;
+  SPC_TRY(dalloc(e, &e->a.tcos, (size_t)cap * N));
+  e->a.tcap = cap;
+  return SPC_OK;
+}
+
 inline int engine_init_verlet(Engine *e, int cap) {
   const size_t N = (size_t)e->pool_cap;
   cap = std::max(32, std::min(cap, kMaskWords * kWarp));

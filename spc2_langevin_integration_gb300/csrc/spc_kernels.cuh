@@ -118,6 +118,10 @@ struct KArgs {
   // the phase difference at vacache[(k * n_active + p) * 4 + 0..3], or null
   double *vacache;
   int vacap;
+  // cell-tile FP64 SRK (single systems): cos of slot p's k-th accepted pair
+  // (k < tcap) from the first pass at tcos[k * n_active + p], or null
+  double *tcos;
+  int tcap;
   int *vrowlen;                      // entries of each row, -1: overflow (scan the stencil)
   int vcap;                          // row limit of the current build
   double *vxb, *vyb;                 // stage positions at the build

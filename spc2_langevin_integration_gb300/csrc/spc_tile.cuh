@@ -377,6 +377,7 @@ __global__ void __launch_bounds__(kTileThreads64) k_tile_fp64(KArgs a, int epi) 
   __shared__ int s_p[kTileCap64];
   __shared__ uint16_t s_q[kQCap][kTileThreads64];
   const int tid = threadIdx.x;
+  const int n_all = a.n_active;
   const int nitems = tile_items(a);
   for (int item = blockIdx.x; item < nitems; item += gridDim.x) {
     TileItem ti;
@@ -422,12 +423,24 @@ __global__ void __launch_bounds__(kTileThreads64) k_tile_fp64(KArgs a, int epi) 
         }
         const int self = st.prefix[4] + (p - c0) - rlo;
         int qn = 0, qh = 0;
-        auto eval = [&](int j) {
+        // accepted pair number `ord` of this particle (the same in both SRK
+        // passes): single systems keep the first pass's cosine for the second
+        // (sincos gives the bits of cos; spc_check_sincos)
+        auto eval = [&](int j, int ord) {
           const double dphi_ = dsub(dsub(s_phi[j], il.phi), sc.alpha);
+          double *slot = (a.tcos && ord < a.tcap) ? a.tcos + (size_t)ord * n_all + p : nullptr;
           if constexpr (KIND == kKindSin) {
-            acc.s0 = dadd(acc.s0, sin(dphi_));  // ChimeraSystem.cpp:412
+            double sn;
+            if (slot) {
+              double cn;
+              sincos(dphi_, &sn, &cn);
+              *slot = cn;
+            } else {
+              sn = sin(dphi_);
+            }
+            acc.s0 = dadd(acc.s0, sn);  // ChimeraSystem.cpp:412
           } else {
-            const double cc = cos(dphi_);      // ChimeraSystem.cpp:634-637
+            const double cc = slot ? *slot : cos(dphi_);  // ChimeraSystem.cpp:634-637
             acc.s0 = dadd(acc.s0, ddiv_by(cc, il.card, il.rcard));
             acc.s1 = dadd(acc.s1, ddiv_by(dmul(dsub(s_d[j], il.dphi), cc), il.card, il.rcard));
           }
@@ -453,17 +466,17 @@ __global__ void __launch_bounds__(kTileThreads64) k_tile_fp64(KArgs a, int epi) 
           int m = __reduce_min_sync(0xffffffffu, valid ? qn - qh : 0x7fffffff);
           if (m == 0x7fffffff) m = 0;
           if (valid) {
-            for (int k = 0; k < m; ++k) eval(s_q[(qh + k) & (kQCap - 1)][tid]);
+            for (int k = 0; k < m; ++k) eval(s_q[(qh + k) & (kQCap - 1)][tid], acc.n + qh + k);
             qh += m;
           }
           // keep room for the next block of 32
           while (qn - qh > kQCap - kWarp) {
-            eval(s_q[qh & (kQCap - 1)][tid]);
+            eval(s_q[qh & (kQCap - 1)][tid], acc.n + qh);
             ++qh;
           }
         }
         while (qh < qn) {  // tail of this round
-          eval(s_q[qh & (kQCap - 1)][tid]);
+          eval(s_q[qh & (kQCap - 1)][tid], acc.n + qh);
           ++qh;
         }
         acc.n += qn;
