@@ -672,6 +672,8 @@ def main():
                     help="serve: seconds of the Poisson trace served (2 s: 384 requests, a few "
                          "minutes of device time; the FP64 form takes most of it)")
     ap.add_argument("--serve-rate", type=float, default=200.0)
+    ap.add_argument("--serve-form", choices=["both", "fp32c", "fp64"], default="both",
+                    help="serve: the precision forms served (one batch each)")
     args = ap.parse_args()
     if args.workload == "ensemble":
         import torch
@@ -743,7 +745,8 @@ def main():
         from spc2_langevin_integration_gb300 import abi
         out = {"metric": "served time-to-result", "workload": "poisson_requests_euler"}
         for name, prec in (("fp32c", abi.PRECISION_FP32C), ("fp64", abi.PRECISION_FP64)):
-            out[name] = run_serving(prec, args.serve_duration, args.serve_rate)
+            if args.serve_form in ("both", name):
+                out[name] = run_serving(prec, args.serve_duration, args.serve_rate)
         print(json.dumps(out))
         return
     if args.ncu_case == "va":
