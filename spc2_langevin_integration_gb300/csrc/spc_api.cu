@@ -195,8 +195,11 @@ int spc_create(const spc_params *p, int32_t n, spc_handle **out) {
     const double want = std::max(2.0 * mean, mean + 8.0 * std::sqrt(mean)) + 64.0;
     rc = engine_init_verlet(&h->e, ((int)want + 31) / 32 * 32);
   }
+  // (cells dense enough for the cell-tile kernel by default: the warp-per-cell
+  // kernel of sparse cells keeps no cosines)
   if (rc == SPC_OK && p->model != SPC_MODEL_VORTEX_ARRAYS && p->stepper == SPC_STEPPER_SRK &&
-      p->precision == SPC_PRECISION_FP64 && p->neighbour == SPC_NEIGHBOUR_CELL && !sc.allpairs) {
+      p->precision == SPC_PRECISION_FP64 && p->neighbour == SPC_NEIGHBOUR_CELL && !sc.allpairs &&
+      (double)n / (double)sc.ncell >= kSparseBelowDefault) {
     // accepted pairs: about pi rho^2 n / L^2 per particle
     const double mean = 3.141592653589793 * p->rho * p->rho * (double)n / (p->L * p->L);
     const double want = std::max(2.0 * mean, mean + 8.0 * std::sqrt(mean)) + 64.0;
