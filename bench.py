@@ -47,6 +47,11 @@ ALG_BYTES_STEP = 168 + 8      # survey accounting for the whole SRK step (+ omeg
 # SRK pass 1) at this workload, from one ncu capture; the command and the raw
 # figures are in profiles/k_tile_fp32c_vortex_srk_n65536.md.
 NCU_TRAFFIC_PASS1 = 2.41e6
+# The same capture's instruction-issue figures for that kernel: issue slots
+# used on the cycles an SM was active, and the SMs' active share of the
+# launch's cycles (the single-wave pass ends with the SMs holding most pairs).
+NCU_ISSUE_ACTIVE_PASS1 = 0.614
+NCU_SM_ACTIVE_PASS1 = 61769.0 / 79240.0
 
 
 def init_inputs(w, seed_offset=0):
@@ -891,7 +896,12 @@ def main():
                      "alg_bytes_per_launch": ALG_BYTES[dom] * w["n"],
                      "compute": {"candidate_tests_per_s": w["n"] * cand / t_pass,
                                  "pair_terms_per_s": w["n"] * pairs / t_pass,
-                                 "candidates_per_particle": cand, "pairs_per_particle": pairs},
+                                 "candidates_per_particle": cand, "pairs_per_particle": pairs,
+                                 "issue_frac": (NCU_ISSUE_ACTIVE_PASS1 * NCU_SM_ACTIVE_PASS1
+                                                if dom == "pass1" else None),
+                                 "issue_frac_source": "ncu (profiles/k_tile_fp32c_vortex_srk_n65536"
+                                                      ".md): issue-active share of active cycles "
+                                                      "x SM-active share of elapsed cycles"},
                      "note": "the passes are bound by issue / latency (float prefilter and "
                              "per-pair trig on an L2-resident working set), not by HBM: the "
                              "HBM fraction is low by construction"},
