@@ -244,7 +244,7 @@ def run_serving(precision, duration, rate, seed=3):
     return out
 
 
-def run_drift(steps=10000, every=100, out_path=None):
+def run_drift(steps=10000, every=100, out_path=None, seed=None):
     """Drift of the order parameters of the FP32-compensated form against FP64.
 
     (1) The vortex SRK workload (N=65,536, L=8): FP32C and the FP64 GPU path from
@@ -255,7 +255,8 @@ def run_drift(steps=10000, every=100, out_path=None):
     run and injected into the others).
     Both also run FP64 from the initial state with every phase moved by one ulp:
     its drift is the dynamics' own sensitivity, the floor for any perturbation.
-    Reports max and mean |delta| over the recorded points."""
+    Reports max and mean |delta| over the recorded points.  `seed` replaces the
+    vortex workload's seed (its initial state, frequencies and Philox key)."""
     from oracle import pyoracle as po
     from spc2_langevin_integration_gb300 import abi
 
@@ -271,7 +272,7 @@ def run_drift(steps=10000, every=100, out_path=None):
 
     res, dump = {}, {}
     # (1) vortex SRK N=65536
-    w = WORKLOAD
+    w = WORKLOAD if seed is None else dict(WORKLOAD, seed=seed)
     st, omega = init_inputs(w)
     st_ulp = st.copy()
     st_ulp[2::3] = np.nextafter(st[2::3], np.inf)
@@ -292,7 +293,8 @@ def run_drift(steps=10000, every=100, out_path=None):
         series[name] = np.array(rows)
     a64 = series["fp64"]
     res["vortex_srk_n65536"] = {
-        "steps": steps, "every": every, "reference": "FP64 GPU path (same Philox counters)",
+        "steps": steps, "every": every, "seed": w["seed"],
+        "reference": "FP64 GPU path (same Philox counters)",
         "fp32c": {"R": stats(a64[:, 1], series["fp32c"][:, 1]),
                   "R_local": stats(a64[:, 2], series["fp32c"][:, 2])},
         "fp64_one_ulp_phases": {"R": stats(a64[:, 1], series["fp64_ulp"][:, 1]),
@@ -673,6 +675,9 @@ def main():
     ap.add_argument("--compare-kernels", action="store_true",
                     help="ensemble: also time every system on the cell-tile passes")
     ap.add_argument("--drift-steps", type=int, default=10000)
+    ap.add_argument("--drift-seed", type=int, default=None,
+                    help="drift: seed of the vortex workload (initial state, frequencies, "
+                         "Philox key) in place of its own (1)")
     ap.add_argument("--serve-duration", type=float, default=2.0,
                     help="serve: seconds of the Poisson trace served (2 s: 384 requests, a few "
                          "minutes of device time; the FP64 form takes most of it)")
@@ -736,7 +741,7 @@ def main():
         return
     if args.workload == "drift":
         out = {"metric": "order-parameter drift, FP32C vs FP64", "workload": "drift"}
-        out.update(run_drift(steps=args.drift_steps, out_path=args.drift_series))
+        out.update(run_drift(steps=args.drift_steps, out_path=args.drift_series, seed=args.drift_seed))
         print(json.dumps(out))
         return
     if args.workload == "observed":

@@ -161,20 +161,32 @@ __device__ __forceinline__ void philox_normal2(uint64_t seed, uint32_t system_id
   z1 = r * s;
 }
 
-// Float form of the same draw for the FP32-compensated path: the same Philox
-// words, 24-bit uniforms and single-precision Box-Muller (the double version's
-// log/sqrt/sincospi run on GB300's 1/64-rate FP64 pipe).
+// Float form of the same draw for the FP32-compensated path: single-precision
+// Box-Muller (the double version's log/sqrt/sincospi run on GB300's 1/64-rate
+// FP64 pipe) on the same two 53-bit integers, each rounded once to float, so
+// that the result keeps float's RELATIVE precision at both ends of u1:
+// * u1 < 1/2 (the normal's tail, steep in u1): log of u1 = (a + 1) 2^-53;
+// * u1 >= 1/2 (near-zero radii, where log u1 ~ u1 - 1): log1p(-e) of
+//   e = 1 - u1 = (2^53 - 1 - a) 2^-53, exact in integers before the rounding.
+// (A 24-bit fixed-point u1 differs from the 53-bit one by up to 2^-24
+// absolute, which moves a tail draw by ~1e-5 relative: that error dominated
+// the FP32C form's drift from FP64.)  The angle is taken as pi*v with
+// v = 2*u2 - 1 in [-1, 1), exact in integers before the rounding, and
+// sinpi / cospi(v + 1) = -sinpi / -cospi(v).
 __device__ __forceinline__ void philox_normal2_f(uint64_t seed, uint32_t system_id, uint64_t step,
                                                  uint32_t i, float &z0, float &z1) {
   const U4 o = philox4x32_10(U4{i, system_id, (uint32_t)step, (uint32_t)(step >> 32)},
                              (uint32_t)seed, (uint32_t)(seed >> 32));
-  const float u1 = (float)((o.x >> 8) + 1u) * 0x1.0p-24f;
-  const float u2 = (float)(o.z >> 8) * 0x1.0p-24f;
-  const float r = sqrtf(-2.0f * logf(u1));
+  const uint64_t a = ((((uint64_t)o.x) << 32) | o.y) >> 11;
+  const uint64_t b = ((((uint64_t)o.z) << 32) | o.w) >> 11;
+  const float lnu = a < (1ull << 52) ? logf((float)(a + 1) * 0x1.0p-53f)
+                                     : log1pf(-(float)((1ull << 53) - 1 - a) * 0x1.0p-53f);
+  const float v = (float)((long long)b - (1ll << 52)) * 0x1.0p-52f;
+  const float r = sqrtf(-2.0f * lnu);
   float s, c;
-  sincospif(2.0f * u2, &s, &c);
-  z0 = r * c;
-  z1 = r * s;
+  sincospif(v, &s, &c);
+  z0 = -r * c;
+  z1 = -r * s;
 }
 
 // Error word bits reported through spc_diagnostics.
