@@ -158,6 +158,44 @@ def ensemble_systems(count=512, seed=2, n_range=(256, 32768), density=1000.0):
     return out
 
 
+def _cpu_replica_worker(job):
+    """One replica of the headline workload on one host core (initial state
+    seeded by replica): a warm-up step, a barrier shared with the other
+    replicas, then `nsteps` timed SRK steps of the oracle port.  Returns the
+    particle-steps done and the wall-clock start and end of the timed steps."""
+    k, nsteps, barrier = job
+    from oracle import pyoracle as po
+    w = WORKLOAD
+    st, omega = init_inputs(w, seed_offset=k)
+    n = w["n"]
+    o = po.OracleSystem(n, w["L"], w["v0"], w["sigma"], w["rho"], w["alpha"], w["D_phi"])
+    noise = np.random.default_rng(99 + k).standard_normal(2 * n * nsteps)
+    o.run(po.SRK, st, 0.0, w["dt"], 1, noise[:2 * n], omega)  # warm
+    barrier.wait()
+    t0 = time.time()
+    o.run(po.SRK, st, 0.0, w["dt"], nsteps, noise, omega)
+    return n * nsteps, t0, time.time()
+
+
+def cpu_replicas_baseline(nsteps=1):
+    """The reference path on every host core: one independent replica of the
+    headline workload per core (the reference runs one system per process; its
+    only multi-core form is independent systems side by side), started
+    together.  Aggregate particle-steps/s over the span of the timed steps."""
+    import multiprocessing as mpc
+    cores = os.cpu_count() or 1
+    ctx = mpc.get_context("spawn")
+    with ctx.Manager() as mgr:
+        barrier = mgr.Barrier(cores)
+        with ctx.Pool(cores) as pool:
+            out = pool.map(_cpu_replica_worker, [(k, nsteps, barrier) for k in range(cores)])
+    work = sum(wk for wk, _, _ in out)
+    span = max(t1 for _, _, t1 in out) - min(t0 for _, t0, _ in out)
+    return {"value": work / span, "unit": "particle-steps/s", "cores": cores, "kind": "port",
+            "sample": f"{cores} replicas of N={WORKLOAD['n']} (one per host core, started "
+                      f"together), {nsteps} SRK step(s) each"}
+
+
 _ENSEMBLE = None
 
 
@@ -829,12 +867,15 @@ def main():
             vals.append(cpu_baseline(w, nsteps=1)["value"])
         v = float(np.mean(vals))
         cb = cpu_baseline(w, nsteps=1)
+        allc = cpu_replicas_baseline(nsteps=1)
         print(json.dumps({
             "impl": "reference", "metric": "particle-steps/s", "value": v,
             "unit": "particle-steps/s", "n_gpus": args.gpus, "steps": args.steps,
             "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": config,
             "cpu_baseline": {"kind": cb["kind"], "cores": 1, "sample": cb["sample"], "value": v},
+            # one system uses one core; every core, one replica each:
+            "all_cores_replicas": allc,
             "e2e": {"value": v, "unit": "particle-steps/s", "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0}}))
         return
