@@ -445,6 +445,8 @@ class Batch:
             raise SpcError(rc, (self._L.spc_batch_last_error(None) or b"").decode())
         self.h = h
         self.n = {}
+        self.capacity = {"particles": int(max_particles), "cells": int(max_cells),
+                         "systems": int(max_systems)}
 
     def _check(self, rc: int):
         if rc != SPC_OK:

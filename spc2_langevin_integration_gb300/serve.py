@@ -140,6 +140,18 @@ class Server:
         cells_bytes = int(hbm_bytes * cell_share)
         return int((hbm_bytes - cells_bytes) // bp), int(cells_bytes // bc), max_systems
 
+    def _may_fit(self, req: Request) -> bool:
+        """A necessary condition for admitting `req` now, from the batch's
+        totals: a free system slot and room for its particles (the pool also
+        needs a contiguous range, and the cells are checked by the batch).
+        Checked before the request's initial state is generated, so that a
+        blocked queue does not draw the states of requests that cannot fit."""
+        cap = getattr(self.b, "capacity", None)
+        if cap is None:
+            return True
+        u = self.b.usage()
+        return u["systems"] < cap["systems"] and u["particles"] + req.n <= cap["particles"]
+
     def run(self, trace: list[Request], time_scale: float = 1.0) -> ServeStats:
         pending = collections.deque(sorted(trace, key=lambda r: r.arrival))
         waiting: collections.deque[Request] = collections.deque()
@@ -162,6 +174,9 @@ class Server:
             for req in list(waiting):
                 if skipped > self.backfill:
                     break
+                if active and not self._may_fit(req):
+                    skipped += 1  # its initial state is not generated until it may fit
+                    continue
                 st, om = req.inputs()
                 try:
                     slot = self.b.admit(req.n, req.params(self.stepper, self.precision), st, om,

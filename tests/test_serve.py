@@ -11,9 +11,14 @@ class FakeBatch:
 
     def __init__(self, max_systems, max_particles, max_cells):
         self.cap = (max_systems, max_particles, max_cells)
+        self.capacity = {"particles": max_particles, "cells": max_cells, "systems": max_systems}
         self.sys = {}
         self.steps_taken = 0
         self.log = []
+
+    def usage(self):
+        return {"particles": sum(v["n"] for v in self.sys.values()),
+                "cells": sum(v["cells"] for v in self.sys.values()), "systems": len(self.sys)}
 
     def admit(self, n, params, state, omega=None, steps=-1):
         cells = abi.cells_of(params.L, params.rho)
@@ -92,6 +97,26 @@ def test_scheduler_respects_capacity_budgets_and_order():
     assert st.p50_s is not None and st.p99_s >= st.p50_s
     released = [e for e in fb.log if e[0] == "release"]
     assert len(released) == len(tr)
+
+
+def test_initial_states_are_drawn_once_per_request(monkeypatch):
+    """A queue blocked on capacity does not draw the initial states of the
+    requests it cannot admit yet: each request's inputs are generated once."""
+    calls = []
+    orig = serve.Request.inputs
+
+    def counted(self):
+        calls.append(self.rid)
+        return orig(self)
+
+    monkeypatch.setattr(serve.Request, "inputs", counted)
+    tr = serve.make_trace(rate=400, duration=0.5, seed=5, n_range=(100, 3000), steps_range=(20, 200))
+    fb = FakeBatch(max_systems=6, max_particles=8000, max_cells=100000)
+    srv = serve.Server(fb, abi.STEPPER_EULER, abi.PRECISION_FP32C, chunk=10, clock=FakeClock(),
+                       limits=(8000, 100000))
+    st = srv.run(tr)
+    assert st.completed == len(tr)
+    assert sorted(calls) == sorted(r.rid for r in tr)
 
 
 def test_requests_that_can_never_fit_are_refused():
