@@ -86,10 +86,11 @@ spc_handle *SpcSystemBase::Handle(int stepper) {
       if ((int)frequencies_.size() != kN) frequencies_.assign((size_t)kN, 0.0);
       Check(spc_upload_omega(h, frequencies_.data()), h);
     }
-  } else if (frequencies_dirty_ && ModelFor(stepper) == SPC_MODEL_VORTEX) {
+    omega_stale_[stepper] = false;
+  } else if (omega_stale_[stepper] && ModelFor(stepper) == SPC_MODEL_VORTEX) {
     Check(spc_upload_omega(handles_[stepper], frequencies_.data()), handles_[stepper]);
+    omega_stale_[stepper] = false;
   }
-  if (ModelFor(stepper) == SPC_MODEL_VORTEX) frequencies_dirty_ = false;
   return handles_[stepper];
 }
 
@@ -97,7 +98,7 @@ void SpcSystemBase::UseFrequencies(const std::vector<Real> &frequencies) {
   if ((int)frequencies.size() != kN) throw std::runtime_error("spc: need N frequencies");
   if (frequencies != frequencies_) {
     frequencies_ = frequencies;
-    frequencies_dirty_ = true;
+    for (bool &stale : omega_stale_) stale = true;  // every handle uploads them on its next use
   }
 }
 

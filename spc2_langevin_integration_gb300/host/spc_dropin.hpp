@@ -143,7 +143,7 @@ class SpcSystemBase {
   Real skin_ = 0.05;
   uint64_t seed_ = 0;
   std::vector<Real> frequencies_;
-  bool frequencies_dirty_ = false;
+  bool omega_stale_[4] = {false, false, false, false};  // per handle: frequencies changed since its upload
   Real mu_plus_ = 0.0, mu_minus_ = 0.0, xi_a_ = 0.0, xi_r_ = 0.0, kappa_ = 0.0;  // vortex arrays
   spc_handle *handles_[4] = {nullptr, nullptr, nullptr, nullptr};
   std::vector<Real> shadow_[4];  // what each handle's device state holds
