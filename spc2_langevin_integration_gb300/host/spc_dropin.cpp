@@ -130,9 +130,14 @@ void SpcSystemBase::RhsSrk(const Real *state, Real *derivative,
   }
 }
 
-void SpcSystemBase::Sync(spc_handle *h, const std::vector<Real> &state) {
+int SpcSystemBase::SlotOf(const spc_handle *h) const {
   int k = 0;
   while (handles_[k] != h) ++k;
+  return k;
+}
+
+void SpcSystemBase::Sync(spc_handle *h, const std::vector<Real> &state) {
+  const int k = SlotOf(h);
   if (shadow_[k] != state) {
     Check(spc_upload_state(h, state.data()), h);
     shadow_[k] = state;
@@ -147,11 +152,13 @@ void SpcSystemBase::Advance(int stepper, std::vector<Real> &state, Real &t, Real
     Check(spc_inject_noise(h, injected_.data(), (int64_t)injected_.size()), h);
     inject_pending_ = false;
   }
+  // the device state moves from here on: until the new state is back on the
+  // host, no shadow claims to know it (a failed call re-uploads next time)
+  const int k = SlotOf(h);
+  shadow_[k].clear();
   double tt = t;
   Check(spc_step(h, &tt, dt, nsteps), h);
   Check(spc_download_state(h, state.data()), h);
-  int k = 0;
-  while (handles_[k] != h) ++k;
   shadow_[k] = state;
   t = tt;
 }
@@ -183,6 +190,8 @@ long SpcSystemBase::Run(int stepper, std::vector<Real> &state, Real &t, Real dt,
     Check(spc_inject_noise(h, injected_.data(), (int64_t)injected_.size()), h);
     inject_pending_ = false;
   }
+  const int k = SlotOf(h);
+  shadow_[k].clear();  // as in Advance: an error or a throwing observer re-uploads next time
   RunCall call{&on_state, nullptr};
   double tt = t;
   int64_t done = 0;
@@ -191,8 +200,6 @@ long SpcSystemBase::Run(int stepper, std::vector<Real> &state, Real &t, Real dt,
   if (call.error) std::rethrow_exception(call.error);
   Check(rc, h);
   Check(spc_download_state(h, state.data()), h);
-  int k = 0;
-  while (handles_[k] != h) ++k;
   shadow_[k] = state;
   t = tt;
   return (long)done;

@@ -129,6 +129,7 @@ class SpcSystemBase {
  protected:
   // the library model of the handle for stepper kind `stepper`
   virtual int ModelFor(int stepper) const { (void)stepper; return model_; }
+  int SlotOf(const spc_handle *h) const;  // index of h in handles_
   void Sync(spc_handle *h, const std::vector<Real> &state);
   void Check(int rc, spc_handle *h) const;
   void RhsRk(const Real *state, const Real *k_prev, Real *k_next, Real k_coef, Real dt);
