@@ -1,13 +1,18 @@
 // The drop-in adapters' host logic against the host-memory stand-in of the
-// C-ABI (fake_spc.cpp): state shadows, frequencies reaching every handle, and
-// recovery after a failed step or a throwing observer.  Prints one line per
+// C-ABI (fake_spc.cpp): state shadows, frequencies reaching every handle,
+// recovery after a failed step or a throwing observer, and the observer files
+// of the device loop against the per-step engine loop.  Prints one line per
 // case and exits non-zero on the first failure.
 #include <cmath>
 #include <cstdio>
+#include <fstream>
+#include <iterator>
+#include <string>
 #include <stdexcept>
 #include <vector>
 
 #include "../../spc2_langevin_integration_gb300/host/spc_dropin.hpp"
+#include "../../spc2_langevin_integration_gb300/host/spc_observer.hpp"
 
 const int kN = 4;
 const Real kL = 1.0;
@@ -142,6 +147,61 @@ int throwing_observer_reuploads_the_callers_state() {
   return 0;
 }
 
+std::string slurp(const std::string &path) {
+  std::ifstream f(path, std::ios::binary);
+  return std::string(std::istreambuf_iterator<char>(f), std::istreambuf_iterator<char>());
+}
+
+// The engine loop of SimulationEngine::RunSimulation (DoStep, then both
+// observer calls, every step) against RunObserved on the device loop: the same
+// frames and summary lines, byte for byte, at several output thresholds, and
+// when the device loop takes over from steps run one at a time.
+int observed_loop_writes_the_per_step_files() {
+  const int thresholds[][2] = {{1, 1}, {3, 2}, {10, 10}, {4, 6}};
+  int trial = 0;
+  for (const auto &th2 : thresholds) {
+    Thread th(0, nullptr);
+    PeriodicBoundaryConditions pbc(&th, kL, kL);
+    ChimeraSystem a(&th, 0.01, 1.0, 0.1, 1.45, 0.0, 1.0, pbc), b(&th, 0.01, 1.0, 0.1, 1.45, 0.0, 1.0, pbc);
+    StochasticEulerStepper stepper(&th);
+    BinaryObserver oa(&th, 0.01, 1.0, 0.1, 1.45, 0.0, 1.0, pbc, 0.1, 2 * trial);
+    BinaryObserver ob(&th, 0.01, 1.0, 0.1, 1.45, 0.0, 1.0, pbc, 0.1, 2 * trial + 1);
+    ++trial;
+    oa.SetOutputThresholds(th2[0], th2[1]);
+    ob.SetOutputThresholds(th2[0], th2[1]);
+    std::vector<Real> sa = start_state(), sb = start_state();
+    Real ta = 0.0, tb = 0.0;
+    const Real dt = 0.1;
+    for (int k = 0; k < 28; ++k) {  // the reference's loop
+      stepper.DoStep(a, sa, ta, dt);
+      ta += dt;
+      oa.SaveSystemState(sa, ta);
+      oa.SaveSummaryStatistics(sa, ta);
+    }
+    for (int k = 0; k < 5; ++k) {  // five steps one at a time, then the device loop
+      stepper.DoStep(b, sb, tb, dt);
+      tb += dt;
+      ob.SaveSystemState(sb, tb);
+      ob.SaveSummaryStatistics(sb, tb);
+    }
+    RunObserved(b, SPC_STEPPER_EULER, sb, tb, dt, 23, &ob);
+    CHECK(sa == sb && std::fabs(ta - tb) < 1e-12);
+    // one more call of each after the device loop: the counters must agree too
+    oa.SaveSystemState(sa, ta);
+    oa.SaveSummaryStatistics(sa, ta);
+    ob.SaveSystemState(sb, tb);
+    ob.SaveSummaryStatistics(sb, tb);
+    const std::string fa = slurp(oa.SimulationFileName()), fb = slurp(ob.SimulationFileName());
+    const std::string qa = slurp(oa.SummaryStatisticsFileName()), qb = slurp(ob.SummaryStatisticsFileName());
+    CHECK(!fa.empty() && fa == fb);
+    CHECK(!qa.empty() && qa == qb);
+    // frames written: ceil(29 / threshold), each 4 bytes of time + 3N float32
+    CHECK(fa.size() == (size_t)((29 + th2[0] - 1) / th2[0]) * (1 + 3 * kN) * 4);
+  }
+  std::printf("ok observed_loop_writes_the_per_step_files\n");
+  return 0;
+}
+
 }  // namespace
 
 int main() {
@@ -149,5 +209,6 @@ int main() {
   if (state_is_uploaded_only_when_it_changed()) return 1;
   if (failed_step_reuploads_the_callers_state()) return 1;
   if (throwing_observer_reuploads_the_callers_state()) return 1;
+  if (observed_loop_writes_the_per_step_files()) return 1;
   return 0;
 }
