@@ -44,8 +44,8 @@ ALG_BYTES = {
 }
 ALG_BYTES_STEP = 168 + 8      # survey accounting for the whole SRK step (+ omega)
 # DRAM bytes (read + write) per launch of the dominant kernel (k_tile_fp32c,
-# SRK pass 1) at this workload, from one ncu capture; the command and the raw
-# figures are in profiles/k_tile_fp32c_vortex_srk_n65536.md.
+# SRK pass 1) at this workload, from one ncu --set full capture of that
+# kernel (`--ncu-case fp32c --cell-list`).
 NCU_TRAFFIC_PASS1 = 2.41e6
 # The same capture's instruction-issue figures for that kernel: issue slots
 # used on the cycles an SM was active, and the SMs' active share of the
@@ -385,6 +385,83 @@ def run_drift(steps=10000, every=100, out_path=None, seed=None):
     return res
 
 
+def run_drift_ensemble(forms, steps=5000, every=100, subset=None, series_path=None):
+    """Per-system drift of the order parameters over the batched ensemble (512
+    Chimera systems, Euler, dt = 0.01): one batch per precision form and one
+    FP64 batch, the same systems, seeds and Philox counters, stepped `every`
+    steps at a time as graph replays; R and R_local of every system after each
+    chunk.  forms: (name, precision) pairs compared against the FP64 batch.
+    A control arm, FP64 from the initial state with every phase moved by one
+    ulp, measures the dynamics' own sensitivity: a system that this arm
+    leaves beyond 1e-4 cannot be followed pointwise by any arithmetic that is
+    not FP64 bit for bit.  Returns, per arm, the maximum |delta| over systems
+    and recorded points, its distribution over the systems, how many systems
+    stay within 1e-4, and (forms) how many of those beyond 1e-4 the control
+    arm also leaves beyond it."""
+    from spc2_langevin_integration_gb300 import abi
+    systems = ensemble_systems()
+    if subset is not None:
+        systems = [systems[i] for i in subset]
+    ntot = sum(n for _, n, _, _, _ in systems)
+    ctot = sum(abi.cells_of(L, prm["rho"]) for _, _, L, prm, _ in systems)
+    cap = len(systems)
+
+    def make(prec, ulp=False):
+        b = abi.Batch(abi.STEPPER_EULER, prec, cap, ntot, ctot)
+        slots = []
+        for k, n, L, prm, st in systems:
+            p = abi.make_params(L=L, stepper=abi.STEPPER_EULER, precision=prec, seed=2,
+                                system_id=k, **prm)
+            if ulp:
+                st = st.copy()
+                st[2::3] = np.nextafter(st[2::3], np.inf)
+            slots.append(b.admit(n, p, st))
+        return b, np.array(slots)
+
+    arms = [("fp64", abi.PRECISION_FP64)] + list(forms) + [("fp64_one_ulp_phases", abi.PRECISION_FP64)]
+    batches = {name: make(prec, ulp=name.endswith("ulp_phases")) for name, prec in arms}
+    rec = {name: {"R": [], "R_local": []} for name, _ in arms}
+    for k in range(every, steps + 1, every):
+        for name, (b, slots) in batches.items():
+            b.step(0.01, every, graph=True)
+            o = b.order_params_all(cap)
+            rec[name]["R"].append(o["R"][slots])
+            rec[name]["R_local"].append(o["R_local"][slots])
+    for b, _ in batches.values():
+        b.close()
+    ref = {q: np.array(rec["fp64"][q]) for q in ("R", "R_local")}
+    sizes = np.array([n for _, n, _, _, _ in systems])
+    out = {"systems": len(systems), "particles": int(ntot), "steps": steps, "every": every,
+           "reference": "FP64 batch (same systems, seeds and Philox counters)"}
+    ctrl = {q: np.abs(np.array(rec["fp64_one_ulp_phases"][q]) - ref[q]).max(axis=0)
+            for q in ("R", "R_local")}
+    for name, _ in list(forms) + [("fp64_one_ulp_phases", None)]:
+        res = {}
+        for q in ("R", "R_local"):
+            d = np.abs(np.array(rec[name][q]) - ref[q])   # [points, systems]
+            per_sys = d.max(axis=0)
+            beyond = per_sys > 1e-4
+            worst = int(per_sys.argmax())
+            first = [int(np.argmax(d[:, s] > 1e-4)) if (d[:, s] > 1e-4).any() else -1
+                     for s in range(d.shape[1])]
+            res[q] = {"max_abs": float(per_sys.max()), "mean_abs": float(d.mean()),
+                      "per_system_max_quantiles": {str(p): float(np.quantile(per_sys, p))
+                                                   for p in (0.5, 0.9, 0.99)},
+                      "systems_within_1e-4": int((per_sys <= 1e-4).sum()),
+                      "beyond_1e-4_also_beyond_in_control": int((beyond & (ctrl[q] > 1e-4)).sum()),
+                      "worst_system": {"index": int(systems[worst][0]), "N": int(sizes[worst]),
+                                       "max_abs": float(per_sys[worst])},
+                      "median_first_step_over_1e-4": (
+                          float(np.median([every * (f + 1) for f in first if f >= 0]))
+                          if any(f >= 0 for f in first) else None)}
+        out[name] = res
+    if series_path:
+        with open(series_path, "w") as f:
+            json.dump({name: {q: np.array(v).tolist() for q, v in r.items()}
+                       for name, r in rec.items()}, f)
+    return out
+
+
 LARGE = dict(name="chimera_rk4_n4194304_L64", n=1 << 22, L=64.0, v0=0.01, sigma=1.0, rho=0.25,
              alpha=1.45, D_phi=0.0, dt=0.01, seed=0, skin=0.05)
 
@@ -673,6 +750,92 @@ def run_form(abi, torch, w, precision, steps, warmup, rank, dist, params=None, s
     return ms, e2e_ms, prof, R, launches
 
 
+def run_configured(abi, torch, w, precision, params, sparse_below, steps, warmup, rank, dist,
+                   total_steps=None):
+    """The whole configured run of the workload (w["steps"] simulation steps
+    from the seeded initial state, Philox counters from 0), split into `steps`
+    bench steps of total_steps / steps simulation steps each (graph replays of
+    100).  One pass gives both measurements:
+      * device time: CUDA events on the library's stream around each bench
+        step's replays (inputs resident in HBM);
+      * end to end: wall clock around each bench step's call cycle through the
+        C-ABI with pinned host buffers: upload of the step's input state, the
+        replays, download of its result (the same state values, so the
+        trajectory is the one the device-time measurement follows).
+    L2 is flushed (a 512 MB write) before each bench step, outside both timers.
+    `warmup` bench steps run first (graph capture, caches); then the state and
+    the step counter are reset, so the timed steps are the configured run.
+    After each bench step, outside the timers, the global and local order
+    parameters are recorded (the drift series)."""
+    import ctypes as C
+    n = w["n"]
+    total = total_steps or w["steps"]
+    per = total // steps
+    if per % SIM_STEPS_PER_BENCH_STEP or per <= 0:
+        raise ValueError(f"--steps must divide the {total}-step run into multiples of 100 steps")
+    reps = per // SIM_STEPS_PER_BENCH_STEP
+    st, omega = init_inputs(w, seed_offset=rank)
+    s = abi.System(n, params)
+    if sparse_below is not None and params.neighbour == abi.NEIGHBOUR_CELL:
+        s.set_tuning(abi.TUNE_SPARSE_BELOW, sparse_below)
+    s.upload_omega(omega)
+    stream = torch.cuda.ExternalStream(s.stream)
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    dt = w["dt"]
+    L = abi.lib()
+    q = C.c_void_p()
+    L.spc_alloc_pinned(3 * n * 8, C.byref(q))
+    host = np.ctypeslib.as_array((C.c_double * (3 * n)).from_address(q.value))
+    s.upload_state(st)
+    for _ in range(warmup):
+        for _ in range(reps):
+            s.step(dt, SIM_STEPS_PER_BENCH_STEP, graph=True)
+    s.synchronize()
+    host[:] = st
+    s.upload_state(host)
+    s.step_counter = 0
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+          for _ in range(steps)]
+    wall, series = [], []
+    if dist is not None:
+        dist.barrier()
+    torch.cuda.synchronize()
+    for k in range(steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        s.upload_state(host)
+        ev[k][0].record(stream)
+        for _ in range(reps):
+            s.step(dt, SIM_STEPS_PER_BENCH_STEP, graph=True)
+        ev[k][1].record(stream)
+        s.download_state(host)
+        wall.append((time.perf_counter() - t0) * 1e3)
+        o = s.order_params()
+        series.append((per * (k + 1), o["R"], o["R_local"]))
+    torch.cuda.synchronize()
+    if dist is not None:
+        dist.barrier()
+    ms = reduce_max(dist, sum(a.elapsed_time(b) for a, b in ev))
+    e2e_ms = reduce_max(dist, sum(wall))
+    launches = s.graph_nodes() * reps * steps
+    prof = s.profile_steps(dt, 20)  # on the final (clustered) state
+    del host
+    L.spc_free_pinned(q)
+    s.close()
+    return {"ms": ms, "e2e_ms": e2e_ms, "steps_per_bench_step": per, "series": series,
+            "profile_ms": prof, "launches": launches,
+            "ms_per_bench_step": [a.elapsed_time(b) for a, b in ev]}
+
+
+def drift_of(ref_series, series):
+    """max |delta| of R and R_local over the recorded points."""
+    a, b = np.array(ref_series), np.array(series)
+    return {"max_dR": float(np.abs(b[:, 1] - a[:, 1]).max()),
+            "max_dR_local": float(np.abs(b[:, 2] - a[:, 2]).max()),
+            "points": len(a), "every_steps": int(a[0, 0])}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -690,7 +853,7 @@ def main():
     ap.add_argument("--ensemble-shard", action="store_true",
                     help="ensemble on N GPUs: partition the 512 systems over the ranks by "
                          "footprint (strong scaling) instead of one full ensemble per rank")
-    ap.add_argument("--form", choices=["fp32c", "fp64"], default=None,
+    ap.add_argument("--form", choices=["fp32c", "fp32x", "fp64"], default=None,
                     help="time only this precision form of the workload with --neighbour / "
                          "--skin (no autotune): the command for a launch list of the timed region")
     ap.add_argument("--neighbour", choices=["cell", "verlet"], default="cell")
@@ -700,11 +863,14 @@ def main():
     ap.add_argument("--cell-list", action="store_true",
                     help="--ncu-case fp32c/fp64: the cell-list passes instead of the Verlet rows")
     ap.add_argument("--workload",
-                    choices=["vortex", "ensemble", "serve", "drift", "large", "va", "observed"],
+                    choices=["vortex", "ensemble", "serve", "drift", "drift-ensemble", "large", "va",
+                             "observed"],
                     default="vortex",
                     help="vortex: the headline single-system line; ensemble: 512 systems in one "
                          "batch; serve: the Poisson request stream; drift: FP32C vs FP64 order "
-                         "parameters over 10^4 steps; large: Chimera RK4, N=2^22, L=64; va: the "
+                         "parameters over 10^4 steps; drift-ensemble: per-system order-parameter "
+                         "drift of the 512-system ensemble against FP64 over 5,000 steps; "
+                         "large: Chimera RK4, N=2^22, L=64; va: the "
                          "vortex-arrays model, N=51,200, L=8; observed: the headline workload "
                          "with a frame every 10 steps, per-step loop vs the device loop")
     ap.add_argument("--sparse-below", type=float, default=None,
@@ -738,6 +904,7 @@ def main():
             subset = replicas.shard(sizes, world, rank)
         res = {}
         runs = [("fp32c", abi.PRECISION_FP32C, 20, args.sparse_below),
+                ("fp32x", abi.PRECISION_FP32X, 20, args.sparse_below),
                 ("fp64", abi.PRECISION_FP64, 3, args.sparse_below)]
         if args.compare_kernels:
             runs += [("fp32c_tile_only", abi.PRECISION_FP32C, 5, 0.0),
@@ -758,6 +925,7 @@ def main():
                               "systems": 512, "particles": ntot, "cells": ctot,
                               **res,
                               "fp32c_over_fp64": res["fp32c"]["value"] / res["fp64"]["value"],
+                              "fp32x_over_fp64": res["fp32x"]["value"] / res["fp64"]["value"],
                               "graph_steps": 100, "l2": "working set > L2 (about 1 GB)",
                               "cpu_baseline": cpu}))
         if dist is not None:
@@ -780,6 +948,15 @@ def main():
     if args.workload == "drift":
         out = {"metric": "order-parameter drift, FP32C vs FP64", "workload": "drift"}
         out.update(run_drift(steps=args.drift_steps, out_path=args.drift_series, seed=args.drift_seed))
+        print(json.dumps(out))
+        return
+    if args.workload == "drift-ensemble":
+        from spc2_langevin_integration_gb300 import abi
+        out = {"metric": "order-parameter drift vs FP64, per system", "workload": "ensemble_512_euler"}
+        subset = list(range(args.ensemble_systems)) if args.ensemble_systems < 512 else None
+        out.update(run_drift_ensemble([("fp32c", abi.PRECISION_FP32C), ("fp32x", abi.PRECISION_FP32X)],
+                                      steps=min(args.drift_steps, 5000), subset=subset,
+                                      series_path=args.drift_series))
         print(json.dumps(out))
         return
     if args.workload == "observed":
@@ -884,7 +1061,8 @@ def main():
     from spc2_langevin_integration_gb300 import abi
     torch.cuda.set_device(local)
     if args.form:
-        prec = abi.PRECISION_FP32C if args.form == "fp32c" else abi.PRECISION_FP64
+        prec = {"fp32c": abi.PRECISION_FP32C, "fp32x": abi.PRECISION_FP32X,
+                "fp64": abi.PRECISION_FP64}[args.form]
         p = workload_params(abi, w, prec, rank)
         p.neighbour = abi.NEIGHBOUR_VERLET if args.neighbour == "verlet" else abi.NEIGHBOUR_CELL
         if args.skin is not None:
@@ -945,9 +1123,10 @@ def main():
                                  "candidates_per_particle": cand, "pairs_per_particle": pairs,
                                  "issue_frac": (NCU_ISSUE_ACTIVE_PASS1 * NCU_SM_ACTIVE_PASS1
                                                 if dom == "pass1" else None),
-                                 "issue_frac_source": "ncu (profiles/k_tile_fp32c_vortex_srk_n65536"
-                                                      ".md): issue-active share of active cycles "
-                                                      "x SM-active share of elapsed cycles"},
+                                 "issue_frac_source": "ncu --set full capture of this kernel at "
+                                                      "this workload: issue-active share of "
+                                                      "active cycles x SM-active share of "
+                                                      "elapsed cycles"},
                      "note": "the passes are bound by issue / latency (float prefilter and "
                              "per-pair trig on an L2-resident working set), not by HBM: the "
                              "HBM fraction is low by construction"},

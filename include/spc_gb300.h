@@ -72,8 +72,19 @@ enum { SPC_NEIGHBOUR_CELL = 0, SPC_NEIGHBOUR_VERLET = 1 };
 /* Precision.  FP64: every value and operation in double, in the reference's
  * order.  FP32C: neighbour sums, sin/cos and stage updates in float with
  * compensated (Kahan) accumulation; the cutoff / minimum-image decision, the
- * wrapped positions and the accumulated phase stay double. */
-enum { SPC_PRECISION_FP64 = 0, SPC_PRECISION_FP32C = 1 };
+ * wrapped positions and the accumulated phase stay double.
+ * FP32X: the per-pair work stays off the FP64 pipe (float prefilter, the
+ * exact FP64 test only near the cutoff), and the neighbour sums are exact:
+ * each particle's cos phi and sin phi (and, for the SRK second pass, the
+ * same weighted by its phase rate) are rounded once to 64-bit fixed point
+ * (2^-52 resolution) and summed as integers, which is exact and independent
+ * of order.  The per-particle work (sin/cos, the angle-addition identity
+ * sin(phi_j - phi_i - alpha) = sin phi_j cos(phi_i + alpha) - cos phi_j
+ * sin(phi_i + alpha), the stepper update and the noise) is FP64 with the
+ * plain form's formulas and normals, so results follow the FP64 form to a
+ * few 1e-16 relative per right-hand side.  Cell list and all pairs only
+ * (SPC_NEIGHBOUR_VERLET is refused); the Chimera and vortex models. */
+enum { SPC_PRECISION_FP64 = 0, SPC_PRECISION_FP32C = 1, SPC_PRECISION_FP32X = 2 };
 
 /* flags */
 #define SPC_FLAG_EXACT_ALL 0x1u /* decide every candidate pair in FP64 (no float prefilter) */
@@ -313,6 +324,12 @@ int spc_batch_upload(spc_batch *b, int32_t slot, const double *aos3n);
 int spc_batch_status(spc_batch *b, int32_t slot, uint64_t *steps_done, int64_t *remaining);
 int spc_batch_usage(spc_batch *b, int64_t *particles, int64_t *cells, int32_t *systems);
 int spc_batch_order_params(spc_batch *b, int32_t slot, double *R, double *psi);
+/* Order parameters of every system of the batch in one call (the per-frame
+ * summary of BinaryObserver.cpp:196-210 for each system, plus the local order
+ * parameter of spc_order_params): entry s of R, psi and R_local (each may be
+ * NULL) is slot s's, for s < cap; slots without a system get NaN.  One
+ * diagnostics pass over the whole batch; synchronises the batch's stream. */
+int spc_batch_order_params_all(spc_batch *b, int32_t cap, double *R, double *psi, double *R_local);
 int spc_batch_synchronize(spc_batch *b);
 void *spc_batch_stream(spc_batch *b);
 /* Per-phase device time of nsteps steps of the whole batch (as
@@ -333,11 +350,17 @@ int spc_batch_get_tuning(const spc_batch *b, int32_t key, double *value);
  * waiting.  Intermediates live in one static device array of about 1.1 MB
  * that every GPU loading the library keeps until the process exits; limits:
  * n <= 8192 particles and int(L/rho)^2 <= 16384 cells, larger sizes return
- * SPC_ERR_CAPACITY.  The first call on a device looks up that array's device
- * address (once per device, with the device current), so make it before any
- * stream capture.  All calls share the one array: calls whose work overlaps
- * on the GPU (different streams, or different host threads) race and must be
- * ordered by the caller. */
+ * SPC_ERR_CAPACITY.  The Chimera and vortex models are supported; the
+ * vortex-arrays model returns SPC_ERR_INVALID.  Positions in d_state must
+ * already be wrapped into [0, L), as after any step: the call does not wrap
+ * them, and cell indices of positions outside are clamped without a report.
+ * The first call on a device looks up that array's device address (with the
+ * device current) and caches it with the current context; a call in another
+ * context, e.g. after cudaDeviceReset, looks it up again.  So make the first
+ * call, and the first after a reset, before any stream capture.  All calls
+ * share the one array: calls whose work overlaps on the GPU (different
+ * streams, or different host threads) race and must be ordered by the
+ * caller. */
 int spc_rhs_srk_noalloc(const spc_params *p, int32_t n, const double *d_state,
                         double *d_derivative, double *d_additional, void *stream);
 

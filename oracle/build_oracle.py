@@ -21,7 +21,10 @@ BUILD = os.path.join(HERE, "_build")
 REF_OUT = os.path.join(HERE, "_ref")
 LIB = os.path.join(BUILD, "libspc_oracle.so")
 REF_BIN = os.path.join(REF_OUT, "spc_ref")
-REFERENCE_ROOT = os.environ.get("SPC_REFERENCE_ROOT", "/root/reference")
+# The reference checkout: SPC_REFERENCE_ROOT, else a `reference` directory
+# beside the repository's own.
+REFERENCE_ROOT = (os.environ.get("SPC_REFERENCE_ROOT")
+                  or os.path.join(os.path.dirname(os.path.dirname(HERE)), "reference"))
 
 # The reference translation units the particle-update path needs.
 REF_SOURCES = [
@@ -33,6 +36,7 @@ REF_SOURCES = [
     "Steppers/RungeKutta4Stepper.cpp",
     "Steppers/RungeKutta4StepperPtr.cpp",
     "DynamicalSystems/VortexArraysSystemPtr.cpp",
+    "Observers/BinaryObserver.cpp",
 ]
 
 FP_FLAGS = ["-O2", "-ffp-contract=off", "-fno-fast-math"]

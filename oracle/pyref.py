@@ -15,7 +15,7 @@ import numpy as np
 
 from . import build_oracle
 
-MODE_RUN, MODE_RHS_RK, MODE_RHS_SRK = 0, 1, 2
+MODE_RUN, MODE_RHS_RK, MODE_RHS_SRK, MODE_OBSERVE = 0, 1, 2, 3
 FAMILY_VECTOR, FAMILY_PTR, FAMILY_VA = 0, 1, 2
 STEP_EULER, STEP_SRK, STEP_RK4 = 0, 1, 2
 

@@ -12,7 +12,11 @@
 // mode 0 = run the engine loop (SimulationEngine.cpp:149-161 / SimulationEnginePtr.cpp:106-115)
 //          nsteps times and write the state every record_every steps (and at the end);
 // mode 1 = one RK-form EvaluateRhs -> k_next[3N];
-// mode 2 = one SRK-form EvaluateRhs -> derivative[3N] then additional[2N] ([i][0], [i][1]).
+// mode 2 = one SRK-form EvaluateRhs -> derivative[3N] then additional[2N] ([i][0], [i][1]);
+// mode 3 = the engine loop of SimulationEngine.cpp:113-127 with the reference's
+//          BinaryObserver (family 0): the initial frame at t0, then after every
+//          step the frame and the summary line, into SPC_REF_OUT_DIR; every
+//          state after a step is written to the output.
 // family 0 = vector classes (Thread, ChimeraSystem, *Stepper);
 // family 1 = shared-window classes (ThreadSharedMemory, ChimeraSystemPtr, *StepperPtr);
 // family 2 = VortexArraysSystemPtr with the *StepperPtr classes; its five extra
@@ -31,11 +35,13 @@
 #include "Steppers/StochasticEulerStepperPtr.hpp"
 #include "Steppers/StochasticRungeKuttaStepperPtr.hpp"
 #include "Steppers/RungeKutta4StepperPtr.hpp"
+#include "Observers/BinaryObserver.hpp"
 
 #include <cstdint>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <string>
 #include <vector>
 
 static int env_int(const char *k) {
@@ -68,6 +74,18 @@ double next_injected_normal() {
     std::exit(3);
   }
   return g_noise[g_pos++];
+}
+
+// BinaryObserver's output folder (see ref_prelude.hpp): SPC_REF_OUT_DIR.
+const char *output_folder(const char *) {
+  static std::string folder;
+  const char *d = std::getenv("SPC_REF_OUT_DIR");
+  if (!d) {
+    std::fprintf(stderr, "spc_ref: SPC_REF_OUT_DIR is not set\n");
+    std::exit(2);
+  }
+  folder = std::string(d) + "/";
+  return folder.c_str();
 }
 }  // namespace spc_ref
 
@@ -127,6 +145,26 @@ int main(int argc, char **argv) {
       system.EvaluateRhs(state, derivative, additional, h.dt);
       dump(derivative.data(), n3);
       for (int i = 0; i < kN; ++i) dump(additional[i].data(), 2);
+    } else if (h.mode == 3) {
+      StochasticEulerStepper euler(&thread);
+      StochasticRungeKuttaStepper srk(&thread);
+      RungeKutta4Stepper rk4(&thread);
+      BinaryObserver observer(&thread, h.v0, h.sigma, h.rho, h.alpha, h.D_phi, h.rho_0, pbc, h.dt, 0);
+      Real t = h.t0;
+      observer.SaveSystemState(state, t);
+      for (int k = 1; k <= h.nsteps; ++k) {
+        t += h.dt;
+        if (h.stepper == 0)
+          euler.DoStep(system, state, t, h.dt);
+        else if (h.stepper == 1)
+          srk.DoStep(system, state, t, h.dt);
+        else
+          rk4.DoStep(system, state, t, h.dt);
+        pbc.ApplyPeriodicBoundaryConditions(state);
+        observer.SaveSystemState(state, t);
+        observer.SaveSummaryStatistics(state, t);
+        dump(state.data(), n3);
+      }
     } else {
       StochasticEulerStepper euler(&thread);
       StochasticRungeKuttaStepper srk(&thread);

@@ -17,7 +17,7 @@ from . import build as _build
 MODEL_CHIMERA, MODEL_VORTEX, MODEL_VORTEX_ARRAYS = 0, 1, 2
 STEPPER_EULER, STEPPER_SRK, STEPPER_RK4, STEPPER_EULER_PTR = 0, 1, 2, 3
 NEIGHBOUR_CELL, NEIGHBOUR_VERLET = 0, 1
-PRECISION_FP64, PRECISION_FP32C = 0, 1
+PRECISION_FP64, PRECISION_FP32C, PRECISION_FP32X = 0, 1, 2
 FLAG_EXACT_ALL = 0x1
 TUNE_SPARSE_BELOW = 1
 TUNE_VERLET_ROW_LIMIT = 2
@@ -123,6 +123,7 @@ def lib() -> C.CDLL:
     L.spc_batch_usage.argtypes = [H, C.POINTER(C.c_int64), C.POINTER(C.c_int64),
                                   C.POINTER(C.c_int32)]
     L.spc_batch_order_params.argtypes = [H, C.c_int32, dp, dp]
+    L.spc_batch_order_params_all.argtypes = [H, C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p]
     L.spc_batch_synchronize.argtypes = [H]
     L.spc_batch_stream.restype = C.c_void_p
     L.spc_batch_stream.argtypes = [H]
@@ -510,6 +511,15 @@ class Batch:
         R, psi = C.c_double(), C.c_double()
         self._check(self._L.spc_batch_order_params(self.h, int(slot), C.byref(R), C.byref(psi)))
         return {"R": R.value, "psi": psi.value}
+
+    def order_params_all(self, cap: int, local: bool = True):
+        """R, psi and (local=True) R_local of slots [0, cap) as float64
+        arrays, NaN where a slot holds no system."""
+        R, psi = np.empty(cap), np.empty(cap)
+        Rl = np.empty(cap) if local else None
+        self._check(self._L.spc_batch_order_params_all(self.h, int(cap), _ptr(R), _ptr(psi),
+                                                       _ptr(Rl) if local else None))
+        return {"R": R, "psi": psi, "R_local": Rl}
 
     def synchronize(self):
         self._check(self._L.spc_batch_synchronize(self.h))

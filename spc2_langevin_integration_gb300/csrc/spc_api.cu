@@ -2,6 +2,7 @@
 // engine (spc_engine.cuh) holding one system; a batch holds many and runs
 // them in the same launches.  No CPU fallback: every entry point that
 // computes launches the kernels of spc_kernels.cuh / spc_tile.cuh / spc_sort.cuh.
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -694,6 +695,7 @@ int spc_autotune(const spc_params *p, int32_t n, const double *aos3n, const doub
                              {SPC_NEIGHBOUR_CELL, p->skin, 0.0},
                              {SPC_NEIGHBOUR_CELL, p->skin, 1e9}};
   for (double f : {0.1, 0.2, 0.4}) {
+    if (p->precision == SPC_PRECISION_FP32X) break;  // the FP32X form runs the cell list
     spc_params q = *p;
     q.neighbour = SPC_NEIGHBOUR_VERLET;
     q.skin = f * p->rho;
@@ -845,7 +847,8 @@ int spc_batch_create(const spc_batch_config *cfg, spc_batch **out) {
     return fail(nullptr, SPC_ERR_INVALID, "bad batch capacities");
   if (cfg->stepper < SPC_STEPPER_EULER || cfg->stepper > SPC_STEPPER_EULER_PTR)
     return fail(nullptr, SPC_ERR_INVALID, "unknown stepper");
-  if (cfg->precision != SPC_PRECISION_FP64 && cfg->precision != SPC_PRECISION_FP32C)
+  if (cfg->precision != SPC_PRECISION_FP64 && cfg->precision != SPC_PRECISION_FP32C &&
+      cfg->precision != SPC_PRECISION_FP32X)
     return fail(nullptr, SPC_ERR_INVALID, "unknown precision");
   spc_batch *b = new spc_batch();
   int rc = engine_init(&b->e, cfg->stepper, cfg->precision, (int)cfg->max_particles, cfg->max_systems,
@@ -962,6 +965,12 @@ int spc_batch_order_params(spc_batch *b, int32_t slot, double *R, double *psi) {
   return engine_order_global(&b->e, slot, R, psi);
 }
 
+int spc_batch_order_params_all(spc_batch *b, int32_t cap, double *R, double *psi, double *R_local) {
+  if (!b || cap < 0) return fail(b ? &b->e : nullptr, SPC_ERR_INVALID, "bad argument");
+  SPC_TRY(engine_set_device(&b->e));
+  return engine_order_all(&b->e, cap, R, psi, R_local);
+}
+
 int spc_batch_synchronize(spc_batch *b) {
   if (!b) return fail(nullptr, SPC_ERR_INVALID, "NULL argument");
   SPC_TRY(engine_set_device(&b->e));
@@ -1023,7 +1032,11 @@ constexpr size_t kNoAllocBytes =
 
 constexpr int kNoAllocMaxDevices = 64;
 std::mutex g_noalloc_mu;
+// per device: the array's device address and the unique ID of the context it
+// was looked up in (a reset device gets a new context, and the module's
+// arrays may then sit at other addresses)
 char *g_noalloc_base[kNoAllocMaxDevices] = {};
+unsigned long long g_noalloc_ctx[kNoAllocMaxDevices] = {};
 
 }  // namespace
 
@@ -1031,21 +1044,54 @@ static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];
 
 namespace {
 
+// Unique ID of the calling thread's current context, 0 when there is none
+// or the driver does not report it.  The driver's cuCtxGetCurrent and
+// cuCtxGetId are reached through the runtime's entry-point query, so the
+// library does not link libcuda itself.
+unsigned long long current_context_id() {
+  typedef CUresult (*GetCurrent)(CUcontext *);
+  typedef CUresult (*GetId)(CUcontext, unsigned long long *);
+  static GetCurrent get_current = nullptr;
+  static GetId get_id = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    void *f = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      get_current = (GetCurrent)f;
+    f = nullptr;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      get_id = (GetId)f;
+  });
+  if (!get_current || !get_id) return 0;
+  CUcontext c = nullptr;
+  if (get_current(&c) != CUDA_SUCCESS || !c) return 0;
+  unsigned long long id = 0;
+  return get_id(c, &id) == CUDA_SUCCESS ? id : 0;
+}
+
 // Device address of g_noalloc_scratch on the current device.  In host code
-// the symbol name is only a stand-in, so the address is looked up once per
-// device with that device current and cached.
+// the symbol name is only a stand-in, so the address is looked up with the
+// device current and cached per device together with the context it belongs
+// to; a call in a different context (after cudaDeviceReset, say) looks it up
+// again.  When the context's ID is unknown, every call looks it up.
 int noalloc_scratch(char **out) {
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return fail(nullptr, SPC_ERR_CUDA, "cudaGetDevice: %s", cudaGetErrorString(e));
   if (dev < 0 || dev >= kNoAllocMaxDevices) return fail(nullptr, SPC_ERR_INVALID, "device %d out of range", dev);
   std::lock_guard<std::mutex> lk(g_noalloc_mu);
-  if (!g_noalloc_base[dev]) {
+  const unsigned long long ctx = current_context_id();
+  if (!g_noalloc_base[dev] || ctx == 0 || ctx != g_noalloc_ctx[dev]) {
     void *ptr = nullptr;
     e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
     if (e != cudaSuccess || !ptr)
       return fail(nullptr, SPC_ERR_CUDA, "cudaGetSymbolAddress(scratch): %s", cudaGetErrorString(e));
     g_noalloc_base[dev] = (char *)ptr;
+    // the lookup makes the device's primary context current if none was
+    g_noalloc_ctx[dev] = current_context_id();
   }
   *out = g_noalloc_base[dev];
   return SPC_OK;
@@ -1067,6 +1113,14 @@ extern "C" int spc_rhs_srk_noalloc(const spc_params *p, int32_t n, const double 
   if (rc) return fail(nullptr, rc, "%s", why.c_str());
   if (!d_state || !d_derivative || !d_additional)
     return fail(nullptr, SPC_ERR_INVALID, "NULL device buffer");
+  // the scratch holds the cell-list and all-pairs intermediates of the
+  // alignment models; the vortex-arrays model's passes need tables of their own
+  if (p->model == SPC_MODEL_VORTEX_ARRAYS)
+    return fail(nullptr, SPC_ERR_INVALID,
+                "spc_rhs_srk_noalloc: the vortex-arrays model is not supported (use spc_rhs_srk)");
+  if (p->precision == SPC_PRECISION_FP32X)
+    return fail(nullptr, SPC_ERR_INVALID,
+                "spc_rhs_srk_noalloc: the FP32X form is not supported (FP64 and FP32C are)");
   if (n > kNoAllocMaxN)
     return fail(nullptr, SPC_ERR_CAPACITY, "spc_rhs_srk_noalloc: n = %d exceeds its maximum of %d particles",
                 n, kNoAllocMaxN);

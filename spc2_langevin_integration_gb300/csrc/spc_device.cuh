@@ -35,6 +35,30 @@ __device__ __forceinline__ double ddiv_by(double a, double b, double y) {
 __device__ __forceinline__ double drcp(double b) { return __drcp_rn(b); }
 __device__ __forceinline__ double dsqrt(double a) { return __dsqrt_rn(a); }
 
+// FP32X fixed point.  A value v with |v| <= 1 is held as the integer
+// RN(v 2^52); a staging round of at most 1024 candidates sums to less than
+// 2^62 in magnitude, so the integer sums are exact, and the conversion back
+// (one rounding to double) is the only error of a round's sum.
+constexpr int kXQ = 52;
+__device__ __forceinline__ long long to_fixed(double v, int q) {
+  return __double2ll_rn(scalbn(v, q));
+}
+__device__ __forceinline__ double from_fixed(long long v, int q) {
+  return scalbn(__ll2double_rn(v), -q);
+}
+// A particle's whole sum over several staging rounds is kept in 128 bits, so
+// it is one exact integer whatever the kernel's round size, and converted to
+// double once: one rounding when it fits 64 bits (always below 2^11
+// neighbours), else a fixed two-step conversion.  Either way the result
+// depends on the integer alone.
+__device__ __forceinline__ double from_fixed128(__int128 v, int q) {
+  const long long lo64 = (long long)v;
+  if ((__int128)lo64 == v) return scalbn(__ll2double_rn(lo64), -q);
+  const long long hi = (long long)(v >> 64);
+  const unsigned long long lo = (unsigned long long)v;
+  return scalbn(__fma_rn(__ll2double_rn(hi), 18446744073709551616.0, __ull2double_rn(lo)), -q);
+}
+
 // Per-system constants, the reference's ChimeraSystem / PeriodicBoundaryConditions
 // members (ChimeraSystem.cpp:19-33, PeriodicBoundaryConditions.cpp:13-14).
 struct SysConst {
@@ -52,6 +76,11 @@ struct SysConst {
   int exact_all;  // decide every candidate in FP64
   int L_pow2;     // L is a power of two: x / L == x * (1 / L) exactly
   float cos_a, sin_a;  // FP32C: cos(alpha), sin(alpha) rounded to float
+  // FP32X: cos(alpha), sin(alpha) in double, and the fixed-point exponent of
+  // the phase-rate-weighted sums of the SRK second pass (sum_j d_j cos phi_j,
+  // sum_j d_j sin phi_j): 2^xq2 per unit, |d_j| <= |sigma| < 2^(52 - xq2)
+  double cos_ad, sin_ad;
+  int xq2;
   // Verlet rows (vR = 0: the system uses the cell-list passes)
   int vR;         // stencil radius in cells, ceil(r_max / cell)
   float vr2;      // build: candidates with float dr^2 <= vr2 (r_max^2 plus a margin) are listed

@@ -19,6 +19,7 @@
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
+#include <limits>
 #include <mutex>
 #include <string>
 #include <vector>
@@ -83,6 +84,14 @@ inline SysConst make_sysconst(const spc_params &p, int n) {
   sc.L_pow2 = is_pow2(p.L);
   sc.cos_a = (float)std::cos(p.alpha);
   sc.sin_a = (float)std::sin(p.alpha);
+  sc.cos_ad = std::cos(p.alpha);
+  sc.sin_ad = std::sin(p.alpha);
+  {
+    // |phase rate| <= |sigma| (sigma times a mean of sines): 2^e >= |sigma|
+    int e = 0;
+    while (e < 40 && std::ldexp(1.0, e) < std::fabs(p.sigma)) ++e;
+    sc.xq2 = kXQ - e - 1;  // one more bit of headroom for the rate's rounding
+  }
   if (p.model == SPC_MODEL_VORTEX_ARRAYS) {
     sc.va = 1;
     sc.mu_plus = p.mu_plus;
@@ -144,8 +153,11 @@ inline int validate_params(const spc_params *p, int n, std::string &why) {
     return bad("the vortex model's natural frequencies enter the Euler and stochastic Runge-Kutta drifts only");
   if (p->neighbour != SPC_NEIGHBOUR_CELL && p->neighbour != SPC_NEIGHBOUR_VERLET)
     return bad("unknown neighbour search");
-  if (p->precision != SPC_PRECISION_FP64 && p->precision != SPC_PRECISION_FP32C)
+  if (p->precision != SPC_PRECISION_FP64 && p->precision != SPC_PRECISION_FP32C &&
+      p->precision != SPC_PRECISION_FP32X)
     return bad("unknown precision");
+  if (p->precision == SPC_PRECISION_FP32X && p->neighbour == SPC_NEIGHBOUR_VERLET)
+    return bad("the FP32X form runs the cell list (Verlet rows are built for FP64 and FP32C)");
   if (p->neighbour == SPC_NEIGHBOUR_VERLET && !(p->skin > 0.0)) return bad("Verlet skin must be positive");
   if (p->rho <= 0.25 * p->L && std::floor(p->L / p->rho) > 46340.0) return bad("too many cells");
   return SPC_OK;
@@ -296,6 +308,8 @@ inline void engine_footprint(int stepper, int precision, long long *per_particle
   if (stepper == SPC_STEPPER_RK4) b += 12 * 8;  // k1..k4
   b += 3 * 8 + 4 * 4 + 3 * 8 + 8 + 4 + 8 + 4 + 4 + 4;  // stage, sort, cell order, fxy, pidx, dphi, cnt, sys_of_p
   if (precision == SPC_PRECISION_FP32C) b += 8 + 4 + (long long)kMaskWords * 4;  // cs, dphi_f, masks
+  if (precision == SPC_PRECISION_FP32X)
+    b += 16 + 16 + 8 + 16 + 4 + (long long)kMaskWords * 4;  // ics, iws, scos, xsum, xcnt, masks
   if (precision == SPC_PRECISION_FP64) b += 8 + 8 + 4;                          // vortex-arrays outputs
   b += 12 * 8 + 4 + 4;                       // AoS staging, histogram share
   *per_particle = b;
@@ -351,6 +365,14 @@ inline int engine_init(Engine *e, int stepper, int precision, int pool_cap, int 
   if (precision == SPC_PRECISION_FP32C) {
     SPC_TRY(dalloc(e, &a.cs, N));
     SPC_TRY(dalloc(e, &a.dphi_f, N));
+    SPC_TRY(dalloc(e, &a.nbmask, (size_t)kMaskWords * N));
+  }
+  if (precision == SPC_PRECISION_FP32X) {
+    SPC_TRY(dalloc(e, &a.ics, N));
+    SPC_TRY(dalloc(e, &a.iws, N));
+    SPC_TRY(dalloc(e, &a.scos, N));
+    SPC_TRY(dalloc(e, &a.xsum, N));
+    SPC_TRY(dalloc(e, &a.xcnt, N));
     SPC_TRY(dalloc(e, &a.nbmask, (size_t)kMaskWords * N));
   }
   SPC_TRY(dalloc(e, &a.cell_start, (size_t)cell_cap + 1));
@@ -757,6 +779,8 @@ inline int eval_cells(Engine *e, KArgs &a, int rk_form, int kq, double kcdt, boo
   a.svals = vin;
   if (e->precision == SPC_PRECISION_FP32C)
     k_gather<kPrecFP32C><<<blocks_for(n + 1, 256), 256, 0, st>>>(a);
+  else if (e->precision == SPC_PRECISION_FP32X)
+    k_gather<kPrecFP32X><<<blocks_for(n + 1, 256), 256, 0, st>>>(a);
   else
     k_gather<kPrecFP64><<<blocks_for(n + 1, 256), 256, 0, st>>>(a);
   SPC_LAUNCHED(e);
@@ -785,10 +809,12 @@ int launch_pass_t(Engine *e, const KArgs &a, int epi) {
     return SPC_OK;
   }
   if (a.n_ap > 0) {
-    k_allpairs_pass<PREC, KIND><<<std::min(a.n_ap, 152 * 16), kAllPairsThreads, 0, st>>>(a, epi);
+    // FP32X all-pairs systems (rho > L/4: small boxes) run the FP64 pass
+    constexpr int PA = PREC == kPrecFP32X ? kPrecFP64 : PREC;
+    k_allpairs_pass<PA, KIND><<<std::min(a.n_ap, 152 * 16), kAllPairsThreads, 0, st>>>(a, epi);
     SPC_LAUNCHED(e);
   }
-  if constexpr (KIND != kKindNb) {
+  if constexpr (KIND != kKindNb && PREC != kPrecFP32X) {  // FP32X is refused with Verlet rows
     if (e->has_cells && e->verlet) {
       k_vtile<PREC, KIND><<<std::min(e->ncell_total, 152 * 256), kVThreads, 0, st>>>(a, epi);
       SPC_LAUNCHED(e);
@@ -807,6 +833,8 @@ int launch_pass_t(Engine *e, const KArgs &a, int epi) {
         const int grid = std::min(e->ncell_tile * std::max(a.tile_split, 1), 152 * 256);
         if constexpr (PREC == kPrecFP32C)
           k_tile_fp32c<KIND><<<grid, kTileThreads32, 0, st>>>(a, epi);
+        else if constexpr (PREC == kPrecFP32X)
+          k_tile_fp32x<KIND><<<grid, kTileThreads32, 0, st>>>(a, epi);
         else
           k_tile_fp64<KIND><<<grid, kTileThreads64, 0, st>>>(a, epi);
         SPC_LAUNCHED(e);
@@ -815,9 +843,18 @@ int launch_pass_t(Engine *e, const KArgs &a, int epi) {
         const int grid = std::min(blocks_for(e->ncell_warp, kWarpPassWarps), 152 * 64);
         if constexpr (PREC == kPrecFP32C)
           k_warp_fp32c<KIND><<<grid, kWarpPassThreads, 0, st>>>(a, epi);
+        else if constexpr (PREC == kPrecFP32X)
+          k_warp_fp32x<KIND><<<grid, kWarpPassThreads, 0, st>>>(a, epi);
         else
           k_warp_fp64<KIND><<<grid, kWarpPassThreads, 0, st>>>(a, epi);
         SPC_LAUNCHED(e);
+      }
+      if constexpr (PREC == kPrecFP32X && KIND != kKindNb) {
+        // the neighbour kernels wrote the sums; the FP64 epilogues run densely
+        if (e->ncell_tile + e->ncell_warp > 0) {
+          k_epilogue_fp32x<KIND><<<blocks_for(e->n_active, 256), 256, 0, st>>>(a, epi);
+          SPC_LAUNCHED(e);
+        }
       }
     }
   }
@@ -825,12 +862,16 @@ int launch_pass_t(Engine *e, const KArgs &a, int epi) {
 }
 
 inline int launch_pass(Engine *e, const KArgs &a, int kind, int epi) {
-  const bool fp32 = e->precision == SPC_PRECISION_FP32C;
-  if (kind == kKindSin)
-    return fp32 ? launch_pass_t<kPrecFP32C, kKindSin>(e, a, epi) : launch_pass_t<kPrecFP64, kKindSin>(e, a, epi);
-  if (kind == kKindCos2)
-    return fp32 ? launch_pass_t<kPrecFP32C, kKindCos2>(e, a, epi) : launch_pass_t<kPrecFP64, kKindCos2>(e, a, epi);
-  return launch_pass_t<kPrecFP64, kKindNb>(e, a, epi);
+  if (kind == kKindNb) return launch_pass_t<kPrecFP64, kKindNb>(e, a, epi);
+  const bool cos2 = kind == kKindCos2;
+  switch (e->precision) {
+    case SPC_PRECISION_FP32C:
+      return cos2 ? launch_pass_t<kPrecFP32C, kKindCos2>(e, a, epi) : launch_pass_t<kPrecFP32C, kKindSin>(e, a, epi);
+    case SPC_PRECISION_FP32X:
+      return cos2 ? launch_pass_t<kPrecFP32X, kKindCos2>(e, a, epi) : launch_pass_t<kPrecFP32X, kKindSin>(e, a, epi);
+    default:
+      return cos2 ? launch_pass_t<kPrecFP64, kKindCos2>(e, a, epi) : launch_pass_t<kPrecFP64, kKindSin>(e, a, epi);
+  }
 }
 
 // Enqueue one DoStep + wrap of every active system.  noise: pool-indexed
@@ -1076,6 +1117,49 @@ inline int engine_order_global(Engine *e, int slot, double *R, double *psi) {
   im /= (double)h.n;
   if (R) *R = std::hypot(re, im);
   if (psi) *psi = std::atan2(im, re);
+  return SPC_OK;
+}
+
+// Global and local order parameters of every system at once: one local-order
+// pass over the whole layout (pool-indexed results), the pool phases and
+// those results copied to the host, and FP64 sums per system there.  Entries
+// [0, cap) are written; slots without a system get NaN.
+inline int engine_order_all(Engine *e, int cap, double *R, double *psi, double *R_local) {
+  SPC_TRY(engine_layout(e));
+  const double nan = std::numeric_limits<double>::quiet_NaN();
+  for (int s = 0; s < cap; ++s) {
+    if (R) R[s] = nan;
+    if (psi) psi[s] = nan;
+    if (R_local) R_local[s] = nan;
+  }
+  if (e->nsys == 0) return SPC_OK;
+  const size_t P = (size_t)e->pool_cap;
+  std::vector<double> phi(P), r;
+  if (R_local) {
+    KArgs a = e->a;
+    a.out_r = e->aos;
+    SPC_TRY(eval_stage(e, a, 0, -1, 0.0, false));
+    SPC_TRY(launch_pass(e, a, kKindNb, kEpiLocalOrder));
+    r.resize(P);
+    SPC_CUDA(e, cudaMemcpyAsync(r.data(), a.out_r, P * 8, cudaMemcpyDeviceToHost, e->stream));
+  }
+  SPC_CUDA(e, cudaMemcpyAsync(phi.data(), e->a.phi, P * 8, cudaMemcpyDeviceToHost, e->stream));
+  SPC_CUDA(e, cudaStreamSynchronize(e->stream));
+  for (int s : e->order) {
+    if (s >= cap) continue;
+    const SysHost &h = e->slots[s];
+    double re = 0.0, im = 0.0, rl = 0.0;
+    for (int i = 0; i < h.n; ++i) {
+      re += std::cos(phi[h.pool_p0 + i]);
+      im += std::sin(phi[h.pool_p0 + i]);
+      if (R_local) rl += r[h.pool_p0 + i];
+    }
+    re /= (double)h.n;
+    im /= (double)h.n;
+    if (R) R[s] = std::hypot(re, im);
+    if (psi) psi[s] = std::atan2(im, re);
+    if (R_local) R_local[s] = rl / (double)h.n;
+  }
   return SPC_OK;
 }
 

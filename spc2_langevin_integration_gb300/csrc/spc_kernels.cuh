@@ -29,7 +29,7 @@
 
 namespace spc {
 
-enum { kPrecFP64 = 0, kPrecFP32C = 1 };
+enum { kPrecFP64 = 0, kPrecFP32C = 1, kPrecFP32X = 2 };
 // what a pass accumulates over the neighbours of i
 enum { kKindSin = 0, kKindCos2 = 1, kKindNb = 2 };
 // what the pass does with the sums (runtime, warp-uniform)
@@ -85,6 +85,11 @@ struct KArgs {
   double *sx, *sy, *sphi;
   float2 *fxy;                       // prefilter coordinates relative to the cell origin
   float2 *cs;                        // FP32C: (cos phi, sin phi)
+  longlong2 *ics;                    // FP32X: (cos phi, sin phi) in fixed point (2^kXQ)
+  longlong2 *iws;                    // FP32X SRK: phase rate times (cos phi, sin phi), fixed point (2^xq2)
+  double *scos;                      // FP32X SRK: pass-1 sum_j cos(phi_j - phi_i - alpha), cell order
+  double2 *xsum;                     // FP32X: a pass's exact neighbour sums (c, s), cell order
+  int *xcnt;                         // FP32X: a pass's neighbour count, cell order
   int *pidx;                         // pool slot of cell-order slot p
   double *dphi_s;                    // SRK pass 1 phase rate, cell order
   float *dphi_f;                     // same, float (FP32C)
@@ -231,6 +236,11 @@ __global__ void k_gather(KArgs a) {
     sincosf(reduced_phase_f(ph), &s, &c);
     a.cs[p] = make_float2(c, s);
   }
+  if constexpr (PREC == kPrecFP32X) {
+    double s, c;
+    sincos(ph, &s, &c);
+    a.ics[p] = make_longlong2(to_fixed(c, kXQ), to_fixed(s, kXQ));
+  }
 }
 
 // ---------------------------------------------------------------------------
@@ -339,7 +349,7 @@ __device__ __forceinline__ double noise_at(const KArgs &a, int q, int k, double 
 // Fused epilogue for the particle in pool slot q (system sd) at cell-order slot p.
 template <int PREC, int KIND>
 __device__ void epilogue(const KArgs &a, int epi, const SysDesc &sd, const ILane &il,
-                         Acc<PREC> &acc, int q) {
+                         Acc<PREC> &acc, int q, const double2 *cs_known = nullptr) {
   const SysConst &sc = sd.sc;
   const int p = il.p;
   if constexpr (KIND == kKindNb) {
@@ -359,7 +369,9 @@ __device__ void epilogue(const KArgs &a, int epi, const SysDesc &sd, const ILane
   const double dt = a.dt;
   if constexpr (PREC == kPrecFP64) {
     if (draws) philox_normal2(sd.seed, sd.system_id, step, (uint32_t)i, z0, z1);
-    const double cph = cos(il.phi), sph = sin(il.phi);
+    // cos / sin of the stage phase: evaluated here, or (FP32X) the gather's
+    // fixed-point values, exact to 2^-53
+    const double cph = cs_known ? cs_known->x : cos(il.phi), sph = cs_known ? cs_known->y : sin(il.phi);
     const double d0 = dmul(sc.v0, cph), d1 = dmul(sc.v0, sph);  // v_0_ * cos(phi_i) (:419-420)
     if constexpr (KIND == kKindSin) {
       // sigma_ * alignment_force_[i] / neighborhood_cardinality_[i] (:421-424)
@@ -548,6 +560,76 @@ __device__ __forceinline__ void load_i(const KArgs &a, const SysConst &sc, ILane
     il.dphi = 0.0;
     il.dphif = 0.0f;
   }
+}
+
+// FP32X: one particle's exact neighbour sums.  Pass 1 (kKindSin): c, s =
+// sum_j cos phi_j, sum_j sin phi_j; pass 2 (kKindCos2): the same weighted by
+// the neighbours' pass-1 phase rates d_j.  The integer sums over all staging
+// rounds are converted to double once (from_fixed128).
+struct XSums {
+  double c, s;
+  int n;
+};
+
+// FP32X epilogue: the sums become the plain form's accumulators by the
+// angle-addition identities (theta_i = phi_i + alpha):
+//   sum_j sin(phi_j - theta_i) = cos(theta_i) sum sin phi_j - sin(theta_i) sum cos phi_j
+//   sum_j cos(phi_j - theta_i) = cos(theta_i) sum cos phi_j + sin(theta_i) sum sin phi_j
+// and the FP64 epilogue finishes the step with the plain form's formulas and
+// normals.  The SRK second pass's per-term divisions by n_i
+// (ChimeraSystem.cpp:634-637) become one division of each sum.
+template <int KIND>
+__device__ void epilogue_fp32x(const KArgs &a, int epi, const SysDesc &sd, const ILane &il, const XSums &x,
+                               int q) {
+  const SysConst &sc = sd.sc;
+  const int p = il.p;
+  const longlong2 cq = a.ics[p];
+  const double2 cs = make_double2(from_fixed(cq.x, kXQ), from_fixed(cq.y, kXQ));
+  const double ct = dsub(dmul(cs.x, sc.cos_ad), dmul(cs.y, sc.sin_ad));  // cos(phi_i + alpha)
+  const double st = dadd(dmul(cs.y, sc.cos_ad), dmul(cs.x, sc.sin_ad));  // sin(phi_i + alpha)
+  Acc<kPrecFP64> acc;
+  acc.n = x.n;
+  acc.s1 = 0.0;
+  if constexpr (KIND == kKindSin) {
+    acc.s0 = x.n ? dsub(dmul(x.s, ct), dmul(x.c, st)) : 0.0;
+    if (epi == kEpiSrk1) {
+      // what the second pass needs: this particle's sum of cosines and its
+      // rate (the FP64 epilogue's value) times cos phi_i, sin phi_i
+      const double rate = x.n ? ddiv(dmul(sc.sigma, acc.s0), (double)x.n) : 0.0;
+      a.scos[p] = x.n ? dadd(dmul(x.c, ct), dmul(x.s, st)) : 0.0;
+      a.iws[p] = make_longlong2(to_fixed(dmul(rate, cs.x), sc.xq2), to_fixed(dmul(rate, cs.y), sc.xq2));
+    }
+  } else {
+    const double scs = a.scos[p];
+    if (x.n) {
+      const double n = (double)x.n;
+      acc.s0 = ddiv(scs, n);
+      // sum_j (d_j - d_i) cos(phi_j - theta_i) / n_i
+      acc.s1 = ddiv(dsub(dadd(dmul(x.c, ct), dmul(x.s, st)), dmul(il.dphi, scs)), n);
+    } else {
+      acc.s0 = 0.0;
+    }
+  }
+  epilogue<kPrecFP64, KIND>(a, epi, sd, il, acc, q, &cs);
+}
+
+// FP32X epilogues as their own dense launch: one thread per cell-order slot,
+// so the FP64 per-particle work (rates, noise, the stepper update) runs on
+// full warps, while the neighbour kernels, whose warps cover cells of a few
+// particles, only write each particle's sums (xsum, xcnt).  All-pairs systems
+// finish in their own (FP64) kernel.
+template <int KIND>
+__global__ void __launch_bounds__(256) k_epilogue_fp32x(KArgs a, int epi) {
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= a.n_active) return;
+  const SysDesc &sd = a.sys[a.sys_of_c[a.skeys[p]]];
+  const SysConst &sc = sd.sc;
+  if (sc.allpairs) return;
+  ILane il;
+  load_i<kPrecFP32X, KIND>(a, sc, il, p, true);
+  const double2 v = a.xsum[p];
+  const XSums x{v.x, v.y, a.xcnt[p]};
+  epilogue_fp32x<KIND>(a, epi, sd, il, x, a.pidx[p]);
 }
 
 constexpr int kPassWarps = 4;

@@ -369,6 +369,204 @@ __global__ void __launch_bounds__(kTileThreads32, kTileMinBlocks32) k_tile_fp32c
 }
 
 // ---------------------------------------------------------------------------
+// FP32X passes.  The same CTA-per-cell staging, work split and pass-1 masks
+// as FP32C, but each accepted candidate adds its fixed-point (cos phi_j,
+// sin phi_j) (pass 2: d_j times those) to two 64-bit integer sums: exact,
+// so the split of the list among warps, the order of the blocks and the
+// staging rounds (added in 128 bits) do not change the result.  The kernel
+// writes each particle's sums; k_epilogue_fp32x applies the angle addition
+// and the stepper update in FP64.
+constexpr int kTileCapX = 768;  // candidates staged per round (24 mask words)
+static_assert(kTileCapX % 128 == 0 && kTileCapX / 32 <= kMaskWords, "FP32X staging round");
+
+struct TileRedX {
+  long long c[4][kTileThreads32], s[4][kTileThreads32];
+  int n[4][kTileThreads32];
+};
+
+// One block of 32 staged candidates against one particle (FP32X): the float
+// test, the fixed-point sums of the inside candidates, their bits, and the
+// smallest |d^2 - mid| for the undecided check (as block32).
+template <bool SELF>
+__device__ __forceinline__ void block32x(const float2 *__restrict__ s_xy, const longlong2 *__restrict__ s_v,
+                                         int j0, int self, float fxi, float fyi, float nmid, float nband,
+                                         long long &C, long long &S, uint32_t &bits, float &mn) {
+#pragma unroll
+  for (int t = 0; t < kWarp; ++t) {
+    const float2 cj = s_xy[j0 + t];
+    const float dx = cj.x - fxi, dy = cj.y - fyi;
+    float off = cutoff_offset(dx, dy, nmid);
+    bool in = off < nband;
+    if (SELF) {
+      in = in && (j0 + t != self);
+      off = (j0 + t != self) ? off : 3.0e38f;
+    }
+    mn = fminf(mn, fabsf(off));
+    if (in) {
+      const longlong2 v = s_v[j0 + t];
+      C += v.x;
+      S += v.y;
+      bits |= 1u << t;
+    }
+  }
+}
+
+template <int KIND>
+__global__ void __launch_bounds__(kTileThreads32, kTileMinBlocks32) k_tile_fp32x(KArgs a, int epi) {
+  __shared__ float2 s_xy[kTileCapX];     // x+shift, y+shift (padded to 32)
+  __shared__ longlong2 s_v[kTileCapX];   // pass 1: ics, pass 2: iws of the candidate
+  __shared__ TileRedX red;
+  const int n_all = a.n_active;
+  const int tid = threadIdx.x, w = tid / kWarp, lane = tid % kWarp;
+  const int nitems = tile_items(a);
+  for (int item = blockIdx.x; item < nitems; item += gridDim.x) {
+    TileItem ti;
+    if (!tile_item(a, item, ti)) continue;
+    const int c = ti.c, c0 = ti.c0, cb = ti.cb, ce = ti.ce;
+    const SysDesc &sd = a.sys[a.sys_of_c[c]];
+    const SysConst &sc = sd.sc;
+    if (sc.allpairs) continue;
+    const float lo2 = sc.lo2, hi2 = sc.hi2;
+    const float band = 0.5f * (hi2 - lo2), nmid = -0.5f * (hi2 + lo2);
+    const bool exact_all = sc.exact_all != 0;
+    Stencil st;
+    stencil_of(a, sd, c, st);
+    const int total = st.prefix[9];
+    const int rounds = (total + kTileCapX - 1) / kTileCapX;
+    const bool masked = rounds == 1 && a.nbmask != nullptr && !exact_all;
+    for (int ig = cb; ig < ce; ig += kTileThreads32) {
+      const int gi = min(kTileThreads32, ce - ig);
+      // thread tid's particle (ig + tid): its sums over all rounds
+      __int128 t_c = 0, t_s = 0;
+      int t_n = 0;
+      for (int r = 0; r < rounds; ++r) {
+        const int rlo = r * kTileCapX, rcnt = min(kTileCapX, total - rlo);
+        const int rpad = (rcnt + kWarp - 1) & ~(kWarp - 1);
+        if (rounds > 1 || ig == cb) {
+          __syncthreads();
+          for (int k = tid; k < rpad; k += blockDim.x) {
+            if (k < rcnt) {
+              int q;
+              const int pj = slot_of(st, rlo + k, q);
+              const float2 f = a.fxy[pj];
+              s_xy[k] = make_float2(f.x + shift_x(q, sc.cell_f), f.y + shift_y(q, sc.cell_f));
+              s_v[k] = KIND == kKindSin ? a.ics[pj] : a.iws[pj];
+            } else {  // padding: far away, never a neighbour, never near the cutoff
+              s_xy[k] = make_float2(3.0e18f, 3.0e18f);
+              s_v[k] = make_longlong2(0, 0);
+            }
+          }
+          __syncthreads();
+        }
+        const int chunks = (gi + kWarp - 1) / kWarp;
+        const int S = chunks >= 4 ? 1 : (chunks == 1 ? 4 : 2);
+        const int items = chunks * S;
+        for (int item = w; item < items; item += kTileThreads32 / kWarp) {
+          const int chunk = item / S, part = item % S;
+          const int li = chunk * kWarp + lane;
+          const bool valid = li < gi;
+          const int p = ig + li;
+          float fxi = 3.0e30f, fyi = 3.0e30f;
+          double xi = 0.0, yi = 0.0;
+          if (valid) {
+            const float2 f = a.fxy[p];
+            fxi = f.x;
+            fyi = f.y;
+            xi = a.sx[p];
+            yi = a.sy[p];
+          }
+          const int self = st.prefix[4] + (p - c0) - rlo;
+          const int jlo = split_point(rpad, part, S), jhi = split_point(rpad, part + 1, S);
+          long long C = 0, Sn = 0;
+          int n = 0;
+          if (KIND == kKindCos2 && masked) {
+            // pass 2 over the neighbour bitmask of pass 1 (same staged list)
+            const uint4 *m4 = reinterpret_cast<const uint4 *>(a.nbmask);
+            const uint4 none = make_uint4(0u, 0u, 0u, 0u);
+            const int w0 = jlo / kWarp, w1 = jhi / kWarp;
+            int g = w0 >> 2;
+            uint4 cur = (valid && w0 < w1) ? m4[(size_t)g * n_all + p] : none;
+            uint4 nxt = (valid && ((g + 1) << 2) < w1) ? m4[(size_t)(g + 1) * n_all + p] : none;
+            for (int j0 = jlo; j0 < jhi; j0 += kWarp) {
+              const int wd = j0 / kWarp;
+              if ((wd >> 2) != g) {
+                ++g;
+                cur = nxt;
+                nxt = (valid && ((g + 1) << 2) < w1) ? m4[(size_t)(g + 1) * n_all + p] : none;
+              }
+              const int sub = wd & 3;
+              const uint32_t bits = sub == 0 ? cur.x : sub == 1 ? cur.y : sub == 2 ? cur.z : cur.w;
+#pragma unroll
+              for (int t = 0; t < kWarp; ++t) {
+                if ((bits >> t) & 1u) {
+                  const longlong2 v = s_v[j0 + t];
+                  C += v.x;
+                  Sn += v.y;
+                }
+              }
+              n += __popc(bits);
+            }
+          } else {
+            for (int j0 = jlo; j0 < jhi; j0 += kWarp) {
+              float mn = 3.0e38f;
+              uint32_t bits = 0u;
+              const bool self_block = (unsigned)(self - j0) < (unsigned)kWarp;
+              if (!exact_all) {
+                if (__any_sync(0xffffffffu, self_block))
+                  block32x<true>(s_xy, s_v, j0, self, fxi, fyi, nmid, -band, C, Sn, bits, mn);
+                else
+                  block32x<false>(s_xy, s_v, j0, self, fxi, fyi, nmid, -band, C, Sn, bits, mn);
+              }
+              // pairs the float test cannot decide: the reference's FP64 test
+              const bool amb = valid && (exact_all || mn <= band);
+              if (__any_sync(0xffffffffu, amb)) {
+                if (amb) {
+                  for (int t = 0; t < kWarp; ++t) {
+                    const int j = j0 + t;
+                    if (j == self || j >= rcnt) continue;
+                    const float2 cj = s_xy[j];
+                    const float dx = cj.x - fxi, dy = cj.y - fyi;
+                    if (!(exact_all || fabsf(cutoff_offset(dx, dy, nmid)) <= band)) continue;
+                    int q;
+                    const int pj = slot_of(st, rlo + j, q);
+                    if (!exact_within(sc, xi, yi, a.sx[pj], a.sy[pj])) continue;
+                    const longlong2 v = s_v[j];
+                    C += v.x;
+                    Sn += v.y;
+                    bits |= 1u << t;
+                  }
+                }
+              }
+              n += __popc(bits);
+              if (KIND == kKindSin && masked && valid) a.nbmask[mask_at(j0 / kWarp, p, n_all)] = bits;
+            }
+          }
+          if (valid) {
+            red.c[part][li] = C;
+            red.s[part][li] = Sn;
+            red.n[part][li] = n;
+          }
+        }
+        __syncthreads();
+        if (tid < gi) {
+          for (int part = 0; part < S; ++part) {
+            t_c += red.c[part][tid];
+            t_s += red.s[part][tid];
+            t_n += red.n[part][tid];
+          }
+        }
+      }
+      if (tid < gi) {
+        const int qv = KIND == kKindSin ? kXQ : sc.xq2;
+        a.xsum[ig + tid] = make_double2(from_fixed128(t_c, qv), from_fixed128(t_s, qv));
+        a.xcnt[ig + tid] = t_n;
+      }
+      __syncthreads();
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
 template <int KIND>
 __global__ void __launch_bounds__(kTileThreads64) k_tile_fp64(KArgs a, int epi) {
   __shared__ float2 s_xy[kTileCap64];   // x+shift, y+shift (prefilter)

@@ -231,6 +231,138 @@ __global__ void __launch_bounds__(kWarpPassThreads, 8) k_warp_fp32c(KArgs a, int
 }
 
 // ---------------------------------------------------------------------------
+// FP32X: the lanes as in k_warp_fp32c; each lane adds its accepted
+// candidates' fixed-point values (pass 1: cos phi_j, sin phi_j; pass 2: d_j
+// times those) to two 64-bit integer sums, and the groups of a particle and
+// the staging rounds are combined by integer adds (128 bits across rounds),
+// so the sums are exact and independent of the grouping: bitwise those of
+// the cell-tile kernel.  The kernel writes each particle's sums for
+// k_epilogue_fp32x.
+struct WarpStageX {
+  float2 xy[kWarpCap];     // x+shift, y+shift
+  longlong2 v[kWarpCap];   // pass 1: ics, pass 2: iws
+  long long c[kWarp], s[kWarp];
+  int n[kWarp];
+};
+
+template <int KIND>
+__global__ void __launch_bounds__(kWarpPassThreads, 8) k_warp_fp32x(KArgs a, int epi) {
+  constexpr unsigned FULL = 0xffffffffu;
+  __shared__ WarpStageX stage_all[kWarpPassWarps];
+  const int w = threadIdx.x / kWarp, lane = threadIdx.x % kWarp;
+  WarpStageX &sm = stage_all[w];
+  const int n_all = a.n_active;
+  const int stride = gridDim.x * kWarpPassWarps;
+  for (int c = a.ncell_tile + blockIdx.x * kWarpPassWarps + w; c < a.va_c0; c += stride) {
+    const int cb = a.cell_start[c], ce = a.cell_start[c + 1];
+    if (cb == ce) continue;
+    const SysDesc &sd = a.sys[a.sys_of_c[c]];
+    const SysConst &sc = sd.sc;
+    if (sc.allpairs) continue;
+    const float lo2 = sc.lo2, hi2 = sc.hi2;
+    const float band = 0.5f * (hi2 - lo2), nmid = -0.5f * (hi2 + lo2);
+    const bool exact_all = sc.exact_all != 0;
+    const int qv = KIND == kKindSin ? kXQ : sc.xq2;
+    Stencil st;
+    stencil_of(a, sd, c, st);
+    const int total = st.prefix[9];
+    const int rounds = (total + kWarpCap - 1) / kWarpCap;
+    const bool masked = rounds == 1 && a.nbmask != nullptr && !exact_all;
+    for (int ib = cb; ib < ce; ib += kWarp) {
+      const int gn = min(kWarp, ce - ib);
+      const bool valid = lane < gn;
+      // lane l: particle pl against candidate group g
+      const int G = kWarp / gn, pl = lane % gn, g = lane / gn;
+      const bool active = g < G;
+      const int pp = ib + pl;
+      const float2 fi = a.fxy[pp];
+      const float fxi = fi.x, fyi = fi.y;
+      __int128 my_c = 0, my_s = 0;  // lane k: particle k of the chunk, over all rounds
+      int my_n = 0;
+      for (int r = 0; r < rounds; ++r) {
+        const int rlo = r * kWarpCap, rcnt = min(kWarpCap, total - rlo);
+        const int self = st.prefix[4] + (pp - cb) - rlo;
+        __syncwarp();
+        if (rounds > 1 || ib == cb) {
+          for (int k = lane; k < rcnt; k += kWarp) {
+            int q;
+            const int pj = slot_of(st, rlo + k, q);
+            const float2 f = a.fxy[pj];
+            sm.xy[k] = make_float2(f.x + shift_x(q, sc.cell_f), f.y + shift_y(q, sc.cell_f));
+            sm.v[k] = KIND == kKindSin ? a.ics[pj] : a.iws[pj];
+          }
+        }
+        __syncwarp();
+        const int W = ((rcnt + G - 1) / G + kWarp - 1) / kWarp;
+        long long pc = 0, ps = 0;
+        int pn = 0;
+        if (active) {
+          if (KIND == kKindCos2 && masked) {
+            for (int wd = 0; wd < W; ++wd) {
+              uint32_t bits = a.nbmask[mask_at(g * W + wd, pp, n_all)];
+              pn += __popc(bits);
+              while (bits) {
+                const int t = __ffs(bits) - 1;
+                bits &= bits - 1u;
+                const longlong2 v = sm.v[g + (wd * kWarp + t) * G];
+                pc += v.x;
+                ps += v.y;
+              }
+            }
+          } else {
+            uint32_t bits = 0u;
+            int k = 0;
+            for (int j = g; j < rcnt; j += G, ++k) {
+              const float2 cj = sm.xy[j];
+              const float dx = cj.x - fxi, dy = cj.y - fyi;
+              const float off = cutoff_offset(dx, dy, nmid);
+              bool in = !exact_all && off < -band;
+              if (exact_all || fabsf(off) <= band) {  // rare: the reference's FP64 test
+                int q;
+                const int pj = slot_of(st, rlo + j, q);
+                in = exact_within(sc, a.sx[pp], a.sy[pp], a.sx[pj], a.sy[pj]);
+              }
+              in = in && j != self;
+              if (in) {
+                bits |= 1u << (k & (kWarp - 1));
+                const longlong2 v = sm.v[j];
+                pc += v.x;
+                ps += v.y;
+              }
+              if ((k & (kWarp - 1)) == kWarp - 1 || j + G >= rcnt) {
+                pn += __popc(bits);
+                if (KIND == kKindSin && masked) a.nbmask[mask_at(g * W + k / kWarp, pp, n_all)] = bits;
+                bits = 0u;
+              }
+            }
+            // a group with fewer candidates than group 0 leaves its last words empty
+            if (KIND == kKindSin && masked)
+              for (int wd = (k + kWarp - 1) / kWarp; wd < W; ++wd) a.nbmask[mask_at(g * W + wd, pp, n_all)] = 0u;
+          }
+        }
+        // combine the groups of each particle on its owner lane (integer adds)
+        sm.c[lane] = pc;
+        sm.s[lane] = ps;
+        sm.n[lane] = pn;
+        __syncwarp();
+        if (valid) {
+          for (int gg = 0; gg < G; ++gg) {
+            const int src = gg * gn + lane;
+            my_c += sm.c[src];
+            my_s += sm.s[src];
+            my_n += sm.n[src];
+          }
+        }
+      }
+      if (valid) {
+        a.xsum[ib + lane] = make_double2(from_fixed128(my_c, qv), from_fixed128(my_s, qv));
+        a.xcnt[ib + lane] = my_n;
+      }
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
 template <int KIND>
 struct WarpStage64 {
   float2 xy[kWarpCap];  // x+shift, y+shift (prefilter)

@@ -4,7 +4,10 @@
 // caller gets the reference's trajectory from the GPU path.
 //
 // usage: SPC_REF_N=<N> SPC_REF_L=<L> spc_dropin_driver <input.bin> <output.bin>
-// (mode 0 = run the engine loop, modes 1/2 = one EvaluateRhs of either form;
+// (mode 0 = run the engine loop, modes 1/2 = one EvaluateRhs of either form,
+//  mode 3 = the engine loop of SimulationEngine.cpp:113-127 for the vector
+//  classes: the observer's frame at t0, then a frame and a summary line after
+//  every step, and every state written to the output;
 //  family 0 = vector classes, family 1 = shared-window classes, whose SRK
 //  stepper takes the first N injected values as its natural frequencies,
 //  family 2 = VortexArraysSystemPtr with the shared-window steppers, whose
@@ -74,7 +77,7 @@ int main(int argc, char **argv) {
     ThreadSharedMemory thread(argc, argv);  // a Thread for the vector classes
     PeriodicBoundaryConditions pbc_config(&thread, kL, kL);
     BinaryObserver *observer = nullptr;
-    if (std::getenv("SPC_OUTPUT_DIR") && h.mode == 0)
+    if (std::getenv("SPC_OUTPUT_DIR") && (h.mode == 0 || h.mode == 3))
       observer = new BinaryObserver(&thread, h.v0, h.sigma, h.rho, h.alpha, h.D_phi, h.rho_0, pbc_config,
                                     h.dt, 0);
     auto observe = [&](std::vector<Real> &s, Real t) {
@@ -160,6 +163,7 @@ int main(int argc, char **argv) {
         StochasticRungeKuttaStepper srk(&thread);
         RungeKutta4Stepper rk4(&thread);
         Real t = h.t0;
+        if (h.mode == 3 && observer) observer->SaveSystemState(state, t);
         if (device_loop)
           run_device(chimera_system,
                      h.stepper == 0 ? SPC_STEPPER_EULER : h.stepper == 1 ? SPC_STEPPER_SRK : SPC_STEPPER_RK4);
@@ -174,7 +178,8 @@ int main(int argc, char **argv) {
           pbc_config.ApplyPeriodicBoundaryConditions(state);
           thread.SynchronizeVector(state);
           observe(state, t);
-          if ((h.record_every > 0 && k % h.record_every == 0) || k == h.nsteps) dump(state.data(), n3);
+          if (h.mode == 3 || (h.record_every > 0 && k % h.record_every == 0) || k == h.nsteps)
+            dump(state.data(), n3);
         }
       }
     } else {

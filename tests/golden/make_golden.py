@@ -128,8 +128,50 @@ def make_va_case(name, n, L, stepper, nsteps, seed, dt=0.01):
     return traj.shape
 
 
+# The reference's BinaryObserver (Observers/BinaryObserver.cpp) in the engine
+# loop of SimulationEngine.cpp:113-127: its .bin frames and summary lines for
+# a short run, written under the file names it builds from the parameters.
+# name: (n, L, params, stepper, nsteps, seed, t0)
+OBSERVER_CASES = {
+    "observer_chimera_euler_n256": (256, 0.5, dict(v0=0.01, sigma=1.0, rho=0.1, alpha=1.45,
+                                                   D_phi=0.005, rho_0=1.0),
+                                    pyref.STEP_EULER, 12, 11, 0.0),
+    "observer_chimera_srk_n200": (200, 0.8, dict(v0=0.02, sigma=0.75, rho=0.15, alpha=0.3,
+                                                 D_phi=0.0125, rho_0=0.5),
+                                  pyref.STEP_SRK, 10, 12, 2.5),
+}
+
+
+def make_observer_case(name, n, L, prm, stepper, nsteps, seed, t0, dt=0.01):
+    import tempfile
+    rng = np.random.default_rng(3000 + seed)
+    state0 = init_state(n, L, seed)
+    m = {pyref.STEP_EULER: 1, pyref.STEP_SRK: 2, pyref.STEP_RK4: 0}[stepper]
+    noise = rng.standard_normal(nsteps * n * m)
+    with tempfile.TemporaryDirectory() as td:
+        traj = pyref.run_reference(n, L, mode=pyref.MODE_OBSERVE, family=pyref.FAMILY_VECTOR,
+                                   stepper=stepper, nsteps=nsteps, t0=t0, dt=dt, state=state0,
+                                   noise=noise, extra_env={"SPC_REF_OUT_DIR": td}, **prm)
+        files = sorted(os.listdir(td))
+        assert len(files) == 2, files
+        bin_name = [f for f in files if f.endswith(".bin")][0]
+        txt_name = [f for f in files if f.endswith(".txt")][0]
+        bin_bytes = np.frombuffer(open(os.path.join(td, bin_name), "rb").read(), np.uint8)
+        txt_bytes = np.frombuffer(open(os.path.join(td, txt_name), "rb").read(), np.uint8)
+    out = dict(n=n, L=L, dt=dt, t0=t0, stepper=stepper, nsteps=nsteps, state0=state0, noise=noise,
+               trajectory=traj.reshape(-1, 3 * n), bin_name=bin_name, txt_name=txt_name,
+               bin_bytes=bin_bytes, txt_bytes=txt_bytes, **prm)
+    os.makedirs(os.path.join(HERE, "observer"), exist_ok=True)
+    np.savez_compressed(os.path.join(HERE, "observer", name + ".npz"), **out)
+    return bin_name, bin_bytes.size, txt_bytes.size
+
+
 def main():
     which = sys.argv[1:]
+    for name, (n, L, prm, stepper, nsteps, seed, t0) in OBSERVER_CASES.items():
+        if which and name not in which:
+            continue
+        print(name, make_observer_case(name, n, L, prm, stepper, nsteps, seed, t0))
     for name, (n, L, prm, family, stepper, nsteps, seed) in CASES.items():
         if which and name not in which:
             continue

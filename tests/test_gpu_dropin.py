@@ -6,6 +6,7 @@ VortexArraysSystemPtr, fed the golden inputs, must reproduce the reference's
 golden trajectories and right-hand sides; with SPC_OUTPUT_DIR set, its
 observer files must be the bytes the reference's observer writes for those
 states."""
+import glob
 import os
 
 import numpy as np
@@ -82,6 +83,33 @@ def test_dropin_engine_loop_matches_reference_golden(name, tmp_path):
             assert tf == float(np.float32(t))
             assert np.array_equal(fr, st.astype(np.float32))
             assert lines[k - 1] + "\n" == obs.summary_line(t, st)
+
+
+OBSERVER_CASES = sorted(glob.glob(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden",
+                                               "observer", "*.npz")))
+
+
+@pytest.mark.parametrize("path", OBSERVER_CASES, ids=[os.path.basename(c)[:-4] for c in OBSERVER_CASES])
+def test_dropin_observer_files_are_the_reference_observers(path, tmp_path):
+    # the engine loop of SimulationEngine.cpp:113-127 on the GPU path, with the
+    # reference's injected normals: its observer files must be the bytes the
+    # reference's BinaryObserver wrote for the reference's own run (frames at
+    # float32, summary lines through operator<<), under the same names
+    z = np.load(path)
+    g = {k: z[k] for k in z.files}
+    n, L = int(g["n"]), float(g["L"])
+    out = pyref.run_reference(n, L, mode=3, family=pyref.FAMILY_VECTOR, stepper=int(g["stepper"]),
+                              nsteps=int(g["nsteps"]), t0=float(g["t0"]), dt=float(g["dt"]),
+                              state=g["state0"], noise=g["noise"],
+                              binary=build_host.build_driver(),
+                              extra_env={"SPC_OUTPUT_DIR": str(tmp_path)},
+                              **{k: float(g[k]) for k in ("v0", "sigma", "rho", "alpha", "D_phi", "rho_0")})
+    frames = out.reshape(-1, 3 * n)
+    for got, want in zip(frames, g["trajectory"]):
+        assert np.abs(periodic_diff(got, want, L)).max() <= TRAJ_TOL
+    assert sorted(os.listdir(tmp_path)) == sorted([str(g["bin_name"]), str(g["txt_name"])])
+    assert open(tmp_path / str(g["bin_name"]), "rb").read() == g["bin_bytes"].tobytes()
+    assert open(tmp_path / str(g["txt_name"]), "rb").read() == g["txt_bytes"].tobytes()
 
 
 @pytest.mark.parametrize("name", va_golden_cases())
