@@ -282,6 +282,17 @@ __device__ __forceinline__ float cutoff_offset(float dx, float dy, float nmid) {
   return fmaf(dx, dx, fmaf(dy, dy, nmid));
 }
 
+// Every neighbour kernel decides a candidate from that one offset: inside when
+// off < -band, undecided (the reference's FP64 test decides) when
+// |off| <= band, outside otherwise.  The inside and undecided sets are then
+// disjoint and leave no gap below mid + band.  Deciding instead from d^2 < lo2
+// and |d^2 - mid| <= band separately leaves one: mid = (lo2 + hi2) / 2 is
+// rounded, and for about one rho in five |lo2 - mid| exceeds band by a
+// fraction of an ulp, so a float d^2 equal to lo2 is in neither set and a pair
+// just inside the cutoff (d^2 ~ rho^2 (1 - 3e-5)) is dropped.
+__device__ __forceinline__ bool float_inside(float off, float band) { return off < -band; }
+__device__ __forceinline__ bool float_undecided(float off, float band) { return fabsf(off) <= band; }
+
 __device__ __forceinline__ void kahan_add(float &sum, float &comp, float v) {
   const float y = v - comp;
   const float t = sum + y;

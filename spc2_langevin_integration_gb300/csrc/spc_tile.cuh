@@ -585,7 +585,7 @@ __global__ void __launch_bounds__(kTileThreads64) k_tile_fp64(KArgs a, int epi) 
     const SysConst &sc = sd.sc;
     if (sc.allpairs) continue;
     const float lo2 = sc.lo2, hi2 = sc.hi2;
-    const float band = 0.5f * (hi2 - lo2), mid = 0.5f * (hi2 + lo2);
+    const float band = 0.5f * (hi2 - lo2), nmid = -0.5f * (hi2 + lo2);
     const bool exact_all = sc.exact_all != 0;
     Stencil st;
     stencil_of(a, sd, c, st);
@@ -647,10 +647,9 @@ __global__ void __launch_bounds__(kTileThreads64) k_tile_fp64(KArgs a, int epi) 
           const int je = min(j0 + kWarp, rcnt);
           for (int j = j0; j < je; ++j) {
             const float2 cj = s_xy[j];
-            const float dx = cj.x - il.fx, dy = cj.y - il.fy;
-            const float d2 = fmaf(dx, dx, dy * dy);
-            bool in = !exact_all && (d2 < lo2) && (j != self);
-            const bool amb = (exact_all || fabsf(d2 - mid) <= band) && (j != self) && valid;
+            const float off = cutoff_offset(cj.x - il.fx, cj.y - il.fy, nmid);
+            bool in = !exact_all && float_inside(off, band) && (j != self);
+            const bool amb = (exact_all || float_undecided(off, band)) && (j != self) && valid;
             if (__any_sync(0xffffffffu, amb)) {
               if (amb) in = exact_within(sc, il.x, il.y, a.sx[s_p[j]], a.sy[s_p[j]]);
             }

@@ -261,7 +261,7 @@ __global__ void __launch_bounds__(kVThreads) k_vtile(KArgs a, int epi) {
     const SysConst &sc = sd.sc;
     if (sc.allpairs) continue;
     const float lo2 = sc.lo2, hi2 = sc.hi2;
-    const float band = 0.5f * (hi2 - lo2), mid = 0.5f * (hi2 + lo2);
+    const float band = 0.5f * (hi2 - lo2), nmid = -0.5f * (hi2 + lo2);
     const bool exact_all = sc.exact_all != 0;
     vstencil_of(a, sd, c, s_start, s_prefix);
     const int D = 2 * sc.vR + 1;
@@ -308,10 +308,9 @@ __global__ void __launch_bounds__(kVThreads) k_vtile(KArgs a, int epi) {
             cx = cj.x;
             cy = cj.y;
           }
-          const float dx = cx - il.fx, dy = cy - il.fy;
-          const float d2 = fmaf(dx, dx, dy * dy);
-          in = !exact_all && d2 < lo2;
-          if (exact_all || fabsf(d2 - mid) <= band) {  // rare: the reference's FP64 test
+          const float off = cutoff_offset(cx - il.fx, cy - il.fy, nmid);
+          in = !exact_all && float_inside(off, band);
+          if (exact_all || float_undecided(off, band)) {  // rare: the reference's FP64 test
             const int pj = vslot_of(sc, s_start, s_prefix, g);
             in = exact_within(sc, il.x, il.y, a.sx[pj], a.sy[pj]);
           }
@@ -398,10 +397,9 @@ __global__ void __launch_bounds__(kVThreads) k_vtile(KArgs a, int epi) {
                     cx = cj.x;
                     cy = cj.y;
                   }
-                  const float dx = cx - il.fx, dy = cy - il.fy;
-                  const float d2 = fmaf(dx, dx, dy * dy);
-                  in = d2 < lo2;
-                  if (fabsf(d2 - mid) <= band) {  // rare: the reference's FP64 test
+                  const float off = cutoff_offset(cx - il.fx, cy - il.fy, nmid);
+                  in = float_inside(off, band);
+                  if (float_undecided(off, band)) {  // rare: the reference's FP64 test
                     const int pj = vslot_of(sc, s_start, s_prefix, j);
                     in = exact_within(sc, il.x, il.y, a.sx[pj], a.sy[pj]);
                   }

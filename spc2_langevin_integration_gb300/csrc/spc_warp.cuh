@@ -247,7 +247,6 @@ struct WarpStageX {
 
 template <int KIND>
 __global__ void __launch_bounds__(kWarpPassThreads, 8) k_warp_fp32x(KArgs a, int epi) {
-  constexpr unsigned FULL = 0xffffffffu;
   __shared__ WarpStageX stage_all[kWarpPassWarps];
   const int w = threadIdx.x / kWarp, lane = threadIdx.x % kWarp;
   WarpStageX &sm = stage_all[w];
@@ -386,7 +385,7 @@ __global__ void __launch_bounds__(kWarpPassThreads) k_warp_fp64(KArgs a, int epi
     const SysConst &sc = sd.sc;
     if (sc.allpairs) continue;
     const float lo2 = sc.lo2, hi2 = sc.hi2;
-    const float band = 0.5f * (hi2 - lo2), mid = 0.5f * (hi2 + lo2);
+    const float band = 0.5f * (hi2 - lo2), nmid = -0.5f * (hi2 + lo2);
     const bool exact_all = sc.exact_all != 0;
     Stencil st;
     stencil_of(a, sd, c, st);
@@ -446,10 +445,9 @@ __global__ void __launch_bounds__(kWarpPassThreads) k_warp_fp64(KArgs a, int epi
             bool in = false, amb = false;
             if (j < rcnt && j != self) {
               const float2 cj = sm.xy[j];
-              const float dx = cj.x - fxi, dy = cj.y - fyi;
-              const float d2 = fmaf(dx, dx, dy * dy);
-              in = !exact_all && d2 < lo2;
-              amb = exact_all || fabsf(d2 - mid) <= band;
+              const float off = cutoff_offset(cj.x - fxi, cj.y - fyi, nmid);
+              in = !exact_all && float_inside(off, band);
+              amb = exact_all || float_undecided(off, band);
             }
             if (amb) {  // rare: the reference's FP64 test
               int q;

@@ -414,3 +414,48 @@ def test_sincos_cosine_is_bitwise_the_cosine():
     x = np.concatenate([rng.uniform(-7, 7, m), rng.uniform(-1e3, 1e3, m), rng.normal(0, 50, m),
                         np.ldexp(rng.random(m), rng.integers(-30, 30, m)) * rng.choice([-1.0, 1.0], m)])
     assert abi.check_sincos(x) == 0
+
+
+def test_pair_at_the_lower_band_edge_is_counted():
+    """A pair whose float prefilter offset lands exactly on the lower edge of
+    the undecided band must still be decided (it is inside the cutoff).  For
+    rho = 0.15 the rounded band centre makes |lo2 - mid| exceed the band
+    half-width, so a test taken from d^2 < lo2 and |d^2 - mid| <= band
+    separately leaves a float d^2 equal to lo2 in neither set and drops the
+    pair.  Particles 0 and 1 sit in the cell at the origin, so their float
+    offsets are their coordinates and the float d^2 is exactly lo2; the
+    reference's FP64 test has them within rho.  Every kernel and precision
+    must give the oracle's rates."""
+    f = np.float32
+    L, rho = 1.0, 0.15
+    st = np.array([0.0078125, 0.0625, 0.3,
+                   0.15781013667583466, 0.06268310546875, -1.1,
+                   0.62, 0.58, 2.0,
+                   0.81, 0.33, -0.4])
+    n = st.size // 3
+    # the geometry: float d^2 == lo2, inside the cutoff in FP64
+    lo2, hi2 = f(rho * rho * (1 - 3e-5)), f(rho * rho * (1 + 3e-5))
+    band, mid = f(f(0.5) * f(hi2 - lo2)), f(f(0.5) * f(hi2 + lo2))
+    dx, dy = f(f(st[3]) - f(st[0])), f(f(st[4]) - f(st[1]))
+    d2 = f(np.float64(dx) * np.float64(dx) + np.float64(f(dy * dy)))
+    assert d2 == lo2 and not (d2 < lo2) and not (abs(f(d2 - mid)) <= band)
+    assert (st[3] - st[0]) ** 2 + (st[4] - st[1]) ** 2 <= rho * rho
+    prm = dict(v0=0.01, sigma=1.0, rho=rho, alpha=1.45, D_phi=0.005)
+    o = po.OracleSystem(n, L, **prm)
+    d_ref, _, counts = o.rhs_srk(st, with_counts=True)
+    assert counts[0] == 1 and counts[1] == 1 and d_ref[2] != 0.0
+    variants = [(abi.PRECISION_FP64, abi.NEIGHBOUR_CELL, k) for k in KERNELS] + \
+        [(abi.PRECISION_FP64, abi.NEIGHBOUR_VERLET, None)] + \
+        [(abi.PRECISION_FP32X, abi.NEIGHBOUR_CELL, k) for k in KERNELS] + \
+        [(abi.PRECISION_FP32C, abi.NEIGHBOUR_CELL, k) for k in KERNELS] + \
+        [(abi.PRECISION_FP32C, abi.NEIGHBOUR_VERLET, None)]
+    for prec, nb, kernel in variants:
+        p = abi.make_params(L=L, stepper=abi.STEPPER_SRK, precision=prec, neighbour=nb, skin=0.05,
+                            **prm)
+        with abi.System(n, p) as s:
+            if kernel is not None:
+                s.set_tuning(abi.TUNE_SPARSE_BELOW, KERNELS[kernel])
+            s.upload_state(st)
+            d, _ = s.rhs_srk()
+        tol = 2e-6 if prec == abi.PRECISION_FP32C else RHS_TOL
+        assert np.all(np.abs(d[2::3] - d_ref[2::3]) <= tol), (prec, nb, kernel, d[2::3], d_ref[2::3])
