@@ -244,6 +244,43 @@ int spc_get_tuning(const spc_handle *h, int32_t key, double *value);
  * SPC_TUNE_SPARSE_BELOW value to set on the handle, and (when not NULL)
  * ms_out[k] the milliseconds per step of candidate k for k < min(cap, count),
  * *count the number of candidates.  The caller's state is not touched. */
+/* One tuning candidate and its measured cost (no counterpart in the
+ * reference): the neighbour method and skin, the SPC_TUNE_SPARSE_BELOW and
+ * SPC_TUNE_TILE_SPLIT values, and milliseconds per step. */
+typedef struct spc_tuning {
+  int32_t neighbour;    /* SPC_NEIGHBOUR_* */
+  int32_t tile_split;   /* CTAs per cell of the cell-tile passes */
+  double skin;          /* Verlet skin (0 for the cell list) */
+  double sparse_below;  /* SPC_TUNE_SPARSE_BELOW value */
+  double ms_per_step;   /* measured */
+} spc_tuning;
+
+/* Autotuner over every tuning dimension (no counterpart in the reference):
+ * the cell-list passes with each kernel choice (all cell-tile, the default
+ * split between cell-tile and warp-per-cell, all warp-per-cell) and, for the
+ * cell-tile kernels, 1, 2 or 4 CTAs per cell; and Verlet rows with skins of
+ * 0.1, 0.2 and 0.4 rho where the stencil and the precision allow.  Each
+ * candidate runs trial_steps steps as a captured graph on its own handle
+ * (after a warm-up call) from the caller's state, which is not touched.
+ * cands[k] (k < cap) receives candidate k with its cost, *count the number of
+ * candidates, *best the fastest's index.  Every candidate computes the same
+ * neighbour sets; FP64 and FP32X results are bitwise the same across the
+ * kernel choices, FP64 Verlet rows differ from the cell list by summation
+ * order, FP32C results by float rounding. */
+int spc_autotune_ex(const spc_params *p, int32_t n, const double *aos3n, const double *omega, double dt,
+                    int32_t trial_steps, spc_tuning *cands, int32_t cap, int32_t *count, int32_t *best);
+
+/* In-place retuning of a running handle (no counterpart in the reference):
+ * as the state evolves (a clustering system's cells fill up) the best kernel
+ * choice can change.  Times trial_steps steps of each kernel-choice
+ * candidate of spc_autotune_ex (not the neighbour method) on the current
+ * state, putting the state, RK4 rates and step counters back after every
+ * trial, and keeps the fastest setting.  The state and counters on return
+ * are those on entry.  Uses Philox noise (SPC_ERR_STATE while injected noise
+ * is pending); allocates a temporary copy of the pool state; synchronises. */
+int spc_retune(spc_handle *h, double dt, int32_t trial_steps, spc_tuning *cands, int32_t cap, int32_t *count,
+               int32_t *best);
+
 int spc_autotune(const spc_params *p, int32_t n, const double *aos3n, const double *omega, double dt,
                  int32_t trial_steps, spc_params *best, double *sparse_below, double *ms_out,
                  int32_t cap, int32_t *count);
@@ -338,6 +375,9 @@ int spc_batch_profile_steps(spc_batch *b, double dt, int32_t nsteps, double *out
 /* The tuning knobs of spc_set_tuning, for a whole batch. */
 int spc_batch_set_tuning(spc_batch *b, int32_t key, double value);
 int spc_batch_get_tuning(const spc_batch *b, int32_t key, double *value);
+/* spc_retune for a whole batch: the kernel choice of every system at once. */
+int spc_batch_retune(spc_batch *b, double dt, int32_t trial_steps, spc_tuning *cands, int32_t cap,
+                     int32_t *count, int32_t *best);
 
 /* SRK-form right-hand side (as spc_rhs_srk) computed without allocating
  * any device memory.  No counterpart in the reference: it exists for callers

@@ -55,6 +55,19 @@ class BatchConfig(C.Structure):
     ]
 
 
+class Tuning(C.Structure):
+    """spc_tuning: one tuning candidate and its measured cost."""
+    _fields_ = [
+        ("neighbour", C.c_int32), ("tile_split", C.c_int32), ("skin", C.c_double),
+        ("sparse_below", C.c_double), ("ms_per_step", C.c_double),
+    ]
+
+    def as_dict(self):
+        return {"neighbour": "verlet" if self.neighbour == NEIGHBOUR_VERLET else "cell",
+                "tile_split": self.tile_split, "skin": self.skin,
+                "sparse_below": self.sparse_below, "ms_per_step": self.ms_per_step}
+
+
 _lib = None
 
 
@@ -135,6 +148,13 @@ def lib() -> C.CDLL:
     L.spc_autotune.argtypes = [C.POINTER(Params), C.c_int32, C.c_void_p, C.c_void_p, C.c_double,
                                C.c_int32, C.POINTER(Params), dp, dp, C.c_int32,
                                C.POINTER(C.c_int32)]
+    L.spc_autotune_ex.argtypes = [C.POINTER(Params), C.c_int32, C.c_void_p, C.c_void_p, C.c_double,
+                                  C.c_int32, C.POINTER(Tuning), C.c_int32, C.POINTER(C.c_int32),
+                                  C.POINTER(C.c_int32)]
+    L.spc_retune.argtypes = [H, C.c_double, C.c_int32, C.POINTER(Tuning), C.c_int32,
+                             C.POINTER(C.c_int32), C.POINTER(C.c_int32)]
+    L.spc_batch_retune.argtypes = [H, C.c_double, C.c_int32, C.POINTER(Tuning), C.c_int32,
+                                   C.POINTER(C.c_int32), C.POINTER(C.c_int32)]
     L.spc_graph_nodes.argtypes = [H, C.POINTER(C.c_int64)]
     L.spc_run.argtypes = [H, dp, C.c_double, C.c_int64, C.c_int32, C.c_void_p, OBSERVE_FN,
                           C.c_void_p, C.POINTER(C.c_int64)]
@@ -377,6 +397,15 @@ class System:
         self._check(self._L.spc_graph_nodes(self.h, C.byref(v)), self.h)
         return v.value
 
+    def retune(self, dt: float, trial_steps: int = 10):
+        """spc_retune: re-time the kernel choices on the current state (which is
+        left as it was) and keep the fastest.  Returns (candidates, best index)."""
+        cands = (Tuning * 16)()
+        cnt, best = C.c_int32(), C.c_int32()
+        self._check(self._L.spc_retune(self.h, dt, int(trial_steps), cands, 16, C.byref(cnt),
+                                       C.byref(best)), self.h)
+        return [cands[k].as_dict() for k in range(min(cnt.value, 16))], best.value
+
     def set_tuning(self, key: int, value: float):
         self._check(self._L.spc_set_tuning(self.h, int(key), float(value)), self.h)
 
@@ -524,6 +553,14 @@ class Batch:
     def synchronize(self):
         self._check(self._L.spc_batch_synchronize(self.h))
 
+    def retune(self, dt: float, trial_steps: int = 10):
+        """spc_batch_retune (see System.retune)."""
+        cands = (Tuning * 16)()
+        cnt, best = C.c_int32(), C.c_int32()
+        self._check(self._L.spc_batch_retune(self.h, dt, int(trial_steps), cands, 16, C.byref(cnt),
+                                             C.byref(best)))
+        return [cands[k].as_dict() for k in range(min(cnt.value, 16))], best.value
+
     def set_tuning(self, key: int, value: float):
         self._check(self._L.spc_batch_set_tuning(self.h, int(key), float(value)))
 
@@ -558,3 +595,27 @@ def autotune(n: int, params: Params, state, omega=None, dt: float = 0.01, trial_
     if rc != SPC_OK:
         raise SpcError(rc, (L.spc_last_error(None) or b"").decode())
     return best, sb.value, [ms[k] for k in range(min(cnt.value, 16))]
+
+
+def autotune_ex(n: int, params: Params, state, omega=None, dt: float = 0.01, trial_steps: int = 20):
+    """spc_autotune_ex: every tuning candidate timed on this state (neighbour
+    method, skin, kernel choice, CTAs per cell).  Returns (candidates, best)."""
+    L = lib()
+    st = _f64(state, 3 * n)
+    om = None if omega is None else _f64(omega, n)
+    cands = (Tuning * 32)()
+    cnt, best = C.c_int32(), C.c_int32()
+    rc = L.spc_autotune_ex(C.byref(params), int(n), _ptr(st), None if om is None else _ptr(om), dt,
+                           int(trial_steps), cands, 32, C.byref(cnt), C.byref(best))
+    if rc != SPC_OK:
+        raise SpcError(rc, (L.spc_last_error(None) or b"").decode())
+    return [cands[k].as_dict() for k in range(min(cnt.value, 32))], best.value
+
+
+def params_with(params: Params, tuning: dict) -> Params:
+    """A copy of params with a candidate's neighbour method and skin."""
+    q = Params.from_buffer_copy(params)
+    q.neighbour = NEIGHBOUR_VERLET if tuning["neighbour"] == "verlet" else NEIGHBOUR_CELL
+    if q.neighbour == NEIGHBOUR_VERLET:
+        q.skin = tuning["skin"]
+    return q

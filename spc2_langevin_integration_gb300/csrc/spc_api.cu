@@ -747,6 +747,78 @@ int spc_autotune(const spc_params *p, int32_t n, const double *aos3n, const doub
   return SPC_OK;
 }
 
+int spc_autotune_ex(const spc_params *p, int32_t n, const double *aos3n, const double *omega, double dt,
+                    int32_t trial_steps, spc_tuning *cands_out, int32_t cap, int32_t *count, int32_t *best) {
+  if (!p || !aos3n || trial_steps <= 0) return fail(nullptr, SPC_ERR_INVALID, "bad argument");
+  if (p->model == SPC_MODEL_VORTEX && !omega) return fail(nullptr, SPC_ERR_INVALID, "vortex model needs omega");
+  std::string why;
+  int rc = validate_params(p, n, why);
+  if (rc) return fail(nullptr, rc, "%s", why.c_str());
+  std::vector<spc_tuning> cands;
+  for (const TuneCand &c : kernel_candidates()) cands.push_back({SPC_NEIGHBOUR_CELL, c.split, 0.0, c.sparse, 0.0});
+  for (double f : {0.1, 0.2, 0.4}) {
+    if (p->precision == SPC_PRECISION_FP32X) break;  // the FP32X form runs the cell list
+    spc_params q = *p;
+    q.neighbour = SPC_NEIGHBOUR_VERLET;
+    q.skin = f * p->rho;
+    if (make_sysconst(q, n).vR > 0) cands.push_back({SPC_NEIGHBOUR_VERLET, 1, q.skin, kSparseBelowDefault, 0.0});
+  }
+  int best_k = 0;
+  for (size_t k = 0; k < cands.size(); ++k) {
+    spc_params q = *p;
+    q.neighbour = cands[k].neighbour;
+    if (q.neighbour == SPC_NEIGHBOUR_VERLET) q.skin = cands[k].skin;
+    spc_handle *h = nullptr;
+    rc = spc_create(&q, n, &h);
+    if (rc == SPC_OK) rc = spc_upload_state(h, aos3n);
+    if (rc == SPC_OK && omega) rc = spc_upload_omega(h, omega);
+    if (rc == SPC_OK && q.neighbour == SPC_NEIGHBOUR_CELL) {
+      rc = spc_set_tuning(h, SPC_TUNE_SPARSE_BELOW, cands[k].sparse_below);
+      if (rc == SPC_OK) rc = spc_set_tuning(h, SPC_TUNE_TILE_SPLIT, cands[k].tile_split);
+    }
+    double t = 0.0;
+    float f = 0.0f;
+    if (rc == SPC_OK) rc = spc_step_graph(h, &t, dt, trial_steps);  // capture + warm-up
+    if (rc == SPC_OK) {
+      cudaEvent_t e0 = nullptr, e1 = nullptr;
+      cudaError_t ce = cudaEventCreate(&e0);
+      if (ce == cudaSuccess) ce = cudaEventCreate(&e1);
+      if (ce == cudaSuccess) ce = cudaEventRecord(e0, h->e.stream);
+      if (ce == cudaSuccess) rc = spc_step_graph(h, &t, dt, trial_steps);
+      if (ce == cudaSuccess && rc == SPC_OK) ce = cudaEventRecord(e1, h->e.stream);
+      if (ce == cudaSuccess && rc == SPC_OK) ce = cudaEventSynchronize(e1);
+      if (ce == cudaSuccess && rc == SPC_OK) ce = cudaEventElapsedTime(&f, e0, e1);
+      if (e0) cudaEventDestroy(e0);
+      if (e1) cudaEventDestroy(e1);
+      if (ce != cudaSuccess && rc == SPC_OK)
+        rc = fail(nullptr, SPC_ERR_CUDA, "autotune timing: %s", cudaGetErrorString(ce));
+    }
+    std::string msg = h ? h->e.err : std::string();
+    spc_destroy(h);
+    if (rc != SPC_OK) return fail(nullptr, rc, "autotune candidate %d: %s", (int)k, msg.c_str());
+    cands[k].ms_per_step = (double)f / trial_steps;
+    if (cands[k].ms_per_step < cands[best_k].ms_per_step) best_k = (int)k;
+  }
+  for (size_t k = 0; k < cands.size() && (int)k < cap && cands_out; ++k) cands_out[k] = cands[k];
+  if (count) *count = (int32_t)cands.size();
+  if (best) *best = best_k;
+  return SPC_OK;
+}
+
+int spc_retune(spc_handle *h, double dt, int32_t trial_steps, spc_tuning *cands, int32_t cap, int32_t *count,
+               int32_t *best) {
+  if (!h) return fail(nullptr, SPC_ERR_INVALID, "NULL argument");
+  SPC_TRY(check_ready(h));
+  int c = 0, b = 0;
+  SPC_TRY(engine_retune(&h->e, dt, trial_steps, cands, cap, &c, &b));
+  if (cands)
+    for (int k = 0; k < std::min(c, (int)cap); ++k)
+      cands[k].skin = h->p.neighbour == SPC_NEIGHBOUR_VERLET ? h->p.skin : 0.0;
+  if (count) *count = c;
+  if (best) *best = b;
+  return SPC_OK;
+}
+
 int spc_philox4x32_10(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]) {
   if (!ctr || !key || !out) return fail(nullptr, SPC_ERR_INVALID, "NULL argument");
   uint32_t *d = nullptr;
@@ -988,6 +1060,16 @@ int spc_batch_set_tuning(spc_batch *b, int32_t key, double value) {
 int spc_batch_get_tuning(const spc_batch *b, int32_t key, double *value) {
   if (!b || !value) return fail(nullptr, SPC_ERR_INVALID, "NULL argument");
   return engine_get_tuning(&b->e, key, value);
+}
+
+int spc_batch_retune(spc_batch *b, double dt, int32_t trial_steps, spc_tuning *cands, int32_t cap,
+                     int32_t *count, int32_t *best) {
+  if (!b) return fail(nullptr, SPC_ERR_INVALID, "NULL argument");
+  int c = 0, k = 0;
+  SPC_TRY(engine_retune(&b->e, dt, trial_steps, cands, cap, &c, &k));
+  if (count) *count = c;
+  if (best) *best = k;
+  return SPC_OK;
 }
 
 int spc_batch_profile_steps(spc_batch *b, double dt, int32_t nsteps, double *out_ms, int32_t cap) {

@@ -1023,6 +1023,122 @@ inline int engine_get_tuning(const Engine *e, int key, double *value) {
   return fail(nullptr, SPC_ERR_INVALID, "unknown tuning key %d", key);
 }
 
+// Kernel-choice candidates of the cell-list passes: the threshold below which
+// systems take the warp-per-cell kernels (all cell-tile, the default, all
+// warp-per-cell) and the cell-tile kernels' CTAs per cell.
+struct TuneCand {
+  double sparse;
+  int split;
+};
+
+inline std::vector<TuneCand> kernel_candidates() {
+  std::vector<TuneCand> c;
+  for (double sb : {0.0, kSparseBelowDefault, 1e9})
+    for (int split : {1, 2, 4}) {
+      if (sb == 1e9 && split != 1) continue;  // no cell-tile systems left: the split does nothing
+      c.push_back({sb, split});
+    }
+  return c;
+}
+
+// Times every kernel-choice candidate on the engine's current state and keeps
+// the fastest.  Each candidate runs trial steps once to settle (layout, first
+// launches) and once under CUDA events; after each run the pool state (and
+// RK4's rates) and every system's step counters are put back, so the state the
+// caller continues from is the one it had.  out[k] (k < cap) gets candidate k
+// with its milliseconds per step.  Verlet engines keep their rows (the knobs
+// apply to the cell list): their one candidate is the current setting.
+inline int engine_retune(Engine *e, double dt, int trial, spc_tuning *out, int cap, int *count, int *best) {
+  if (e->injecting) return fail(e, SPC_ERR_STATE, "retuning runs Philox-noise steps; clear injected noise first");
+  if (trial <= 0) return fail(e, SPC_ERR_INVALID, "trial_steps must be positive");
+  SPC_TRY(engine_set_device(e));
+  SPC_TRY(engine_layout(e));
+  std::vector<TuneCand> cands = e->verlet ? std::vector<TuneCand>{{e->sparse_below, e->tile_split_tune}}
+                                          : kernel_candidates();
+  const size_t P = (size_t)e->pool_cap;
+  std::vector<double *> live = {e->a.x, e->a.y, e->a.phi};
+  if (e->stepper == SPC_STEPPER_RK4)
+    for (int q = 0; q < 4; ++q) live.insert(live.end(), {e->a.kx[q], e->a.ky[q], e->a.kphi[q]});
+  double *save = nullptr;
+  SPC_CUDA(e, cudaMalloc(&save, live.size() * P * sizeof(double)));
+  std::vector<std::pair<unsigned long long, long long>> ctr;
+  for (int s : e->order) ctr.push_back({e->slots[s].step, e->slots[s].remaining});
+  auto copy_all = [&](bool to_save) -> cudaError_t {
+    for (size_t k = 0; k < live.size(); ++k) {
+      double *dst = to_save ? save + k * P : live[k];
+      const double *src = to_save ? live[k] : save + k * P;
+      const cudaError_t ce = cudaMemcpyAsync(dst, src, P * sizeof(double), cudaMemcpyDeviceToDevice, e->stream);
+      if (ce != cudaSuccess) return ce;
+    }
+    return cudaSuccess;
+  };
+  auto restore = [&]() -> int {
+    const cudaError_t ce = copy_all(false);
+    if (ce != cudaSuccess) return fail(e, SPC_ERR_CUDA, "retune restore: %s", cudaGetErrorString(ce));
+    size_t i = 0;
+    for (int s : e->order) {
+      e->slots[s].step = ctr[i].first;
+      e->slots[s].remaining = ctr[i].second;
+      ++i;
+    }
+    e->dirty = true;  // the device table is rebuilt from the restored counters
+    return SPC_OK;
+  };
+  const double sb0 = e->sparse_below;
+  const int split0 = e->tile_split_tune;
+  cudaEvent_t ev[2] = {nullptr, nullptr};
+  cudaError_t ce = copy_all(true);
+  if (ce == cudaSuccess) ce = cudaEventCreate(&ev[0]);
+  if (ce == cudaSuccess) ce = cudaEventCreate(&ev[1]);
+  int rc = ce == cudaSuccess ? SPC_OK : fail(e, SPC_ERR_CUDA, "retune: %s", cudaGetErrorString(ce));
+  int best_k = 0;
+  double best_ms = 1e300;
+  for (size_t k = 0; k < cands.size() && rc == SPC_OK; ++k) {
+    e->sparse_below = cands[k].sparse;
+    e->tile_split_tune = cands[k].split;
+    e->dirty = true;
+    rc = engine_steps(e, dt, trial, false, nullptr, 0);
+    if (rc == SPC_OK) rc = restore();
+    if (rc == SPC_OK) rc = engine_layout(e);  // outside the timed region
+    if (rc == SPC_OK && cudaEventRecord(ev[0], e->stream) != cudaSuccess) rc = fail(e, SPC_ERR_CUDA, "event");
+    if (rc == SPC_OK) rc = engine_steps(e, dt, trial, false, nullptr, 0);
+    float ms = 0.0f;
+    if (rc == SPC_OK && (cudaEventRecord(ev[1], e->stream) != cudaSuccess ||
+                         cudaEventSynchronize(ev[1]) != cudaSuccess ||
+                         cudaEventElapsedTime(&ms, ev[0], ev[1]) != cudaSuccess))
+      rc = fail(e, SPC_ERR_CUDA, "retune timing");
+    if (rc == SPC_OK) rc = restore();
+    const double per = (double)ms / trial;
+    if (rc == SPC_OK && (int)k < cap && out) {
+      out[k].neighbour = e->verlet ? SPC_NEIGHBOUR_VERLET : SPC_NEIGHBOUR_CELL;
+      out[k].tile_split = tile_split_for(cands[k].split);
+      out[k].skin = 0.0;
+      out[k].sparse_below = cands[k].sparse;
+      out[k].ms_per_step = per;
+    }
+    if (rc == SPC_OK && per < best_ms) {
+      best_ms = per;
+      best_k = (int)k;
+    }
+  }
+  for (cudaEvent_t x : ev)
+    if (x) cudaEventDestroy(x);
+  cudaStreamSynchronize(e->stream);
+  cudaFree(save);
+  if (rc != SPC_OK) {  // keep the caller's settings
+    e->sparse_below = sb0;
+    e->tile_split_tune = split0;
+    e->dirty = true;
+    return rc;
+  }
+  e->sparse_below = cands[best_k].sparse;
+  e->tile_split_tune = cands[best_k].split;
+  e->dirty = true;
+  if (count) *count = (int)cands.size();
+  if (best) *best = best_k;
+  return SPC_OK;
+}
+
 // nsteps eagerly launched steps with CUDA events between the phases; out_ms[k]
 // is the mean per step of: stage, sort, gather, first pass, rest of the step,
 // whole step.

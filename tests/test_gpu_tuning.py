@@ -1,0 +1,98 @@
+"""The autotuner's candidates and in-place retuning.
+
+* spc_autotune_ex offers every tuning dimension: the kernel choice (all
+  cell-tile, the default split, all warp-per-cell), 1, 2 or 4 CTAs per cell,
+  and Verlet skins where the precision and stencil allow them.
+* Every kernel-choice candidate computes the same neighbour sets: FP64 and
+  FP32X trajectories are bit for bit the same under each of them.
+* spc_retune / spc_batch_retune leave the state and the step counters as they
+  were, so a run that retunes midway equals one that does not, bit for bit.
+"""
+import numpy as np
+import pytest
+
+from spc2_langevin_integration_gb300 import abi
+from tests._helpers import init_state
+
+pytestmark = pytest.mark.gpu
+
+PRM = dict(v0=0.02, sigma=1.3, rho=0.12, alpha=1.4, D_phi=0.01)
+N, L = 6000, 1.5
+
+
+def _params(precision, stepper=abi.STEPPER_SRK):
+    return abi.make_params(L=L, stepper=stepper, precision=precision, seed=31, **PRM)
+
+
+def test_autotune_ex_offers_every_dimension():
+    st = init_state(N, L, 90)
+    cands, best = abi.autotune_ex(N, _params(abi.PRECISION_FP64), st, trial_steps=5)
+    cell = [c for c in cands if c["neighbour"] == "cell"]
+    assert {c["tile_split"] for c in cell} == {1, 2, 4}
+    assert {c["sparse_below"] for c in cell} >= {0.0, 1e9}
+    assert any(c["neighbour"] == "verlet" for c in cands)
+    assert 0 <= best < len(cands) and all(c["ms_per_step"] > 0 for c in cands)
+    # FP32X runs the cell list only
+    cx, _ = abi.autotune_ex(N, _params(abi.PRECISION_FP32X), st, trial_steps=5)
+    assert all(c["neighbour"] == "cell" for c in cx) and len(cx) == len(cell)
+
+
+@pytest.mark.parametrize("precision", [abi.PRECISION_FP64, abi.PRECISION_FP32X])
+def test_kernel_choices_give_identical_trajectories(precision):
+    st = init_state(N, L, 91)
+    out = []
+    for sb, split in ((0.0, 1), (0.0, 2), (0.0, 4), (24.0, 1), (1e9, 1)):
+        with abi.System(N, _params(precision)) as s:
+            s.set_tuning(abi.TUNE_SPARSE_BELOW, sb)
+            s.set_tuning(abi.TUNE_TILE_SPLIT, split)
+            s.upload_state(st)
+            s.step(0.005, 30)
+            out.append(s.download_state())
+    for o in out[1:]:
+        assert np.array_equal(o, out[0])
+
+
+@pytest.mark.parametrize("precision", [abi.PRECISION_FP64, abi.PRECISION_FP32X])
+def test_retune_midway_leaves_the_run_unchanged(precision):
+    st = init_state(N, L, 92)
+    finals = []
+    for retune in (False, True):
+        with abi.System(N, _params(precision)) as s:
+            s.upload_state(st)
+            s.step(0.005, 20, graph=True)
+            if retune:
+                before, ctr = s.download_state(), s.step_counter
+                cands, best = s.retune(0.005, trial_steps=5)
+                assert len(cands) == 7 and 0 <= best < 7
+                assert np.array_equal(s.download_state(), before) and s.step_counter == ctr
+                assert s.get_tuning(abi.TUNE_TILE_SPLIT) == cands[best]["tile_split"]
+            s.step(0.005, 20, graph=True)
+            finals.append(s.download_state())
+    assert np.array_equal(finals[0], finals[1])
+
+
+def test_batch_retune_leaves_the_run_unchanged():
+    systems = [(1500, 1.0, dict(PRM, rho=0.1)), (4000, 1.3, dict(PRM, rho=0.2)),
+               (300, 0.6, dict(PRM, rho=0.16))]
+    ntot = sum(n for n, _, _ in systems)
+    ctot = sum(abi.cells_of(Lb, p["rho"]) for _, Lb, p in systems)
+    finals = []
+    for retune in (False, True):
+        with abi.Batch(abi.STEPPER_EULER, abi.PRECISION_FP32X, 3, ntot, ctot) as b:
+            slots = [b.admit(n, abi.make_params(L=Lb, stepper=abi.STEPPER_EULER,
+                                                precision=abi.PRECISION_FP32X, seed=4, system_id=k, **p),
+                             init_state(n, Lb, 93 + k), steps=60)
+                     for k, (n, Lb, p) in enumerate(systems)]
+            b.step(0.01, 30)
+            if retune:
+                before = [b.download(s) for s in slots]
+                status = [b.status(s) for s in slots]
+                cands, best = b.retune(0.01, trial_steps=5)
+                assert len(cands) == 7
+                assert all(np.array_equal(b.download(s), x) for s, x in zip(slots, before))
+                assert [b.status(s) for s in slots] == status
+            b.step(0.01, 40)  # past the budgets: every system stops at 60 steps
+            finals.append([b.download(s) for s in slots])
+            assert all(b.status(s)[1] == 0 for s in slots)
+    for x, y in zip(*finals):
+        assert np.array_equal(x, y)
