@@ -12,6 +12,11 @@ join the next chunk: their work overlaps with the running ones on the device.
 A system's result does not depend on what else is in the batch (its noise is
 keyed by seed, system id, step and particle; its neighbour sums see only its
 own particles), so a served result equals the same request run alone.
+
+Host work overlaps the device: a chunk is enqueued on the batch's stream and,
+while it runs, the server draws the initial states of the requests that have
+arrived (the costly host step for large N), so that their admission after the
+chunk is only the upload.
 """
 from __future__ import annotations
 
@@ -44,6 +49,7 @@ class Request:
     admitted_at: Optional[float] = None
     finished_at: Optional[float] = None
     result: Optional[np.ndarray] = None
+    prepared: Optional[tuple] = None  # inputs() drawn ahead of admission
 
     def params(self, stepper: int, precision: int) -> abi.Params:
         return abi.make_params(L=self.L, v0=self.v0, sigma=self.sigma, rho=self.rho,
@@ -119,13 +125,17 @@ class Server:
     """Continuous batching over one spc_batch.
 
     backend: an object with the Batch interface (abi.Batch on a GPU; tests
-    pass a stand-in to check the scheduling on the CPU)."""
+    pass a stand-in to check the scheduling on the CPU).  keep_results: True
+    keeps every result on its request, a set of request ids keeps those."""
 
     def __init__(self, backend, stepper: int, precision: int, dt: float = 0.01,
                  chunk: int = 50, backfill: int = 64,
                  clock: Callable[[], float] = time.perf_counter, keep_results: bool = False,
-                 limits: Optional[tuple[int, int]] = None):
+                 limits: Optional[tuple[int, int]] = None, prefetch_particles: int = 1 << 21):
         self.b = backend
+        # initial states drawn ahead, while a chunk runs: at most this many
+        # particles' worth (host memory bound), in arrival order
+        self.prefetch_particles = int(prefetch_particles)
         self.limits = limits  # (max_particles, max_cells): larger requests are refused
         self.stepper, self.precision = stepper, precision
         self.dt, self.chunk, self.backfill = dt, int(chunk), int(backfill)
@@ -152,6 +162,21 @@ class Server:
         u = self.b.usage()
         return u["systems"] < cap["systems"] and u["particles"] + req.n <= cap["particles"]
 
+    def _prefetch(self, waiting) -> int:
+        """Draw the initial states of waiting requests (arrival order) up to
+        the prefetch budget; returns how many were drawn."""
+        held = sum(r.n for r in waiting if r.prepared is not None)
+        drawn = 0
+        for req in waiting:
+            if req.prepared is not None:
+                continue
+            if held + req.n > self.prefetch_particles:
+                break
+            req.prepared = req.inputs()
+            held += req.n
+            drawn += 1
+        return drawn
+
     def run(self, trace: list[Request], time_scale: float = 1.0) -> ServeStats:
         pending = collections.deque(sorted(trace, key=lambda r: r.arrival))
         waiting: collections.deque[Request] = collections.deque()
@@ -161,6 +186,7 @@ class Server:
         now = lambda: (self.clock() - t0) / time_scale  # noqa: E731
         max_active = 0
         self.refused: list[Request] = []
+        self.prefetched = 0
         while pending or waiting or active:
             t = now()
             while pending and pending[0].arrival <= t:
@@ -177,7 +203,8 @@ class Server:
                 if active and not self._may_fit(req):
                     skipped += 1  # its initial state is not generated until it may fit
                     continue
-                st, om = req.inputs()
+                st, om = req.prepared if req.prepared is not None else req.inputs()
+                req.prepared = None
                 try:
                     slot = self.b.admit(req.n, req.params(self.stepper, self.precision), st, om,
                                         steps=req.steps)
@@ -196,14 +223,22 @@ class Server:
                     if wait > 0:
                         time.sleep(min(wait * time_scale, 0.05))
                 continue
-            self.b.step(self.dt, self.chunk)
+            self.b.step(self.dt, self.chunk)  # enqueued; runs while the host works
+            t = now()
+            while pending and pending[0].arrival <= t:
+                req = pending.popleft()
+                if self.limits and (req.n > self.limits[0] or req.cells > self.limits[1]):
+                    self.refused.append(req)
+                else:
+                    waiting.append(req)
+            self.prefetched += self._prefetch(waiting)
             self.b.synchronize()
             for slot in list(active):
                 _, remaining = self.b.status(slot)
                 if remaining <= 0:
                     req = active.pop(slot)
                     res = self.b.download(slot)
-                    if self.keep_results:
+                    if self.keep_results is True or (self.keep_results and req.rid in self.keep_results):
                         req.result = res
                     self.b.release(slot)
                     req.finished_at = now()
