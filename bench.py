@@ -881,7 +881,10 @@ def run_configured(abi, torch, w, precision, params, tuning, steps, warmup, rank
     `warmup` bench steps run first (graph capture, caches); then the state and
     the step counter are reset, so the timed steps are the configured run.
     After each bench step, outside the timers, the global and local order
-    parameters are recorded (the drift series)."""
+    parameters are recorded (the drift series), and a cell-list handle whose
+    cost per step has moved by more than 25% since its last tuning is
+    retuned in place (spc_retune: the kernel choice and CTAs per cell on the
+    current, clustering state; state and step counter are left as they were)."""
     import ctypes as C
     n = w["n"]
     total = total_steps or w["steps"]
@@ -912,7 +915,8 @@ def run_configured(abi, torch, w, precision, params, tuning, steps, warmup, rank
     s.step_counter = 0
     ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
           for _ in range(steps)]
-    wall, series = [], []
+    wall, series, retunes = [], [], []
+    tuned_at = None  # ms per simulation step when last tuned
     if dist is not None:
         dist.barrier()
     torch.cuda.synchronize()
@@ -929,6 +933,14 @@ def run_configured(abi, torch, w, precision, params, tuning, steps, warmup, rank
         wall.append((time.perf_counter() - t0) * 1e3)
         o = s.order_params()
         series.append((per * (k + 1), o["R"], o["R_local"]))
+        cost = ev[k][0].elapsed_time(ev[k][1]) / per
+        if params.neighbour == abi.NEIGHBOUR_CELL:
+            if tuned_at is None:
+                tuned_at = cost
+            elif abs(cost - tuned_at) > 0.25 * tuned_at and k + 1 < steps:
+                cands, best = s.retune(dt, trial_steps=10)
+                retunes.append({"after_step": per * (k + 1), "choice": cands[best]})
+                tuned_at = cost
     torch.cuda.synchronize()
     if dist is not None:
         dist.barrier()
@@ -940,7 +952,7 @@ def run_configured(abi, torch, w, precision, params, tuning, steps, warmup, rank
     L.spc_free_pinned(q)
     s.close()
     return {"ms": ms, "e2e_ms": e2e_ms, "steps_per_bench_step": per, "series": series,
-            "profile_ms": prof, "launches": launches,
+            "profile_ms": prof, "launches": launches, "retunes": retunes,
             "ms_per_bench_step": [a.elapsed_time(b) for a, b in ev]}
 
 
@@ -1236,6 +1248,7 @@ def main():
             "ms_per_bench_step": r["ms_per_bench_step"],
             "profile_ms_final_state": r["profile_ms"],
             "autotune": tuned[name][2],
+            "retunes": r["retunes"],
             "order_params_series": [[int(k), R, Rl] for k, R, Rl in r["series"]]}
         if name != "fp64":
             per_form[name]["drift_vs_fp64"] = drift_of(runs["fp64"]["series"], r["series"])

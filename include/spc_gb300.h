@@ -224,10 +224,12 @@ int spc_profile_steps(spc_handle *h, double dt, int32_t nsteps, double *out_ms, 
  * kept; a particle with more candidates within rho + skin scans its whole
  * cell stencil instead (same results).  Between 1 and the row capacity the
  * handle allocated (its default value); the rows are rebuilt on the next step.
- * SPC_TUNE_TILE_SPLIT: CTAs per cell of the cell-tile passes, 1 to 8 (each
- * takes a run of 32-particle chunks of the cell), or 0 for the default, 1;
- * spc_get_tuning returns the split in effect.  Results are bitwise
- * independent of it in FP64.
+ * SPC_TUNE_TILE_SPLIT: CTAs per cell of the cell-tile passes, 1 to 8, or 0
+ * for the default, 1.  Each CTA takes whole groups of the cell's particles
+ * (128 in the float forms, 64 in FP64), so a cell of at most one group stays
+ * on one CTA and only cells that hold several groups (a clustered state) are
+ * spread out.  spc_get_tuning returns the split in effect.  Results are
+ * bitwise independent of it in every precision.
  * spc_get_tuning reads a knob back. */
 enum { SPC_TUNE_SPARSE_BELOW = 1, SPC_TUNE_VERLET_ROW_LIMIT = 2, SPC_TUNE_TILE_SPLIT = 3 };
 int spc_set_tuning(spc_handle *h, int32_t key, double value);

@@ -83,22 +83,29 @@ constexpr int kMaskWords = kTileCap / 32;
 static_assert(kMaskWords % 4 == 0, "mask words come in groups of four");
 
 // Work item `item` of the cell-tile kernels: cell c = item / K and part
-// item % K of its particles, K = a.tile_split CTAs per cell.  Parts are
-// multiples of 32 particles, so a warp chunk never straddles two CTAs.  c0 is
-// the cell's first particle (the own cell's stencil entry starts there).
+// item % K of its particles, K = a.tile_split CTAs per cell.  A part is a
+// whole number of the kernel's particle groups (GROUP = the CTA's threads,
+// the particles it processes at a time), so a cell of at most GROUP
+// particles stays one item and is staged once, while the few cells of a
+// clustered state that hold several groups are spread over up to K CTAs
+// instead of running their groups one after another on one CTA (the tail of
+// a single-wave pass).  Items past a cell's last group are empty.  c0 is the
+// cell's first particle (the own cell's stencil entry starts there).
 struct TileItem {
   int c, c0, cb, ce;
 };
 
 __device__ __forceinline__ int tile_items(const KArgs &a) { return a.ncell_tile * max(a.tile_split, 1); }
 
+template <int GROUP>
 __device__ __forceinline__ bool tile_item(const KArgs &a, int item, TileItem &t) {
   const int K = max(a.tile_split, 1);
   t.c = item / K;
   const int h = item - t.c * K;
   t.c0 = a.cell_start[t.c];
   const int c1 = a.cell_start[t.c + 1];
-  const int per = ((c1 - t.c0 + K - 1) / K + 31) & ~31;
+  const int groups = (c1 - t.c0 + GROUP - 1) / GROUP;
+  const int per = ((groups + K - 1) / K) * GROUP;
   t.cb = t.c0 + h * per;
   t.ce = min(c1, t.cb + per);
   return t.cb < t.ce;
@@ -171,7 +178,7 @@ __global__ void __launch_bounds__(kTileThreads32, kTileMinBlocks32) k_tile_fp32c
   const int nitems = tile_items(a);
   for (int item = blockIdx.x; item < nitems; item += gridDim.x) {
     TileItem ti;
-    if (!tile_item(a, item, ti)) continue;
+    if (!tile_item<kTileThreads32>(a, item, ti)) continue;
     const int c = ti.c, c0 = ti.c0, cb = ti.cb, ce = ti.ce;
     const SysDesc &sd = a.sys[a.sys_of_c[c]];
     const SysConst &sc = sd.sc;
@@ -421,7 +428,7 @@ __global__ void __launch_bounds__(kTileThreads32, kTileMinBlocks32) k_tile_fp32x
   const int nitems = tile_items(a);
   for (int item = blockIdx.x; item < nitems; item += gridDim.x) {
     TileItem ti;
-    if (!tile_item(a, item, ti)) continue;
+    if (!tile_item<kTileThreads32>(a, item, ti)) continue;
     const int c = ti.c, c0 = ti.c0, cb = ti.cb, ce = ti.ce;
     const SysDesc &sd = a.sys[a.sys_of_c[c]];
     const SysConst &sc = sd.sc;
@@ -579,7 +586,7 @@ __global__ void __launch_bounds__(kTileThreads64) k_tile_fp64(KArgs a, int epi) 
   const int nitems = tile_items(a);
   for (int item = blockIdx.x; item < nitems; item += gridDim.x) {
     TileItem ti;
-    if (!tile_item(a, item, ti)) continue;
+    if (!tile_item<kTileThreads64>(a, item, ti)) continue;
     const int c = ti.c, c0 = ti.c0, cb = ti.cb, ce = ti.ce;
     const SysDesc &sd = a.sys[a.sys_of_c[c]];
     const SysConst &sc = sd.sc;

@@ -37,11 +37,21 @@ def test_autotune_ex_offers_every_dimension():
     assert all(c["neighbour"] == "cell" for c in cx) and len(cx) == len(cell)
 
 
-@pytest.mark.parametrize("precision", [abi.PRECISION_FP64, abi.PRECISION_FP32X])
+@pytest.mark.parametrize("precision", [abi.PRECISION_FP64, abi.PRECISION_FP32X, abi.PRECISION_FP32C])
 def test_kernel_choices_give_identical_trajectories(precision):
+    """FP64 and FP32X: every kernel choice; FP32C: every CTA split of the
+    cell-tile kernels (its cell-tile and warp-per-cell kernels sum in
+    different orders).  The state is clustered into a patch so that cells
+    hold several particle groups and the splits really spread them."""
+    rng = np.random.default_rng(91)
     st = init_state(N, L, 91)
+    st[0::3] = 0.2 + 0.45 * rng.random(N)  # 6,000 particles in a 0.45 x 0.45 patch
+    st[1::3] = 0.2 + 0.45 * rng.random(N)
+    choices = ((0.0, 1), (0.0, 2), (0.0, 4), (24.0, 1), (1e9, 1))
+    if precision == abi.PRECISION_FP32C:
+        choices = choices[:3]
     out = []
-    for sb, split in ((0.0, 1), (0.0, 2), (0.0, 4), (24.0, 1), (1e9, 1)):
+    for sb, split in choices:
         with abi.System(N, _params(precision)) as s:
             s.set_tuning(abi.TUNE_SPARSE_BELOW, sb)
             s.set_tuning(abi.TUNE_TILE_SPLIT, split)
