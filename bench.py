@@ -600,15 +600,15 @@ def run_large(precision, steps):
     st[2::3] = rng.uniform(-np.pi, np.pi, n)
     p = abi.make_params(L=L, v0=w["v0"], sigma=w["sigma"], rho=w["rho"], alpha=w["alpha"],
                         D_phi=w["D_phi"], stepper=abi.STEPPER_RK4, precision=precision,
-                        seed=w["seed"], neighbour=abi.NEIGHBOUR_VERLET, skin=w["skin"])
+                        seed=w["seed"], skin=w["skin"])
     t0 = time.perf_counter()
-    best, sb, ms = abi.autotune(n, p, st, dt=w["dt"], trial_steps=2)
+    cands, k = abi.autotune_ex(n, p, st, dt=w["dt"], trial_steps=2)
     tune_s = time.perf_counter() - t0
-    names = ["cell (default kernels)", "cell (cell-tile)", "cell (warp-per-cell)"]
-    names += ["verlet skin %.3g" % (f * w["rho"]) for f in (0.1, 0.2, 0.4)][: len(ms) - 3]
+    best, tun = abi.params_with(p, cands[k]), cands[k]
     with abi.System(n, best) as s:
         if best.neighbour == abi.NEIGHBOUR_CELL:
-            s.set_tuning(abi.TUNE_SPARSE_BELOW, sb)
+            s.set_tuning(abi.TUNE_SPARSE_BELOW, tun["sparse_below"])
+            s.set_tuning(abi.TUNE_TILE_SPLIT, tun["tile_split"])
         s.upload_state(st)
         stream = torch.cuda.ExternalStream(s.stream)
         s.step(w["dt"], steps, graph=True)  # capture + warm
@@ -619,14 +619,14 @@ def run_large(precision, steps):
         e1.record(stream)
         s.synchronize()
         t_ms = e0.elapsed_time(e1)
+        final = s.download_state()
+        o = s.order_params()
         prof = s.profile_steps(w["dt"], 1)
         launches = s.graph_nodes()
     return {"value": n * steps / (t_ms / 1e3), "unit": "particle-steps/s", "steps": steps,
             "ms_per_step": t_ms / steps, "profile_ms_one_step": prof,
-            "gpu_launches_per_replay": launches,
-            "autotune": {"choice": {"neighbour": "verlet" if best.neighbour == abi.NEIGHBOUR_VERLET
-                                    else "cell", "skin": best.skin, "sparse_below": sb},
-                         "candidates_ms_per_step": dict(zip(names, ms)), "tuning_s": tune_s}}
+            "gpu_launches_per_replay": launches, "order_params": o, "_state": final,
+            "autotune": {"choice": tun, "candidates": cands, "tuning_s": tune_s}}
 
 
 VA = dict(name="vortex_arrays_srk_n51200_L8", n=51200, L=8.0, velocity=0.1, mu_plus=100.0,
@@ -881,10 +881,14 @@ def run_configured(abi, torch, w, precision, params, tuning, steps, warmup, rank
     `warmup` bench steps run first (graph capture, caches); then the state and
     the step counter are reset, so the timed steps are the configured run.
     After each bench step, outside the timers, the global and local order
-    parameters are recorded (the drift series), and a cell-list handle whose
-    cost per step has moved by more than 25% since its last tuning is
-    retuned in place (spc_retune: the kernel choice and CTAs per cell on the
-    current, clustering state; state and step counter are left as they were)."""
+    parameters are recorded (the drift series), and a handle whose cost per
+    step has moved by more than 25% since its last tuning is tuned again on
+    the current, clustering state: a cell-list handle in place (spc_retune:
+    kernel choice and CTAs per cell; state and step counter are left as they
+    were), a Verlet-row handle by spc_autotune_ex over every method, moving
+    to a new handle (state, frequencies and step counter carried over) when
+    another method wins.  The step graph is captured again before the next
+    bench step (spc_prepare_graph), so no capture falls inside the timers."""
     import ctypes as C
     n = w["n"]
     total = total_steps or w["steps"]
@@ -934,13 +938,30 @@ def run_configured(abi, torch, w, precision, params, tuning, steps, warmup, rank
         o = s.order_params()
         series.append((per * (k + 1), o["R"], o["R_local"]))
         cost = ev[k][0].elapsed_time(ev[k][1]) / per
-        if params.neighbour == abi.NEIGHBOUR_CELL:
-            if tuned_at is None:
-                tuned_at = cost
-            elif abs(cost - tuned_at) > 0.25 * tuned_at and k + 1 < steps:
+        if tuned_at is None:
+            tuned_at = cost
+        elif abs(cost - tuned_at) > 0.25 * tuned_at and k + 1 < steps:
+            if params.neighbour == abi.NEIGHBOUR_CELL:
                 cands, best = s.retune(dt, trial_steps=10)
-                retunes.append({"after_step": per * (k + 1), "choice": cands[best]})
-                tuned_at = cost
+                choice = cands[best]
+            else:
+                cands, best = abi.autotune_ex(n, params, host, omega, dt=dt, trial_steps=5)
+                choice = cands[best]
+                if choice["neighbour"] != "verlet" or choice["skin"] != params.skin:
+                    ctr = s.step_counter
+                    s.close()
+                    params = abi.params_with(params, choice)
+                    s = abi.System(n, params)
+                    if params.neighbour == abi.NEIGHBOUR_CELL:
+                        s.set_tuning(abi.TUNE_SPARSE_BELOW, choice["sparse_below"])
+                        s.set_tuning(abi.TUNE_TILE_SPLIT, choice["tile_split"])
+                    s.upload_omega(omega)
+                    s.upload_state(host)
+                    s.step_counter = ctr
+                    stream = torch.cuda.ExternalStream(s.stream)
+            s.prepare_graph(dt, SIM_STEPS_PER_BENCH_STEP)
+            retunes.append({"after_step": per * (k + 1), "choice": choice})
+            tuned_at = cost
     torch.cuda.synchronize()
     if dist is not None:
         dist.barrier()
@@ -1066,12 +1087,21 @@ def main():
         return
     if args.workload == "large":
         from spc2_langevin_integration_gb300 import abi
+        # each form: a warm replay of `steps` steps, then the timed replay of the
+        # next `steps` (the same number for every form, so the final states
+        # can be compared: RK4 with D = 0 is deterministic)
         out = {"metric": "particle-steps/s", "workload": LARGE["name"], "config": LARGE,
-               "fp32c": run_large(abi.PRECISION_FP32C, 20),
+               "fp32x": run_large(abi.PRECISION_FP32X, 4),
+               "fp32c": run_large(abi.PRECISION_FP32C, 4),
                "fp64": run_large(abi.PRECISION_FP64, 4),
                "note": "throughput over a timed prefix of the 2,000-step run (one graph replay "
                        "per form after a warm replay); working set >> L2"}
-        out["fp32c_over_fp64"] = out["fp32c"]["value"] / out["fp64"]["value"]
+        ref = out["fp64"].pop("_state")
+        for f in ("fp32x", "fp32c"):
+            d = (out[f].pop("_state") - ref).reshape(-1, 3)
+            d[:, :2] -= LARGE["L"] * np.round(d[:, :2] / LARGE["L"])
+            out[f]["max_abs_state_diff_vs_fp64_after_8_steps"] = float(np.abs(d).max())
+            out[f + "_over_fp64"] = out[f]["value"] / out["fp64"]["value"]
         print(json.dumps(out))
         return
     if args.workload == "drift":

@@ -137,6 +137,12 @@ int spc_step(spc_handle *h, double *t_inout, double dt, int32_t nsteps);
 /* Same, captured as a CUDA graph of nsteps steps on first use and replayed
  * (fixed-length step loops; requires Philox noise). */
 int spc_step_graph(spc_handle *h, double *t_inout, double dt, int32_t nsteps);
+/* Capture the graph spc_step_graph(h, ., dt, nsteps) replays, without
+ * launching it (no counterpart in the reference): after a change that drops
+ * the cached graph (a tuning change, a new handle), the capture cost then
+ * falls here instead of inside the next timed or latency-bound call.  State
+ * and step counter are untouched. */
+int spc_prepare_graph(spc_handle *h, double dt, int32_t nsteps);
 
 /* The engine loop with its observers, on the device
  * (SimulationEngine.cpp:149-161, SimulationEnginePtr.cpp:106-115): nsteps

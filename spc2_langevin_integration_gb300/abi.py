@@ -155,6 +155,7 @@ def lib() -> C.CDLL:
                              C.POINTER(C.c_int32), C.POINTER(C.c_int32)]
     L.spc_batch_retune.argtypes = [H, C.c_double, C.c_int32, C.POINTER(Tuning), C.c_int32,
                                    C.POINTER(C.c_int32), C.POINTER(C.c_int32)]
+    L.spc_prepare_graph.argtypes = [H, C.c_double, C.c_int32]
     L.spc_graph_nodes.argtypes = [H, C.POINTER(C.c_int64)]
     L.spc_run.argtypes = [H, dp, C.c_double, C.c_int64, C.c_int32, C.c_void_p, OBSERVE_FN,
                           C.c_void_p, C.POINTER(C.c_int64)]
@@ -290,6 +291,10 @@ class System:
         self._check(f(self.h, C.byref(t), dt, int(nsteps)), self.h)
         self.t = t.value
         return self.t
+
+    def prepare_graph(self, dt: float, nsteps: int):
+        """spc_prepare_graph: capture the step graph without running it."""
+        self._check(self._L.spc_prepare_graph(self.h, dt, int(nsteps)), self.h)
 
     def run(self, dt: float, nsteps: int, period: int = 1, observe=None, fn=None) -> int:
         """The engine loop with its observers on the device (spc_run): after

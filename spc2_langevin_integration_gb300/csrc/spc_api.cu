@@ -325,6 +325,14 @@ int spc_step_graph(spc_handle *h, double *t_inout, double dt, int32_t nsteps) {
   return SPC_OK;
 }
 
+int spc_prepare_graph(spc_handle *h, double dt, int32_t nsteps) {
+  if (!h) return hfail(h, SPC_ERR_INVALID, "NULL argument");
+  if (nsteps <= 0) return hfail(h, SPC_ERR_INVALID, "nsteps must be positive");
+  SPC_TRY(check_ready(h));
+  if (h->e.injecting) return fail(&h->e, SPC_ERR_STATE, "graph replay needs Philox noise");
+  return engine_prepare_graph(&h->e, dt, nsteps);
+}
+
 int spc_run(spc_handle *h, double *t_inout, double dt, int64_t nsteps, int32_t period,
             const uint8_t *observe, spc_observe_fn fn, void *user, int64_t *steps_done) {
   if (steps_done) *steps_done = 0;

@@ -629,9 +629,19 @@ inline int system_class(const Engine *e, const SysHost &h) {
 }
 
 // Rebuild the device layout tables from the host mirror.
+// What a captured step graph bakes in beyond device pointers: kernel grid
+// sizes and the counts passed by value.  A layout that leaves these unchanged
+// (new step counters or budgets, a system replaced by one of the same shape)
+// keeps the cached graphs, whose kernels read the rewritten tables.
+inline std::vector<long long> launch_shape(const Engine *e) {
+  const KArgs &a = e->a;
+  return {e->nsys, e->n_active, e->ncell_total, e->ntiles, e->radix_bits, e->sort_passes, e->ncell_tile,
+          e->ncell_warp, e->ncell_va, e->n_ap_all, e->has_cells, a.n_ap, a.tile_split, a.hist_len};
+}
+
 inline int engine_layout(Engine *e) {
   if (!e->dirty) return SPC_OK;
-  drop_graph(e);
+  const std::vector<long long> shape0 = launch_shape(e);
   e->verlet_stale = true;  // slots and systems move: rebuild the rows
   std::vector<SysDesc> table;
   std::vector<int> ap, ap_all;
@@ -696,6 +706,7 @@ inline int engine_layout(Engine *e) {
     // host-side copies above read pageable memory: finish before `table` dies
     SPC_CUDA(e, cudaStreamSynchronize(e->stream));
   }
+  if (launch_shape(e) != shape0) drop_graph(e);
   e->dirty = false;
   return SPC_OK;
 }
@@ -931,6 +942,47 @@ inline void mirror_call(Engine *e, int nsteps) {
 
 // nsteps steps of every active system (eagerly launched or as a replayed
 // CUDA graph).  noise (single-system injection) is consumed per step.
+// The graph of nsteps steps at dt, captured and instantiated unless the
+// cached one fits (the layout must be current).
+inline int engine_capture(Engine *e, double dt, int nsteps) {
+  if (e->graph && e->graph_steps == nsteps && e->graph_dt == dt) return SPC_OK;
+  drop_graph(e);
+  const int sb = blocks_for(e->nsys, 128);
+  cudaGraph_t g = nullptr;
+  SPC_CUDA(e, cudaStreamBeginCapture(e->stream, cudaStreamCaptureModeThreadLocal));
+  int rc = SPC_OK;
+  k_begin_call<<<sb, 128, 0, e->stream>>>(e->d_sys, e->nsys, nsteps);
+  for (int s = 0; s < nsteps && rc == SPC_OK; ++s) rc = enqueue_step(e, dt, s, nullptr);
+  k_end_call<<<sb, 128, 0, e->stream>>>(e->d_sys, e->nsys);
+  cudaError_t ce = cudaStreamEndCapture(e->stream, &g);
+  if (rc != SPC_OK) {
+    if (g) cudaGraphDestroy(g);
+    return rc;
+  }
+  if (ce != cudaSuccess) return fail(e, SPC_ERR_CUDA, "graph capture: %s", cudaGetErrorString(ce));
+  e->graph_nodes = 0;
+  cudaGraphGetNodes(g, nullptr, &e->graph_nodes);
+  ce = cudaGraphInstantiate(&e->graph, g, 0);
+  cudaGraphDestroy(g);
+  if (ce != cudaSuccess) {
+    e->graph = nullptr;
+    return fail(e, SPC_ERR_CUDA, "graph instantiate: %s", cudaGetErrorString(ce));
+  }
+  e->graph_steps = nsteps;
+  e->graph_dt = dt;
+  return SPC_OK;
+}
+
+// Captures (without launching) the step graph a later graph call of nsteps
+// steps at dt will replay, so that its capture cost falls outside whatever
+// the caller times.
+inline int engine_prepare_graph(Engine *e, double dt, int nsteps) {
+  SPC_TRY(engine_set_device(e));
+  SPC_TRY(engine_layout(e));
+  if (e->nsys == 0 || nsteps <= 0) return SPC_OK;
+  return engine_capture(e, dt, nsteps);
+}
+
 inline int engine_steps(Engine *e, double dt, int nsteps, bool use_graph, const double *noise_base,
                         long long noise_per_step) {
   SPC_TRY(engine_set_device(e));
@@ -946,31 +998,7 @@ inline int engine_steps(Engine *e, double dt, int nsteps, bool use_graph, const 
     k_end_call<<<sb, 128, 0, e->stream>>>(e->d_sys, e->nsys);
     SPC_LAUNCHED(e);
   } else {
-    if (!e->graph || e->graph_steps != nsteps || e->graph_dt != dt) {
-      drop_graph(e);
-      cudaGraph_t g = nullptr;
-      SPC_CUDA(e, cudaStreamBeginCapture(e->stream, cudaStreamCaptureModeThreadLocal));
-      int rc = SPC_OK;
-      k_begin_call<<<sb, 128, 0, e->stream>>>(e->d_sys, e->nsys, nsteps);
-      for (int s = 0; s < nsteps && rc == SPC_OK; ++s) rc = enqueue_step(e, dt, s, nullptr);
-      k_end_call<<<sb, 128, 0, e->stream>>>(e->d_sys, e->nsys);
-      cudaError_t ce = cudaStreamEndCapture(e->stream, &g);
-      if (rc != SPC_OK) {
-        if (g) cudaGraphDestroy(g);
-        return rc;
-      }
-      if (ce != cudaSuccess) return fail(e, SPC_ERR_CUDA, "graph capture: %s", cudaGetErrorString(ce));
-      e->graph_nodes = 0;
-      cudaGraphGetNodes(g, nullptr, &e->graph_nodes);
-      ce = cudaGraphInstantiate(&e->graph, g, 0);
-      cudaGraphDestroy(g);
-      if (ce != cudaSuccess) {
-        e->graph = nullptr;
-        return fail(e, SPC_ERR_CUDA, "graph instantiate: %s", cudaGetErrorString(ce));
-      }
-      e->graph_steps = nsteps;
-      e->graph_dt = dt;
-    }
+    SPC_TRY(engine_capture(e, dt, nsteps));
     SPC_CUDA(e, cudaGraphLaunch(e->graph, e->stream));
   }
   mirror_call(e, nsteps);

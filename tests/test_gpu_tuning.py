@@ -76,6 +76,9 @@ def test_retune_midway_leaves_the_run_unchanged(precision):
                 assert len(cands) == 7 and 0 <= best < 7
                 assert np.array_equal(s.download_state(), before) and s.step_counter == ctr
                 assert s.get_tuning(abi.TUNE_TILE_SPLIT) == cands[best]["tile_split"]
+                s.prepare_graph(0.005, 20)  # captured, not run: state and counter unchanged
+                assert s.graph_nodes() > 0
+                assert np.array_equal(s.download_state(), before) and s.step_counter == ctr
             s.step(0.005, 20, graph=True)
             finals.append(s.download_state())
     assert np.array_equal(finals[0], finals[1])
