@@ -536,6 +536,7 @@ int spc_rhs_rk(spc_handle *h, const double *k_prev, double k_coef, double dt, do
   SPC_LAUNCHED(e);
   KArgs a = base;
   a.dt = dt;
+  a.sdt = std::sqrt(dt);
   SPC_TRY(verlet_prepare(e));
   SPC_TRY(open_eval(e, 1));
   SPC_TRY(eval_stage(e, a, 1, 4, k_coef * dt));
@@ -1289,6 +1290,7 @@ extern "C" int spc_rhs_srk_noalloc(const spc_params *p, int32_t n, const double 
   e.ncell_tile = a.ncell_tile;
   e.ncell_warp = 0;
   a.n_ap = sc.allpairs ? 1 : 0;
+  e.ap_items = sc.allpairs ? (n + kAllPairsThreads - 1) / kAllPairsThreads : 0;
   a.hist_len = (1 << e.radix_bits) * e.ntiles;
   SysHost h;
   h.used = true;

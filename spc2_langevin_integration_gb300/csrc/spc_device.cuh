@@ -33,6 +33,10 @@ __device__ __forceinline__ double ddiv_by(double a, double b, double y) {
   return __fma_rn(r, y, q);
 }
 __device__ __forceinline__ double drcp(double b) { return __drcp_rn(b); }
+// sqrt(3) and RN(1 / sqrt(3)) for the SRK update's U2 / sqrt(3) (by ddiv_by,
+// bitwise the division)
+constexpr double kSqrt3 = 1.7320508075688772;
+constexpr double kRcpSqrt3 = 1.0 / kSqrt3;
 __device__ __forceinline__ double dsqrt(double a) { return __dsqrt_rn(a); }
 
 // FP32X fixed point.  A value v with |v| <= 1 is held as the integer
@@ -81,6 +85,7 @@ struct SysConst {
   // sum_j d_j sin phi_j): 2^xq2 per unit, |d_j| <= |sigma| < 2^(52 - xq2)
   double cos_ad, sin_ad;
   int xq2;
+  double s2D;     // sqrt(2 D), rounded once (the update's per-particle factor)
   // Verlet rows (vR = 0: the system uses the cell-list passes)
   int vR;         // stencil radius in cells, ceil(r_max / cell)
   float vr2;      // build: candidates with float dr^2 <= vr2 (r_max^2 plus a margin) are listed

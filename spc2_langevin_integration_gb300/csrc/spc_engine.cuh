@@ -84,6 +84,7 @@ inline SysConst make_sysconst(const spc_params &p, int n) {
   sc.L_pow2 = is_pow2(p.L);
   sc.cos_a = (float)std::cos(p.alpha);
   sc.sin_a = (float)std::sin(p.alpha);
+  sc.s2D = std::sqrt(2.0 * p.D_phi);  // correctly rounded, as the device's sqrt
   sc.cos_ad = std::cos(p.alpha);
   sc.sin_ad = std::sin(p.alpha);
   {
@@ -187,6 +188,8 @@ struct Engine {
   int *d_ap = nullptr;      // cells of the all-pairs systems the all-pairs kernel integrates
   int *d_ap_all = nullptr;  // ... and of every all-pairs system (diagnostics)
   int n_ap_all = 0;
+  // particle blocks (work items of k_allpairs_pass) of those systems
+  int ap_items = 0, ap_items_all = 0;
   unsigned long long *d_clamped = nullptr;
   uint32_t *keys_alt = nullptr, *vals_alt = nullptr, *hist = nullptr, *part = nullptr;
   double *aos = nullptr;  // AoS staging (12 x pool_cap doubles)
@@ -636,7 +639,8 @@ inline int system_class(const Engine *e, const SysHost &h) {
 inline std::vector<long long> launch_shape(const Engine *e) {
   const KArgs &a = e->a;
   return {e->nsys, e->n_active, e->ncell_total, e->ntiles, e->radix_bits, e->sort_passes, e->ncell_tile,
-          e->ncell_warp, e->ncell_va, e->n_ap_all, e->has_cells, a.n_ap, a.tile_split, a.hist_len};
+          e->ncell_warp, e->ncell_va, e->n_ap_all, e->has_cells, a.n_ap, a.tile_split, a.hist_len,
+          e->ap_items, e->ap_items_all};
 }
 
 inline int engine_layout(Engine *e) {
@@ -650,14 +654,22 @@ inline int engine_layout(Engine *e) {
   // cell-tile systems first, then warp-per-cell, vortex-arrays and all-pairs
   // systems, so that each neighbour kernel covers one contiguous range of cells
   int ncell_tile = 0, ncell_warp = 0, ncell_va = 0;
+  e->ap_items = e->ap_items_all = 0;
   for (int cls = 0; cls < 4; ++cls) {
     for (int slot : e->order) {
       const SysHost &h = e->slots[slot];
       if (system_class(e, h) != cls) continue;
       e->slot_layout[slot] = (int)table.size();
       table.push_back(desc_of(h, dense, cells));
-      if (cls == 3) ap.push_back(cells);
-      if (h.sc.allpairs) ap_all.push_back(cells);
+      const int blocks = (h.n + kAllPairsThreads - 1) / kAllPairsThreads;
+      if (cls == 3) {
+        ap.push_back(cells);
+        e->ap_items += blocks;
+      }
+      if (h.sc.allpairs) {
+        ap_all.push_back(cells);
+        e->ap_items_all += blocks;
+      }
       dense += h.n;
       cells += h.ncell;
       if (cls == 0) ncell_tile += h.ncell;
@@ -809,7 +821,7 @@ int launch_pass_t(Engine *e, const KArgs &a, int epi) {
     b.ap_cells = e->d_ap_all;
     b.n_ap = e->n_ap_all;
     if (b.n_ap > 0) {
-      k_allpairs_pass<PREC, KIND><<<std::min(b.n_ap, 152 * 16), kAllPairsThreads, 0, st>>>(b, epi);
+      k_allpairs_pass<PREC, KIND><<<std::min(e->ap_items_all, 152 * 16), kAllPairsThreads, 0, st>>>(b, epi);
       SPC_LAUNCHED(e);
     }
     if (e->ncell_total > e->n_ap_all) {
@@ -822,7 +834,7 @@ int launch_pass_t(Engine *e, const KArgs &a, int epi) {
   if (a.n_ap > 0) {
     // FP32X all-pairs systems (rho > L/4: small boxes) run the FP64 pass
     constexpr int PA = PREC == kPrecFP32X ? kPrecFP64 : PREC;
-    k_allpairs_pass<PA, KIND><<<std::min(a.n_ap, 152 * 16), kAllPairsThreads, 0, st>>>(a, epi);
+    k_allpairs_pass<PA, KIND><<<std::min(e->ap_items, 152 * 16), kAllPairsThreads, 0, st>>>(a, epi);
     SPC_LAUNCHED(e);
   }
   if constexpr (KIND != kKindNb && PREC != kPrecFP32X) {  // FP32X is refused with Verlet rows
@@ -890,6 +902,7 @@ inline int launch_pass(Engine *e, const KArgs &a, int kind, int epi) {
 inline int enqueue_step(Engine *e, double dt, int step_off, const double *noise) {
   KArgs a = e->a;
   a.dt = dt;
+  a.sdt = std::sqrt(dt);
   a.noise = noise;
   a.noise_m = noise_per_particle(e->stepper);
   a.step_off = step_off;

@@ -108,6 +108,7 @@ struct KArgs {
   int *list_idx;
   // stepping
   double dt;
+  double sdt;                        // sqrt(dt), rounded once on the host
   int kq_out;                        // k slot written by kEpiRkK / kEpiRk4Combine (k4)
   const double *noise;               // injected normals of this step (pool-indexed), or null
   int noise_m;                       // normals per particle
@@ -413,8 +414,8 @@ __device__ void epilogue(const KArgs &a, int epi, const SysDesc &sd, const ILane
         // StochasticEulerStepper.hpp:43-45 with AddNoise (ChimeraSystem.cpp:927-930);
         // a vortex system adds its frequency to the phase drift as the
         // SRK-Ptr stepper does (StochasticRungeKuttaStepperPtr.hpp:65)
-        const double sdt = dsqrt(dt);
-        const double sto = dmul(dsqrt(dmul(2.0, sc.D)), noise_at(a, q, 0, z0, z1));
+        const double sdt = a.sdt;
+        const double sto = dmul(sc.s2D, noise_at(a, q, 0, z0, z1));
         const double xs = dadd(a.x[q], dadd(dmul(dt, d0), dmul(sdt, 0.0)));
         const double ys = dadd(a.y[q], dadd(dmul(dt, d1), dmul(sdt, 0.0)));
         const double drift = sd.is_vortex ? dadd(a.omega[q], rate) : rate;
@@ -424,10 +425,10 @@ __device__ void epilogue(const KArgs &a, int epi, const SysDesc &sd, const ILane
       } else if (epi == kEpiEulerPtr) {
         if (!live) return;
         // StochasticEulerStepperPtr.hpp:44-51
-        const double dW = dmul(dsqrt(dt), noise_at(a, q, 0, z0, z1));
+        const double dW = dmul(a.sdt, noise_at(a, q, 0, z0, z1));
         const double xs = dadd(a.x[q], dmul(d0, dt));
         const double ys = dadd(a.y[q], dmul(d1, dt));
-        a.phi[q] = dadd(a.phi[q], dadd(dmul(rate, dt), dmul(dsqrt(dmul(2.0, sc.D)), dW)));
+        a.phi[q] = dadd(a.phi[q], dadd(dmul(rate, dt), dmul(sc.s2D, dW)));
         a.x[q] = wrap_1d(xs, sc.rL, sc.L);
         a.y[q] = wrap_1d(ys, sc.rL, sc.L);
       } else if (epi == kEpiSrk1) {
@@ -435,7 +436,7 @@ __device__ void epilogue(const KArgs &a, int epi, const SysDesc &sd, const ILane
         a.cnt_s[p] = acc.n;
       }
     } else {  // kKindCos2: SRK pass 2 (ChimeraSystem.cpp:642-643)
-      const double A0 = dmul(acc.s0, -dsqrt(dmul(2.0, sc.D)));
+      const double A0 = dmul(acc.s0, -sc.s2D);
       const double A1 = dadd(acc.s1, dmul(dmul(-2.0, sc.D), il.dphi));
       const double d2 = il.dphi;
       if (epi == kEpiSrk2Out) {
@@ -448,11 +449,11 @@ __device__ void epilogue(const KArgs &a, int epi, const SysDesc &sd, const ILane
         if (!live) return;
         // StochasticRungeKuttaStepper.hpp:44-55 (+ omega: StochasticRungeKuttaStepperPtr.hpp:65)
         const double U1 = noise_at(a, q, 0, z0, z1), U2 = noise_at(a, q, 1, z0, z1);
-        const double sdt = dsqrt(dt);
+        const double sdt = a.sdt;
         const double dW = dmul(U1, sdt);
-        const double dZ = dmul(dmul(dmul(0.5, dt), sdt), dadd(U1, ddiv(U2, dsqrt(3.0))));
+        const double dZ = dmul(dmul(dmul(0.5, dt), sdt), dadd(U1, ddiv_by(U2, kSqrt3, kRcpSqrt3)));
         const double D = sc.D;
-        const double s2D = dsqrt(dmul(2.0, D));
+        const double s2D = sc.s2D;
         const double dtdt_x = dmul(dmul(dmul(0.5, dadd(dmul(d2, d1), dmul(D, d0))), dt), dt);
         const double xs = dadd(a.x[q], dsub(dsub(dmul(d0, dt), dmul(dmul(s2D, d1), dZ)), dtdt_x));
         const double dtdt_y = dmul(dmul(dmul(0.5, dsub(dmul(d2, d0), dmul(D, d1))), dt), dt);
@@ -716,9 +717,11 @@ __global__ void __launch_bounds__(kPassThreads) k_cell_pass(KArgs a, int epi) {
   }
 }
 
-// All pairs (rho > L/4): ChimeraSystem.cpp:117-255.  One CTA per all-pairs
-// system (its particles form one cell, in index order); one thread per i,
-// j ascending, exact FP64 test on unwrapped stage positions.
+// All pairs (rho > L/4): ChimeraSystem.cpp:117-255.  An all-pairs system's
+// particles form one cell, in index order.  A work item is one block of
+// kAllPairsThreads particles of one such system, so a large system spreads
+// over many CTAs; one thread per i walks j ascending (the reference's order),
+// with the exact FP64 test on unwrapped stage positions.
 constexpr int kAllPairsThreads = 128;
 
 template <int PREC, int KIND>
@@ -726,12 +729,23 @@ __global__ void __launch_bounds__(kAllPairsThreads) k_allpairs_pass(KArgs a, int
   __shared__ double tx[kAllPairsThreads], ty[kAllPairsThreads];
   __shared__ float2 tcs[kAllPairsThreads];
   __shared__ float td[kAllPairsThreads];
-  for (int w = blockIdx.x; w < a.n_ap; w += gridDim.x) {
+  for (int item = blockIdx.x;; item += gridDim.x) {
+    // the item's system (w) and particle block (rest), uniform over the CTA
+    int w = 0, rest = item, cb = 0, ce = 0;
+    for (; w < a.n_ap; ++w) {
+      const int cw = a.ap_cells[w];
+      cb = a.cell_start[cw];
+      ce = a.cell_start[cw + 1];
+      const int nb = (ce - cb + kAllPairsThreads - 1) / kAllPairsThreads;
+      if (rest < nb) break;
+      rest -= nb;
+    }
+    if (w >= a.n_ap) break;
     const int c = a.ap_cells[w];
     const SysDesc &sd = a.sys[a.sys_of_c[c]];
     const SysConst &sc = sd.sc;
-    const int cb = a.cell_start[c], ce = a.cell_start[c + 1];
-    for (int ib = cb; ib < ce; ib += kAllPairsThreads) {
+    {
+      const int ib = cb + rest * kAllPairsThreads;
       const int i = ib + threadIdx.x;
       ILane il;
       Acc<PREC> acc;

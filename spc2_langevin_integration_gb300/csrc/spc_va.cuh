@@ -89,10 +89,10 @@ __device__ void va_epilogue(const KArgs &a, int epi, const SysDesc &sd, int p, i
       if (!live) return;
       // StochasticEulerStepperPtr.hpp:56-76
       const double rate = rate_from(0.0);
-      const double dW = dmul(dsqrt(dt), noise_at(a, q, 0, z0, z1));
+      const double dW = dmul(a.sdt, noise_at(a, q, 0, z0, z1));
       const double xs = dadd(a.x[q], dmul(d0, dt));
       const double ys = dadd(a.y[q], dmul(d1, dt));
-      a.phi[q] = dadd(a.phi[q], dadd(dmul(rate, dt), dmul(dsqrt(dmul(2.0, sc.D)), dW)));
+      a.phi[q] = dadd(a.phi[q], dadd(dmul(rate, dt), dmul(sc.s2D, dW)));
       a.x[q] = wrap_1d(xs, sc.rL, sc.L);
       a.y[q] = wrap_1d(ys, sc.rL, sc.L);
     } else if (epi == kEpiRkK || epi == kEpiRk4Combine) {
@@ -116,7 +116,7 @@ __device__ void va_epilogue(const KArgs &a, int epi, const SysDesc &sd, int p, i
     }
   } else {
     // additional_derivative[i][0] *= sqrt(2 D) (VortexArraysSystemPtr.cpp:732)
-    const double A0 = dmul(r.a0, dsqrt(dmul(2.0, sc.D)));
+    const double A0 = dmul(r.a0, sc.s2D);
     const double A1 = r.a1;
     const double d0 = a.va_vx[p], d1 = a.va_vy[p], d2 = a.dphi_s[p];
     if (epi == kEpiSrk2Out) {
@@ -129,11 +129,11 @@ __device__ void va_epilogue(const KArgs &a, int epi, const SysDesc &sd, int p, i
       if (!live) return;
       // StochasticRungeKuttaStepperPtr.hpp:70-96 (no natural frequencies)
       const double U1 = noise_at(a, q, 0, z0, z1), U2 = noise_at(a, q, 1, z0, z1);
-      const double sdt = dsqrt(dt);
+      const double sdt = a.sdt;
       const double dW = dmul(U1, sdt);
-      const double dZ = dmul(dmul(dmul(0.5, dt), sdt), dadd(U1, ddiv(U2, dsqrt(3.0))));
+      const double dZ = dmul(dmul(dmul(0.5, dt), sdt), dadd(U1, ddiv_by(U2, kSqrt3, kRcpSqrt3)));
       const double D = sc.D;
-      const double s2D = dsqrt(dmul(2.0, D));
+      const double s2D = sc.s2D;
       const double dtdt_x = dmul(dmul(dmul(0.5, dadd(dmul(d2, d1), dmul(D, d0))), dt), dt);
       const double xs = dadd(a.x[q], dsub(dsub(dmul(d0, dt), dmul(dmul(s2D, d1), dZ)), dtdt_x));
       const double dtdt_y = dmul(dmul(dmul(0.5, dsub(dmul(d2, d0), dmul(D, d1))), dt), dt);
