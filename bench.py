@@ -49,10 +49,31 @@ ALG_BYTES = {
     "pass2": 32 + 12 + 8 + 24 + 24,  # + own rate/n_i, omega, state in, state out
 }
 ALG_BYTES_STEP = 168 + 8      # survey accounting for the whole SRK step (+ omega)
-# DRAM bytes (read + write) per launch of each form's first neighbour pass
-# at this workload's initial state, from one ncu capture of that kernel
-# (`--ncu-case <form> --cell-list`).
-NCU_TRAFFIC_PASS1 = {"fp32c": 2.41e6}
+# The kernels of each phase, by form (the cell-list forms; a phase that runs
+# the cell-tile and the warp-per-cell kernels, for dense and sparse cells,
+# counts both).
+PHASE_KERNELS = {
+    "fp32c": {"stage": ["k_stage"], "sort": ["k_scan_digits", "k_radix_scatter"],
+              "gather": ["k_gather<1>"], "pass1": ["k_tile_fp32c<0>", "k_warp_fp32c<0>"],
+              "pass2": ["k_tile_fp32c<1>", "k_warp_fp32c<1>"]},
+    "fp32x": {"stage": ["k_stage"], "sort": ["k_scan_digits", "k_radix_scatter"],
+              "gather": ["k_gather<2>"],
+              "pass1": ["k_tile_fp32x<0>", "k_warp_fp32x<0>", "k_epilogue_fp32x<0>"],
+              "pass2": ["k_tile_fp32x<1>", "k_warp_fp32x<1>", "k_epilogue_fp32x<1>"]},
+    "fp64": {"stage": ["k_stage"], "sort": ["k_scan_digits", "k_radix_scatter"],
+             "gather": ["k_gather<0>", "k_vgather<0>"], "pass1": ["k_vtile<0,0>", "k_tile_fp64<0>"],
+             "pass2": ["k_vtile<0,1>", "k_tile_fp64<1>"]},
+}
+# DRAM bytes (read + write) per launch of a phase's kernels, from one ncu
+# capture (`--ncu-case <form> --cell-list --ncu-state <state>`, cold caches),
+# summed over the phase's kernels; keyed by (form, phase).  FP32C pass 2 reads
+# the pass-1 neighbour masks (~3.5 MB here) on top of its algorithmic bytes.
+NCU_TRAFFIC = {
+    ("fp32c", "pass1"): {"bytes": 2.41e6, "state": "initial; the same at the clustered state"},
+    ("fp32c", "pass2"): {"bytes": 1.007e7, "state": "clustered (step 4,000, tests/golden/states)"},
+    ("fp32x", "pass1"): {"bytes": 5.59e6, "state": "initial (k_tile_fp32x<0> + k_epilogue_fp32x<0>)"},
+    ("fp32x", "pass2"): {"bytes": 1.398e7, "state": "initial (k_tile_fp32x<1> + k_epilogue_fp32x<1>)"},
+}
 
 
 def init_inputs(w, seed_offset=0):
@@ -865,8 +886,35 @@ def run_form(abi, torch, w, precision, steps, warmup, rank, dist, params=None, s
     return ms, e2e_ms, prof, R, launches
 
 
+def candidates_per_particle(w, state):
+    """Mean candidate tests per particle of the cell-list passes on a state:
+    the members of each particle's 3x3 stencil of cells of side L / int(L / rho)."""
+    L, nc = w["L"], int(w["L"] / w["rho"])
+    cx = np.minimum((state[0::3] / L * nc).astype(np.int64), nc - 1)
+    cy = np.minimum((state[1::3] / L * nc).astype(np.int64), nc - 1)
+    occ = np.bincount(cy * nc + cx, minlength=nc * nc).reshape(nc, nc)
+    sten = sum(np.roll(np.roll(occ, dy, 0), dx, 1) for dy in (-1, 0, 1) for dx in (-1, 0, 1))
+    return float(sten[cy, cx].mean())
+
+
+def phase_sample(abi, w, params, s, state, omega, dt):
+    """Outside the timers: a per-phase CUDA-event profile of 10 steps and the
+    neighbour work (candidate tests, pairs within rho) on a copy of the current
+    state, in a second handle with the same parameters and tuning, so the
+    measured handle, its graph and its trajectory are left as they are."""
+    with abi.System(w["n"], params) as c:
+        if params.neighbour == abi.NEIGHBOUR_CELL:
+            c.set_tuning(abi.TUNE_SPARSE_BELOW, s.get_tuning(abi.TUNE_SPARSE_BELOW))
+            c.set_tuning(abi.TUNE_TILE_SPLIT, s.get_tuning(abi.TUNE_TILE_SPLIT))
+        c.upload_omega(omega)
+        c.upload_state(state)
+        pairs = float(c.neighbour_counts().mean())
+        prof = c.profile_steps(dt, 10)
+    return {"profile_ms": prof, "candidates": candidates_per_particle(w, state), "pairs": pairs}
+
+
 def run_configured(abi, torch, w, precision, params, tuning, steps, warmup, rank, dist,
-                   total_steps=None):
+                   total_steps=None, sample_phases=False):
     """The whole configured run of the workload (w["steps"] simulation steps
     from the seeded initial state, Philox counters from 0), split into `steps`
     bench steps of total_steps / steps simulation steps each (graph replays of
@@ -888,7 +936,10 @@ def run_configured(abi, torch, w, precision, params, tuning, steps, warmup, rank
     were), a Verlet-row handle by spc_autotune_ex over every method, moving
     to a new handle (state, frequencies and step counter carried over) when
     another method wins.  The step graph is captured again before the next
-    bench step (spc_prepare_graph), so no capture falls inside the timers."""
+    bench step (spc_prepare_graph), so no capture falls inside the timers.
+    sample_phases: after each bench step, also a phase profile and the
+    neighbour work on a copy of the state (phase_sample), for the roofline
+    averaged over the run."""
     import ctypes as C
     n = w["n"]
     total = total_steps or w["steps"]
@@ -919,7 +970,7 @@ def run_configured(abi, torch, w, precision, params, tuning, steps, warmup, rank
     s.step_counter = 0
     ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
           for _ in range(steps)]
-    wall, series, retunes = [], [], []
+    wall, series, retunes, samples = [], [], [], []
     tuned_at = None  # ms per simulation step when last tuned
     if dist is not None:
         dist.barrier()
@@ -938,6 +989,8 @@ def run_configured(abi, torch, w, precision, params, tuning, steps, warmup, rank
         o = s.order_params()
         series.append((per * (k + 1), o["R"], o["R_local"]))
         cost = ev[k][0].elapsed_time(ev[k][1]) / per
+        if sample_phases:
+            samples.append(phase_sample(abi, w, params, s, host, omega, dt))
         if tuned_at is None:
             tuned_at = cost
         elif abs(cost - tuned_at) > 0.25 * tuned_at and k + 1 < steps:
@@ -969,11 +1022,13 @@ def run_configured(abi, torch, w, precision, params, tuning, steps, warmup, rank
     e2e_ms = reduce_max(dist, sum(wall))
     launches = s.graph_nodes() * reps * steps
     prof = s.profile_steps(dt, 20)  # on the final (clustered) state
+    final_state = host.copy()
     del host
     L.spc_free_pinned(q)
     s.close()
     return {"ms": ms, "e2e_ms": e2e_ms, "steps_per_bench_step": per, "series": series,
-            "profile_ms": prof, "launches": launches, "retunes": retunes,
+            "profile_ms": prof, "launches": launches, "retunes": retunes, "samples": samples,
+            "final_state": final_state,
             "ms_per_bench_step": [a.elapsed_time(b) for a, b in ev]}
 
 
@@ -1010,6 +1065,14 @@ def main():
     ap.add_argument("--skin", type=float, default=None)
     ap.add_argument("--tile-split", type=int, default=None,
                     help="--form: CTAs per cell of the cell-tile passes (0: the default, 1)")
+    ap.add_argument("--save-final-states", default=None,
+                    help="headline run: write each form's state after the whole run to "
+                         "<dir>/final_state_<form>.npz")
+    ap.add_argument("--ncu-state", default="initial",
+                    help="--ncu-case fp32c/fp32x/fp64: start from the seeded initial state "
+                         "('initial'), the clustered state of tests/golden/states (4,000 FP64 "
+                         "steps, 'clustered') or a state file of --save-final-states; "
+                         "--tile-split and --sparse-below set the kernel choice")
     ap.add_argument("--cell-list", action="store_true",
                     help="--ncu-case fp32c/fp64: the cell-list passes instead of the Verlet rows")
     ap.add_argument("--workload",
@@ -1190,6 +1253,13 @@ def main():
         from spc2_langevin_integration_gb300 import abi
         w = WORKLOAD
         st, omega = init_inputs(w)
+        if args.ncu_state != "initial":
+            # "clustered": the workload after 4,000 FP64 steps
+            # (tests/golden/make_clustered.py); else a state file written by
+            # --save-final-states
+            path = (os.path.join(ROOT, "tests", "golden", "states", "vortex_clustered_n65536.npz")
+                    if args.ncu_state == "clustered" else args.ncu_state)
+            st = np.load(path)["state"].copy()
         prec = {"fp32c": abi.PRECISION_FP32C, "fp32x": abi.PRECISION_FP32X,
                 "fp64": abi.PRECISION_FP64}[args.ncu_case]
         p = abi.make_params(L=w["L"], v0=w["v0"], sigma=w["sigma"], rho=w["rho"],
@@ -1199,6 +1269,11 @@ def main():
                                        else abi.NEIGHBOUR_VERLET),
                             skin=w["skin"])
         with abi.System(w["n"], p) as s:
+            if p.neighbour == abi.NEIGHBOUR_CELL:
+                if args.sparse_below is not None:
+                    s.set_tuning(abi.TUNE_SPARSE_BELOW, args.sparse_below)
+                if args.tile_split is not None:
+                    s.set_tuning(abi.TUNE_TILE_SPLIT, args.tile_split)
             s.upload_state(st)
             s.upload_omega(omega)
             s.step(w["dt"], 3)
@@ -1266,8 +1341,13 @@ def main():
         for name, prec in forms:
             best, tun, _ = tuned[name]
             runs[name] = run_configured(abi, torch, w, prec, best, tun, args.steps, args.warmup,
-                                        rank, dist)
+                                        rank, dist, sample_phases=True)
     total = runs["fp64"]["steps_per_bench_step"] * args.steps  # 10^4 when K divides it
+    if args.save_final_states and rank == 0:
+        os.makedirs(args.save_final_states, exist_ok=True)
+        for name in runs:
+            np.savez(os.path.join(args.save_final_states, f"final_state_{name}.npz"),
+                     state=runs[name]["final_state"], omega=init_inputs(w)[1])
     per_form = {}
     for name, _ in forms:
         r = runs[name]
@@ -1297,15 +1377,20 @@ def main():
                                 dist, best, tun["sparse_below"], e2e=False,
                                 tile_split=tun["tile_split"])
     hbm, peak_kind = peaks()
-    prof = hr["profile_ms"]
-    phases = {k: prof[k] for k in ("stage", "sort", "gather", "pass1", "pass2")}
+    # per-phase launch durations averaged over the run: a CUDA-event profile
+    # after each bench step (on a copy of the state, outside the timers)
+    smp = hr["samples"]
+    phases = {k: float(np.mean([x["profile_ms"][k] for x in smp]))
+              for k in ("stage", "sort", "gather", "pass1", "pass2")}
     dom = max(phases, key=phases.get)
     achieved = ALG_BYTES[dom] * w["n"] / (phases[dom] * 1e-3) / 1e9
-    # compute-side work of one neighbour pass at the initial density: candidate
-    # tests (3x3 cells of side L / int(L / rho)) and pair terms (within rho)
-    dens = w["n"] / w["L"] ** 2
-    cell = w["L"] / int(w["L"] / w["rho"])
-    cand, pairs = 9 * dens * cell ** 2, np.pi * w["rho"] ** 2 * dens
+    # compute-side work of one neighbour pass over the run: candidate tests
+    # (3x3 cells of side L / int(L / rho)) and pairs within rho per particle,
+    # from the same sampled states
+    cand = float(np.mean([x["candidates"] for x in smp]))
+    pairs = float(np.mean([x["pairs"] for x in smp]))
+    p1 = sum(x["profile_ms"]["pass1"] for x in smp) * 1e-3
+    traffic = NCU_TRAFFIC.get((head, dom))
     dtypes = {"fp32x": "f32x (f32 pair tests; exact i64 fixed-point neighbour sums; f64 "
                        "per-particle rates, noise, positions, phase)",
               "fp32c": "f32c (f32 sums/trig/increments; f64 cutoff, positions, phase)",
@@ -1328,16 +1413,21 @@ def main():
         "fp32c_over_fp64": per_form["fp32c"]["value"] / per_form["fp64"]["value"],
         "value_warm_window": n_total * SIM_STEPS_PER_BENCH_STEP * args.steps / (ms_w / 1e3),
         "gpu_launches": hr["launches"],
-        "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm,
+        "roofline": {"bound": "hbm", "kernel": dom, "kernels": PHASE_KERNELS[head][dom],
+                     "achieved": achieved, "peak": hbm,
                      "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / hbm,
-                     "traffic": NCU_TRAFFIC_PASS1.get(head) if dom == "pass1" else None,
+                     "traffic": traffic["bytes"] if traffic else None,
+                     "traffic_state": traffic["state"] if traffic else None,
                      "alg_bytes_per_particle": ALG_BYTES[dom],
                      "alg_bytes_per_launch": ALG_BYTES[dom] * w["n"],
-                     "timing": "live CUDA-event profile of 20 steps on the run's final state",
-                     "compute": {"candidate_tests_per_s": w["n"] * cand / (phases["pass1"] * 1e-3),
-                                 "pair_terms_per_s": w["n"] * pairs / (phases["pass1"] * 1e-3),
-                                 "candidates_per_particle_initial": cand,
-                                 "pairs_per_particle_initial": pairs},
+                     "phase_ms_run_mean": phases,
+                     "timing": "live CUDA-event profile of 10 steps after each of the %d bench "
+                               "steps (on a copy of the state, outside the timers), averaged "
+                               "over the run" % len(smp),
+                     "compute": {"candidate_tests_per_s": w["n"] * cand * len(smp) / p1,
+                                 "pair_terms_per_s": w["n"] * pairs * len(smp) / p1,
+                                 "candidates_per_particle_run_mean": cand,
+                                 "pairs_per_particle_run_mean": pairs},
                      "note": "the neighbour passes are bound by instruction issue and latency "
                              "on an L2-resident working set, not by HBM: the HBM fraction is "
                              "low by construction"},

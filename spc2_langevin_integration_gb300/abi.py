@@ -375,6 +375,13 @@ class System:
         self._check(self._L.spc_rhs_srk(self.h, _ptr(d), _ptr(a)), self.h)
         return d, a
 
+    def neighbour_counts(self) -> np.ndarray:
+        """n_i of every particle (in the order of the state), without the lists."""
+        counts = np.empty(self.n, np.int32)
+        total = C.c_int64()
+        self._check(self._L.spc_neighbours(self.h, _ptr(counts), None, 0, C.byref(total)), self.h)
+        return counts
+
     def neighbours(self):
         counts = np.empty(self.n, np.int32)
         total = C.c_int64()

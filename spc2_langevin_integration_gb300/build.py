@@ -29,6 +29,7 @@ def nvcc() -> str:
 def sources() -> list[str]:
     return sorted(glob.glob(os.path.join(PKG, "csrc", "*.cu")) +
                   glob.glob(os.path.join(PKG, "csrc", "*.cuh")) +
+                  glob.glob(os.path.join(PKG, "csrc", "*.h")) +
                   [os.path.join(ROOT, "include", "spc_gb300.h")])
 
 

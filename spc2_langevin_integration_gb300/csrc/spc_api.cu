@@ -1291,6 +1291,7 @@ extern "C" int spc_rhs_srk_noalloc(const spc_params *p, int32_t n, const double 
   e.ncell_warp = 0;
   a.n_ap = sc.allpairs ? 1 : 0;
   e.ap_items = sc.allpairs ? (n + kAllPairsThreads - 1) / kAllPairsThreads : 0;
+  e.ap_items_small = sc.allpairs ? (n + kAllPairsThreadsSmall - 1) / kAllPairsThreadsSmall : 0;
   a.hist_len = (1 << e.radix_bits) * e.ntiles;
   SysHost h;
   h.used = true;

@@ -8,6 +8,8 @@
 #include <cstdint>
 #include <cuda_runtime.h>
 
+#include "spc_fixed.h"
+
 namespace spc {
 
 constexpr int kWarp = 32;
@@ -44,12 +46,12 @@ __device__ __forceinline__ double dsqrt(double a) { return __dsqrt_rn(a); }
 // 2^62 in magnitude, so the integer sums are exact, and the conversion back
 // (one rounding to double) is the only error of a round's sum.
 constexpr int kXQ = 52;
+// v 2^q is exact (a power-of-two scaling of a normal result), then rounded
+// to the nearest integer
 __device__ __forceinline__ long long to_fixed(double v, int q) {
-  return __double2ll_rn(scalbn(v, q));
+  return __double2ll_rn(__dmul_rn(v, pow2i(q)));
 }
-__device__ __forceinline__ double from_fixed(long long v, int q) {
-  return scalbn(__ll2double_rn(v), -q);
-}
+__device__ __forceinline__ double from_fixed(long long v, int q) { return fixed_to_double(v, q); }
 // A particle's whole sum over several staging rounds is kept in 128 bits, so
 // it is one exact integer whatever the kernel's round size, and converted to
 // double once: one rounding when it fits 64 bits (always below 2^11
@@ -57,10 +59,31 @@ __device__ __forceinline__ double from_fixed(long long v, int q) {
 // depends on the integer alone.
 __device__ __forceinline__ double from_fixed128(__int128 v, int q) {
   const long long lo64 = (long long)v;
-  if ((__int128)lo64 == v) return scalbn(__ll2double_rn(lo64), -q);
+  if ((__int128)lo64 == v) return fixed_to_double(lo64, q);
   const long long hi = (long long)(v >> 64);
   const unsigned long long lo = (unsigned long long)v;
-  return scalbn(__fma_rn(__ll2double_rn(hi), 18446744073709551616.0, __ull2double_rn(lo)), -q);
+  return __dmul_rn(__fma_rn(__ll2double_rn(hi), 18446744073709551616.0, __ull2double_rn(lo)), pow2i(-q));
+}
+// c += v.x, s += v.y when p: predicated 64-bit adds, so a candidate loop whose
+// lanes disagree on p runs straight through instead of branching around the
+// adds of each candidate
+__device__ __forceinline__ void add2_if(long long &c, long long &s, longlong2 v, bool p) {
+  asm("{\n\t.reg .pred q;\n\tsetp.ne.b32 q, %4, 0;\n\t@q add.s64 %0, %0, %2;\n\t@q add.s64 %1, %1, %3;\n\t}"
+      : "+l"(c), "+l"(s)
+      : "l"(v.x), "l"(v.y), "r"((int)p));
+}
+// the same for float sums: c += x, s += y when p (each rounded to nearest,
+// as the plain adds)
+__device__ __forceinline__ void addf2_if(float &c, float &s, float x, float y, bool p) {
+  asm("{\n\t.reg .pred q;\n\tsetp.ne.b32 q, %4, 0;\n\t@q add.rn.f32 %0, %0, %2;\n\t@q add.rn.f32 %1, %1, %3;\n\t}"
+      : "+f"(c), "+f"(s)
+      : "f"(x), "f"(y), "r"((int)p));
+}
+// c = fma(d, x, c), s = fma(d, y, s) when p
+__device__ __forceinline__ void fmaf2_if(float &c, float &s, float d, float x, float y, bool p) {
+  asm("{\n\t.reg .pred q;\n\tsetp.ne.b32 q, %5, 0;\n\t@q fma.rn.f32 %0, %2, %3, %0;\n\t@q fma.rn.f32 %1, %2, %4, %1;\n\t}"
+      : "+f"(c), "+f"(s)
+      : "f"(d), "f"(x), "f"(y), "r"((int)p));
 }
 
 // Per-system constants, the reference's ChimeraSystem / PeriodicBoundaryConditions

@@ -188,8 +188,10 @@ struct Engine {
   int *d_ap = nullptr;      // cells of the all-pairs systems the all-pairs kernel integrates
   int *d_ap_all = nullptr;  // ... and of every all-pairs system (diagnostics)
   int n_ap_all = 0;
-  // particle blocks (work items of k_allpairs_pass) of those systems
+  // particle blocks (work items of k_allpairs_pass) of those systems, in
+  // blocks of kAllPairsThreads and of kAllPairsThreadsSmall particles
   int ap_items = 0, ap_items_all = 0;
+  int ap_items_small = 0, ap_items_all_small = 0;
   unsigned long long *d_clamped = nullptr;
   uint32_t *keys_alt = nullptr, *vals_alt = nullptr, *hist = nullptr, *part = nullptr;
   double *aos = nullptr;  // AoS staging (12 x pool_cap doubles)
@@ -640,7 +642,7 @@ inline std::vector<long long> launch_shape(const Engine *e) {
   const KArgs &a = e->a;
   return {e->nsys, e->n_active, e->ncell_total, e->ntiles, e->radix_bits, e->sort_passes, e->ncell_tile,
           e->ncell_warp, e->ncell_va, e->n_ap_all, e->has_cells, a.n_ap, a.tile_split, a.hist_len,
-          e->ap_items, e->ap_items_all};
+          e->ap_items, e->ap_items_all, e->ap_items_small, e->ap_items_all_small};
 }
 
 inline int engine_layout(Engine *e) {
@@ -655,6 +657,7 @@ inline int engine_layout(Engine *e) {
   // systems, so that each neighbour kernel covers one contiguous range of cells
   int ncell_tile = 0, ncell_warp = 0, ncell_va = 0;
   e->ap_items = e->ap_items_all = 0;
+  e->ap_items_small = e->ap_items_all_small = 0;
   for (int cls = 0; cls < 4; ++cls) {
     for (int slot : e->order) {
       const SysHost &h = e->slots[slot];
@@ -662,13 +665,16 @@ inline int engine_layout(Engine *e) {
       e->slot_layout[slot] = (int)table.size();
       table.push_back(desc_of(h, dense, cells));
       const int blocks = (h.n + kAllPairsThreads - 1) / kAllPairsThreads;
+      const int blocks_small = (h.n + kAllPairsThreadsSmall - 1) / kAllPairsThreadsSmall;
       if (cls == 3) {
         ap.push_back(cells);
         e->ap_items += blocks;
+        e->ap_items_small += blocks_small;
       }
       if (h.sc.allpairs) {
         ap_all.push_back(cells);
         e->ap_items_all += blocks;
+        e->ap_items_all_small += blocks_small;
       }
       dense += h.n;
       cells += h.ncell;
@@ -811,6 +817,17 @@ inline int eval_cells(Engine *e, KArgs &a, int rk_form, int kq, double kcdt, boo
   return SPC_OK;
 }
 
+// The all-pairs kernel at 128 threads per CTA when its systems give at least
+// two blocks per SM, else at one warp per CTA.
+template <int PREC, int KIND>
+void launch_allpairs(const KArgs &a, int epi, int items, int items_small, cudaStream_t st) {
+  if (items >= 2 * 152)
+    k_allpairs_pass<PREC, KIND, kAllPairsThreads><<<std::min(items, 152 * 16), kAllPairsThreads, 0, st>>>(a, epi);
+  else
+    k_allpairs_pass<PREC, KIND, kAllPairsThreadsSmall>
+        <<<std::min(items_small, 152 * 32), kAllPairsThreadsSmall, 0, st>>>(a, epi);
+}
+
 template <int PREC, int KIND>
 int launch_pass_t(Engine *e, const KArgs &a, int epi) {
   cudaStream_t st = e->stream;
@@ -821,7 +838,7 @@ int launch_pass_t(Engine *e, const KArgs &a, int epi) {
     b.ap_cells = e->d_ap_all;
     b.n_ap = e->n_ap_all;
     if (b.n_ap > 0) {
-      k_allpairs_pass<PREC, KIND><<<std::min(e->ap_items_all, 152 * 16), kAllPairsThreads, 0, st>>>(b, epi);
+      launch_allpairs<PREC, KIND>(b, epi, e->ap_items_all, e->ap_items_all_small, st);
       SPC_LAUNCHED(e);
     }
     if (e->ncell_total > e->n_ap_all) {
@@ -834,7 +851,7 @@ int launch_pass_t(Engine *e, const KArgs &a, int epi) {
   if (a.n_ap > 0) {
     // FP32X all-pairs systems (rho > L/4: small boxes) run the FP64 pass
     constexpr int PA = PREC == kPrecFP32X ? kPrecFP64 : PREC;
-    k_allpairs_pass<PA, KIND><<<std::min(e->ap_items, 152 * 16), kAllPairsThreads, 0, st>>>(a, epi);
+    launch_allpairs<PA, KIND>(a, epi, e->ap_items, e->ap_items_small, st);
     SPC_LAUNCHED(e);
   }
   if constexpr (KIND != kKindNb && PREC != kPrecFP32X) {  // FP32X is refused with Verlet rows

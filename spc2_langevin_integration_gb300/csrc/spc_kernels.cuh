@@ -718,17 +718,21 @@ __global__ void __launch_bounds__(kPassThreads) k_cell_pass(KArgs a, int epi) {
 }
 
 // All pairs (rho > L/4): ChimeraSystem.cpp:117-255.  An all-pairs system's
-// particles form one cell, in index order.  A work item is one block of
-// kAllPairsThreads particles of one such system, so a large system spreads
-// over many CTAs; one thread per i walks j ascending (the reference's order),
-// with the exact FP64 test on unwrapped stage positions.
+// particles form one cell, in index order.  A work item is one block of T
+// particles of one such system, so a large system spreads over many CTAs;
+// one thread per i walks j ascending (the reference's order), with the exact
+// FP64 test on unwrapped stage positions.  T is the CTA width: 128, or 32
+// (one warp per CTA, four times the CTAs) when the all-pairs systems hold too
+// few particles to give every SM work at 128 (each thread's sums are the
+// same either way).
 constexpr int kAllPairsThreads = 128;
+constexpr int kAllPairsThreadsSmall = 32;
 
-template <int PREC, int KIND>
-__global__ void __launch_bounds__(kAllPairsThreads) k_allpairs_pass(KArgs a, int epi) {
-  __shared__ double tx[kAllPairsThreads], ty[kAllPairsThreads];
-  __shared__ float2 tcs[kAllPairsThreads];
-  __shared__ float td[kAllPairsThreads];
+template <int PREC, int KIND, int T = kAllPairsThreads>
+__global__ void __launch_bounds__(T) k_allpairs_pass(KArgs a, int epi) {
+  __shared__ double tx[T], ty[T];
+  __shared__ float2 tcs[T];
+  __shared__ float td[T];
   for (int item = blockIdx.x;; item += gridDim.x) {
     // the item's system (w) and particle block (rest), uniform over the CTA
     int w = 0, rest = item, cb = 0, ce = 0;
@@ -736,7 +740,7 @@ __global__ void __launch_bounds__(kAllPairsThreads) k_allpairs_pass(KArgs a, int
       const int cw = a.ap_cells[w];
       cb = a.cell_start[cw];
       ce = a.cell_start[cw + 1];
-      const int nb = (ce - cb + kAllPairsThreads - 1) / kAllPairsThreads;
+      const int nb = (ce - cb + T - 1) / T;
       if (rest < nb) break;
       rest -= nb;
     }
@@ -745,14 +749,14 @@ __global__ void __launch_bounds__(kAllPairsThreads) k_allpairs_pass(KArgs a, int
     const SysDesc &sd = a.sys[a.sys_of_c[c]];
     const SysConst &sc = sd.sc;
     {
-      const int ib = cb + rest * kAllPairsThreads;
+      const int ib = cb + rest * T;
       const int i = ib + threadIdx.x;
       ILane il;
       Acc<PREC> acc;
       load_i<PREC, KIND>(a, sc, il, i, i < ce);
       acc.init();
       long long wpos = (a.list_idx && il.valid) ? a.list_off[a.pidx[i]] : 0;
-      for (int jt = cb; jt < ce; jt += kAllPairsThreads) {
+      for (int jt = cb; jt < ce; jt += T) {
         const int jl = jt + threadIdx.x;
         __syncthreads();
         if (jl < ce) {
@@ -764,7 +768,7 @@ __global__ void __launch_bounds__(kAllPairsThreads) k_allpairs_pass(KArgs a, int
           }
         }
         __syncthreads();
-        const int cnt = min(kAllPairsThreads, ce - jt);
+        const int cnt = min(T, ce - jt);
         if (!il.valid) continue;
         for (int t = 0; t < cnt; ++t) {
           const int j = jt + t;

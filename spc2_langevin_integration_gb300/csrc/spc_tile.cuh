@@ -152,16 +152,9 @@ __device__ __forceinline__ void block32(const float4 *__restrict__ s_c4, const f
       off = (j0 + t != self) ? off : 3.0e38f;
     }
     mn = fminf(mn, fabsf(off));
-    if (in) {
-      sc_ += cj.z;
-      ss_ += cj.w;
-      if constexpr (KIND == kKindCos2) {
-        const float dj = s_d[j0 + t];
-        sdc = fmaf(dj, cj.z, sdc);
-        sds = fmaf(dj, cj.w, sds);
-      }
-      bits |= 1u << t;
-    }
+    addf2_if(sc_, ss_, cj.z, cj.w, in);
+    if constexpr (KIND == kKindCos2) fmaf2_if(sdc, sds, s_d[j0 + t], cj.z, cj.w, in);
+    bits |= (uint32_t)in << t;
   }
 }
 
@@ -409,12 +402,8 @@ __device__ __forceinline__ void block32x(const float2 *__restrict__ s_xy, const 
       off = (j0 + t != self) ? off : 3.0e38f;
     }
     mn = fminf(mn, fabsf(off));
-    if (in) {
-      const longlong2 v = s_v[j0 + t];
-      C += v.x;
-      S += v.y;
-      bits |= 1u << t;
-    }
+    add2_if(C, S, s_v[j0 + t], in);
+    bits |= (uint32_t)in << t;
   }
 }
 

@@ -322,12 +322,8 @@ __global__ void __launch_bounds__(kWarpPassThreads, 8) k_warp_fp32x(KArgs a, int
                 in = exact_within(sc, a.sx[pp], a.sy[pp], a.sx[pj], a.sy[pj]);
               }
               in = in && j != self;
-              if (in) {
-                bits |= 1u << (k & (kWarp - 1));
-                const longlong2 v = sm.v[j];
-                pc += v.x;
-                ps += v.y;
-              }
+              bits |= (uint32_t)in << (k & (kWarp - 1));
+              add2_if(pc, ps, sm.v[j], in);
               if ((k & (kWarp - 1)) == kWarp - 1 || j + G >= rcnt) {
                 pn += __popc(bits);
                 if (KIND == kKindSin && masked) a.nbmask[mask_at(g * W + k / kWarp, pp, n_all)] = bits;
