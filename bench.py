@@ -628,8 +628,7 @@ def run_large(precision, steps):
     best, tun = abi.params_with(p, cands[k]), cands[k]
     with abi.System(n, best) as s:
         if best.neighbour == abi.NEIGHBOUR_CELL:
-            s.set_tuning(abi.TUNE_SPARSE_BELOW, tun["sparse_below"])
-            s.set_tuning(abi.TUNE_TILE_SPLIT, tun["tile_split"])
+            apply_tuning(abi, s, tun)
         s.upload_state(st)
         stream = torch.cuda.ExternalStream(s.stream)
         s.step(w["dt"], steps, graph=True)  # capture + warm
@@ -812,7 +811,7 @@ def tune_form(abi, w, precision, rank=0):
 
 
 def run_form(abi, torch, w, precision, steps, warmup, rank, dist, params=None, sparse_below=None,
-             e2e=True, tile_split=None):
+             e2e=True, tile_split=None, heavy_units=None):
     """Device-timed graph replays of the workload; then (e2e) the same through
     the C-ABI with host buffers, and a per-phase profile.
 
@@ -830,6 +829,8 @@ def run_form(abi, torch, w, precision, steps, warmup, rank, dist, params=None, s
         s.set_tuning(abi.TUNE_SPARSE_BELOW, sparse_below)
     if tile_split is not None:
         s.set_tuning(abi.TUNE_TILE_SPLIT, tile_split)
+    if heavy_units is not None:
+        s.set_tuning(abi.TUNE_HEAVY_UNITS, heavy_units)
     s.upload_state(st)
     s.upload_omega(omega)
     stream = torch.cuda.ExternalStream(s.stream)
@@ -897,6 +898,13 @@ def candidates_per_particle(w, state):
     return float(sten[cy, cx].mean())
 
 
+def apply_tuning(abi, s, tun):
+    """Set a cell-list handle's kernel choice from a tuning candidate."""
+    s.set_tuning(abi.TUNE_SPARSE_BELOW, tun["sparse_below"])
+    s.set_tuning(abi.TUNE_TILE_SPLIT, tun["tile_split"])
+    s.set_tuning(abi.TUNE_HEAVY_UNITS, tun.get("heavy_units", 0))
+
+
 def phase_sample(abi, w, params, s, state, omega, dt):
     """Outside the timers: a per-phase CUDA-event profile of 10 steps and the
     neighbour work (candidate tests, pairs within rho) on a copy of the current
@@ -904,8 +912,8 @@ def phase_sample(abi, w, params, s, state, omega, dt):
     measured handle, its graph and its trajectory are left as they are."""
     with abi.System(w["n"], params) as c:
         if params.neighbour == abi.NEIGHBOUR_CELL:
-            c.set_tuning(abi.TUNE_SPARSE_BELOW, s.get_tuning(abi.TUNE_SPARSE_BELOW))
-            c.set_tuning(abi.TUNE_TILE_SPLIT, s.get_tuning(abi.TUNE_TILE_SPLIT))
+            for key in (abi.TUNE_SPARSE_BELOW, abi.TUNE_TILE_SPLIT, abi.TUNE_HEAVY_UNITS):
+                c.set_tuning(key, s.get_tuning(key))
         c.upload_omega(omega)
         c.upload_state(state)
         pairs = float(c.neighbour_counts().mean())
@@ -950,8 +958,7 @@ def run_configured(abi, torch, w, precision, params, tuning, steps, warmup, rank
     st, omega = init_inputs(w, seed_offset=rank)
     s = abi.System(n, params)
     if params.neighbour == abi.NEIGHBOUR_CELL:
-        s.set_tuning(abi.TUNE_SPARSE_BELOW, tuning["sparse_below"])
-        s.set_tuning(abi.TUNE_TILE_SPLIT, tuning["tile_split"])
+        apply_tuning(abi, s, tuning)
     s.upload_omega(omega)
     stream = torch.cuda.ExternalStream(s.stream)
     flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
@@ -1006,8 +1013,7 @@ def run_configured(abi, torch, w, precision, params, tuning, steps, warmup, rank
                     params = abi.params_with(params, choice)
                     s = abi.System(n, params)
                     if params.neighbour == abi.NEIGHBOUR_CELL:
-                        s.set_tuning(abi.TUNE_SPARSE_BELOW, choice["sparse_below"])
-                        s.set_tuning(abi.TUNE_TILE_SPLIT, choice["tile_split"])
+                        apply_tuning(abi, s, choice)
                     s.upload_omega(omega)
                     s.upload_state(host)
                     s.step_counter = ctr
@@ -1065,6 +1071,9 @@ def main():
     ap.add_argument("--skin", type=float, default=None)
     ap.add_argument("--tile-split", type=int, default=None,
                     help="--form: CTAs per cell of the cell-tile passes (0: the default, 1)")
+    ap.add_argument("--heavy-units", type=int, choices=[0, 1], default=None,
+                    help="--form / --ncu-case (FP32C, FP32X): run heavy cells as units in a second "
+                         "launch of each pass (SPC_TUNE_HEAVY_UNITS)")
     ap.add_argument("--save-final-states", default=None,
                     help="headline run: write each form's state after the whole run to "
                          "<dir>/final_state_<form>.npz")
@@ -1274,6 +1283,8 @@ def main():
                     s.set_tuning(abi.TUNE_SPARSE_BELOW, args.sparse_below)
                 if args.tile_split is not None:
                     s.set_tuning(abi.TUNE_TILE_SPLIT, args.tile_split)
+                if args.heavy_units is not None:
+                    s.set_tuning(abi.TUNE_HEAVY_UNITS, args.heavy_units)
             s.upload_state(st)
             s.upload_omega(omega)
             s.step(w["dt"], 3)
@@ -1325,7 +1336,8 @@ def main():
         if args.skin is not None:
             p.skin = args.skin
         ms, e2e_ms, prof, _, launches = run_form(abi, torch, w, prec, args.steps, args.warmup,
-                                                 rank, dist, p, tile_split=args.tile_split)
+                                                 rank, dist, p, tile_split=args.tile_split,
+                                                 heavy_units=args.heavy_units)
         if rank == 0:
             print(json.dumps({"form": args.form, "neighbour": args.neighbour, "skin": p.skin,
                               "tile_split": args.tile_split,
@@ -1375,7 +1387,7 @@ def main():
     best, tun, _ = tuned[head]
     ms_w, _, _, _, _ = run_form(abi, torch, w, dict(forms)[head], args.steps, args.warmup, rank,
                                 dist, best, tun["sparse_below"], e2e=False,
-                                tile_split=tun["tile_split"])
+                                tile_split=tun["tile_split"], heavy_units=tun["heavy_units"])
     hbm, peak_kind = peaks()
     # per-phase launch durations averaged over the run: a CUDA-event profile
     # after each bench step (on a copy of the state, outside the timers)

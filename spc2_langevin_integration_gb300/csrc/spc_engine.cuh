@@ -212,6 +212,11 @@ struct Engine {
   double sparse_below = kSparseBelowDefault;
   // tuning: CTAs per cell of the cell-tile kernels (0: chosen per layout)
   int tile_split_tune = 0;
+  // tuning: heavy cells of the float cell-tile passes run as units (1) or as
+  // whole groups (0)
+  int heavy_units_tune = 0;
+  // the heavy-unit buffers (float forms; allocated at init)
+  int2 *units_buf = nullptr;
   std::vector<int> slot_layout;  // slot -> layout index (-1 if inactive)
   // noise injection (single-system handles)
   double *d_noise = nullptr;
@@ -315,10 +320,13 @@ inline void engine_footprint(int stepper, int precision, long long *per_particle
   if (precision == SPC_PRECISION_FP32C) b += 8 + 4 + (long long)kMaskWords * 4;  // cs, dphi_f, masks
   if (precision == SPC_PRECISION_FP32X)
     b += 16 + 16 + 8 + 16 + 4 + (long long)kMaskWords * 4;  // ics, iws, scos, xsum, xcnt, masks
+  if (precision != SPC_PRECISION_FP64)  // heavy units: round sums, counts, chunk counters, list
+    b += kSplitRounds * ((precision == SPC_PRECISION_FP32X ? 16 : 8) + 4) + 4 + kSplitRounds * 8 / 32;
   if (precision == SPC_PRECISION_FP64) b += 8 + 8 + 4;                          // vortex-arrays outputs
   b += 12 * 8 + 4 + 4;                       // AoS staging, histogram share
   *per_particle = b;
-  *per_cell = 4 + 4;                         // cell_start, sys_of_c
+  *per_cell = 4 + 4 + (precision != SPC_PRECISION_FP64 ? kSplitRounds * 8 + 1 : 0);  // cell_start,
+                                                                      // sys_of_c, heavy-unit list and flag
 }
 
 inline int engine_init(Engine *e, int stepper, int precision, int pool_cap, int sys_cap, int cell_cap) {
@@ -371,6 +379,7 @@ inline int engine_init(Engine *e, int stepper, int precision, int pool_cap, int 
     SPC_TRY(dalloc(e, &a.cs, N));
     SPC_TRY(dalloc(e, &a.dphi_f, N));
     SPC_TRY(dalloc(e, &a.nbmask, (size_t)kMaskWords * N));
+    SPC_TRY(dalloc(e, &a.part_f, (size_t)kSplitRounds * N));
   }
   if (precision == SPC_PRECISION_FP32X) {
     SPC_TRY(dalloc(e, &a.ics, N));
@@ -379,6 +388,16 @@ inline int engine_init(Engine *e, int stepper, int precision, int pool_cap, int 
     SPC_TRY(dalloc(e, &a.xsum, N));
     SPC_TRY(dalloc(e, &a.xcnt, N));
     SPC_TRY(dalloc(e, &a.nbmask, (size_t)kMaskWords * N));
+    SPC_TRY(dalloc(e, &a.part_x, (size_t)kSplitRounds * N));
+  }
+  if (precision != SPC_PRECISION_FP64) {
+    // a heavy cell of n_c particles lists ceil(n_c / 32) x (at most
+    // kSplitRounds) units, so (N / 32 + cells) x kSplitRounds entries hold any layout
+    SPC_TRY(dalloc(e, &e->units_buf, ((N + kWarp - 1) / kWarp + (size_t)cell_cap) * kSplitRounds));
+    SPC_TRY(dalloc(e, &a.unit_count, 1));
+    SPC_TRY(dalloc(e, &a.cell_heavy, (size_t)cell_cap));
+    SPC_TRY(dalloc(e, &a.part_n, (size_t)kSplitRounds * N));
+    SPC_TRY(dalloc(e, &a.unit_done, N));
   }
   SPC_TRY(dalloc(e, &a.cell_start, (size_t)cell_cap + 1));
   SPC_TRY(dalloc(e, &sys_of_c, (size_t)cell_cap));
@@ -401,6 +420,10 @@ inline int engine_init(Engine *e, int stepper, int precision, int pool_cap, int 
   SPC_CUDA(e, cudaMemsetAsync(omega, 0, N * 8, st));
   SPC_CUDA(e, cudaMemsetAsync(e->hist, 0, (size_t)(1 << 11) * e->tile_cap * 4, st));
   SPC_CUDA(e, cudaMemsetAsync(e->d_clamped, 0, 8, st));
+  if (a.unit_done) {
+    SPC_CUDA(e, cudaMemsetAsync(a.unit_done, 0, N * 4, st));
+    SPC_CUDA(e, cudaMemsetAsync(a.unit_count, 0, 4, st));
+  }
   if (stepper == SPC_STEPPER_RK4)
     for (int q = 0; q < 4; ++q) {
       SPC_CUDA(e, cudaMemsetAsync(a.kx[q], 0, N * 8, st));
@@ -642,7 +665,7 @@ inline std::vector<long long> launch_shape(const Engine *e) {
   const KArgs &a = e->a;
   return {e->nsys, e->n_active, e->ncell_total, e->ntiles, e->radix_bits, e->sort_passes, e->ncell_tile,
           e->ncell_warp, e->ncell_va, e->n_ap_all, e->has_cells, a.n_ap, a.tile_split, a.hist_len,
-          e->ap_items, e->ap_items_all, e->ap_items_small, e->ap_items_all_small};
+          e->ap_items, e->ap_items_all, e->ap_items_small, e->ap_items_all_small, a.units != nullptr};
 }
 
 inline int engine_layout(Engine *e) {
@@ -702,6 +725,7 @@ inline int engine_layout(Engine *e) {
   a.ncell_total = e->ncell_total;
   a.ncell_tile = e->ncell_tile;
   a.tile_split = tile_split_for(e->tile_split_tune);
+  a.units = e->heavy_units_tune ? e->units_buf : nullptr;
   a.va_c0 = e->ncell_tile + e->ncell_warp;
   a.va_c1 = a.va_c0 + e->ncell_va;
   a.n_ap = (int)ap.size();
@@ -813,6 +837,13 @@ inline int eval_cells(Engine *e, KArgs &a, int rk_form, int kq, double kcdt, boo
   else
     k_gather<kPrecFP64><<<blocks_for(n + 1, 256), 256, 0, st>>>(a);
   SPC_LAUNCHED(e);
+  if (a.units && e->ncell_tile > 0 && !e->verlet) {  // the heavy cells' units of this evaluation
+    if (e->precision == SPC_PRECISION_FP32C)
+      k_list_units<kTileCap><<<blocks_for(e->ncell_tile, 128), 128, 0, st>>>(a);
+    else
+      k_list_units<kTileCapX><<<blocks_for(e->ncell_tile, 128), 128, 0, st>>>(a);
+    SPC_LAUNCHED(e);
+  }
   if (marks) mark(e, 3);
   return SPC_OK;
 }
@@ -871,13 +902,28 @@ int launch_pass_t(Engine *e, const KArgs &a, int epi) {
     {
       if (e->ncell_tile > 0) {
         const int grid = std::min(e->ncell_tile * std::max(a.tile_split, 1), 152 * 256);
-        if constexpr (PREC == kPrecFP32C)
-          k_tile_fp32c<KIND><<<grid, kTileThreads32, 0, st>>>(a, epi);
-        else if constexpr (PREC == kPrecFP32X)
-          k_tile_fp32x<KIND><<<grid, kTileThreads32, 0, st>>>(a, epi);
-        else
+        if constexpr (PREC == kPrecFP32C) {
+          if (a.units)
+            k_tile_fp32c<KIND, true><<<grid, kTileThreads32, 0, st>>>(a, epi);
+          else
+            k_tile_fp32c<KIND, false><<<grid, kTileThreads32, 0, st>>>(a, epi);
+        } else if constexpr (PREC == kPrecFP32X) {
+          if (a.units)
+            k_tile_fp32x<KIND, true><<<grid, kTileThreads32, 0, st>>>(a, epi);
+          else
+            k_tile_fp32x<KIND, false><<<grid, kTileThreads32, 0, st>>>(a, epi);
+        } else
           k_tile_fp64<KIND><<<grid, kTileThreads64, 0, st>>>(a, epi);
         SPC_LAUNCHED(e);
+        if constexpr ((PREC == kPrecFP32C || PREC == kPrecFP32X) && KIND != kKindNb) {
+          if (a.units) {  // the heavy cells' units the cell-tile kernel listed
+            if constexpr (PREC == kPrecFP32C)
+              k_units_fp32c<KIND><<<152 * kTileMinBlocks32, kTileThreads32, 0, st>>>(a, epi);
+            else
+              k_units_fp32x<KIND><<<152 * kTileMinBlocks32, kTileThreads32, 0, st>>>(a, epi);
+            SPC_LAUNCHED(e);
+          }
+        }
       }
       if (e->ncell_warp > 0) {
         const int grid = std::min(blocks_for(e->ncell_warp, kWarpPassWarps), 152 * 64);
@@ -1045,6 +1091,16 @@ inline int engine_set_tuning(Engine *e, int key, double value) {
     drop_graph(e);
     return SPC_OK;
   }
+  if (key == SPC_TUNE_HEAVY_UNITS) {
+    if (value != 0.0 && value != 1.0) return fail(e, SPC_ERR_INVALID, "heavy units must be 0 or 1");
+    if (value == 1.0 && e->precision == SPC_PRECISION_FP64)
+      return fail(e, SPC_ERR_INVALID, "heavy units apply to the FP32C and FP32X cell-tile passes");
+    if ((int)value != e->heavy_units_tune) {
+      e->heavy_units_tune = (int)value;
+      e->dirty = true;
+    }
+    return SPC_OK;
+  }
   if (key == SPC_TUNE_TILE_SPLIT) {
     if (!(value >= 0.0) || !(value <= 8.0) || value != std::floor(value))
       return fail(e, SPC_ERR_INVALID, "tile split must be an integer in [0, 8]");
@@ -1074,6 +1130,10 @@ inline int engine_get_tuning(const Engine *e, int key, double *value) {
     *value = e->sparse_below;
     return SPC_OK;
   }
+  if (key == SPC_TUNE_HEAVY_UNITS) {
+    *value = (double)e->heavy_units_tune;
+    return SPC_OK;
+  }
   if (key == SPC_TUNE_TILE_SPLIT) {  // the split in effect
     *value = (double)tile_split_for(e->tile_split_tune);
     return SPC_OK;
@@ -1087,15 +1147,21 @@ inline int engine_get_tuning(const Engine *e, int key, double *value) {
 struct TuneCand {
   double sparse;
   int split;
+  int heavy;
 };
 
-inline std::vector<TuneCand> kernel_candidates() {
+// The kernel-choice candidates; heavy units (float forms) with one and two
+// CTAs per cell.
+inline std::vector<TuneCand> kernel_candidates(int precision) {
   std::vector<TuneCand> c;
   for (double sb : {0.0, kSparseBelowDefault, 1e9})
     for (int split : {1, 2, 4}) {
       if (sb == 1e9 && split != 1) continue;  // no cell-tile systems left: the split does nothing
-      c.push_back({sb, split});
+      c.push_back({sb, split, 0});
     }
+  if (precision != SPC_PRECISION_FP64)
+    for (double sb : {0.0, kSparseBelowDefault})
+      for (int split : {1, 2}) c.push_back({sb, split, 1});
   return c;
 }
 
@@ -1111,8 +1177,9 @@ inline int engine_retune(Engine *e, double dt, int trial, spc_tuning *out, int c
   if (trial <= 0) return fail(e, SPC_ERR_INVALID, "trial_steps must be positive");
   SPC_TRY(engine_set_device(e));
   SPC_TRY(engine_layout(e));
-  std::vector<TuneCand> cands = e->verlet ? std::vector<TuneCand>{{e->sparse_below, e->tile_split_tune}}
-                                          : kernel_candidates();
+  std::vector<TuneCand> cands = e->verlet ? std::vector<TuneCand>{{e->sparse_below, e->tile_split_tune,
+                                                                    e->heavy_units_tune}}
+                                          : kernel_candidates(e->precision);
   const size_t P = (size_t)e->pool_cap;
   std::vector<double *> live = {e->a.x, e->a.y, e->a.phi};
   if (e->stepper == SPC_STEPPER_RK4)
@@ -1143,7 +1210,7 @@ inline int engine_retune(Engine *e, double dt, int trial, spc_tuning *out, int c
     return SPC_OK;
   };
   const double sb0 = e->sparse_below;
-  const int split0 = e->tile_split_tune;
+  const int split0 = e->tile_split_tune, heavy0 = e->heavy_units_tune;
   cudaEvent_t ev[2] = {nullptr, nullptr};
   cudaError_t ce = copy_all(true);
   if (ce == cudaSuccess) ce = cudaEventCreate(&ev[0]);
@@ -1154,6 +1221,7 @@ inline int engine_retune(Engine *e, double dt, int trial, spc_tuning *out, int c
   for (size_t k = 0; k < cands.size() && rc == SPC_OK; ++k) {
     e->sparse_below = cands[k].sparse;
     e->tile_split_tune = cands[k].split;
+    e->heavy_units_tune = cands[k].heavy;
     e->dirty = true;
     rc = engine_steps(e, dt, trial, false, nullptr, 0);
     if (rc == SPC_OK) rc = restore();
@@ -1173,6 +1241,7 @@ inline int engine_retune(Engine *e, double dt, int trial, spc_tuning *out, int c
       out[k].skin = 0.0;
       out[k].sparse_below = cands[k].sparse;
       out[k].ms_per_step = per;
+      out[k].heavy_units = cands[k].heavy;
     }
     if (rc == SPC_OK && per < best_ms) {
       best_ms = per;
@@ -1186,11 +1255,13 @@ inline int engine_retune(Engine *e, double dt, int trial, spc_tuning *out, int c
   if (rc != SPC_OK) {  // keep the caller's settings
     e->sparse_below = sb0;
     e->tile_split_tune = split0;
+    e->heavy_units_tune = heavy0;
     e->dirty = true;
     return rc;
   }
   e->sparse_below = cands[best_k].sparse;
   e->tile_split_tune = cands[best_k].split;
+  e->heavy_units_tune = cands[best_k].heavy;
   e->dirty = true;
   if (count) *count = (int)cands.size();
   if (best) *best = best_k;

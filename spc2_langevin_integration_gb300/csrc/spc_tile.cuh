@@ -158,7 +158,225 @@ __device__ __forceinline__ void block32(const float4 *__restrict__ s_c4, const f
   }
 }
 
+// Stage candidates [rlo, rlo + rcnt) of the stencil list (padded to rpad) for
+// the FP32C passes.
 template <int KIND>
+__device__ __forceinline__ void stage_fp32c(const KArgs &a, const SysConst &sc, const Stencil &st, int rlo,
+                                            int rcnt, int rpad, float4 *s_c4, float *s_d) {
+  for (int k = threadIdx.x; k < rpad; k += blockDim.x) {
+    if (k < rcnt) {
+      int q;
+      const int pj = slot_of(st, rlo + k, q);
+      const float2 f = a.fxy[pj];
+      const float2 cs = a.cs[pj];
+      s_c4[k] = make_float4(f.x + shift_x(q, sc.cell_f), f.y + shift_y(q, sc.cell_f), cs.x, cs.y);
+      if constexpr (KIND == kKindCos2) s_d[k] = a.dphi_f[pj];
+    } else {  // padding: far away, never a neighbour, never near the cutoff
+      s_c4[k] = make_float4(3.0e18f, 3.0e18f, 0.0f, 0.0f);
+      if constexpr (KIND == kKindCos2) s_d[k] = 0.0f;
+    }
+  }
+}
+
+// One warp: particle ig + li of a group of gi (lane li; li >= gi idle) against
+// part [jlo, jhi) of the staged round [rlo, rlo + rcnt); its compensated sums
+// and count go to red.*[part][li].  Called by all 32 lanes of the warp.
+template <int KIND>
+__device__ __forceinline__ void part_fp32c(const KArgs &a, const SysConst &sc, const Stencil &st,
+                                           const float4 *s_c4, const float *s_d, TileRed<KIND> &red,
+                                           int c0, int ig, int li, int gi, int rlo, int rcnt, int jlo,
+                                           int jhi, int part, bool masked, bool exact_all, float band,
+                                           float nmid) {
+  const int n_all = a.n_active;
+  const bool valid = li < gi;
+  const int p = ig + li;
+  float fxi = 3.0e30f, fyi = 3.0e30f, ca = 0.0f, sa = 0.0f, di = 0.0f;
+  double xi = 0.0, yi = 0.0;
+  if (valid) {
+    const float2 f = a.fxy[p];
+    fxi = f.x;
+    fyi = f.y;
+    const float2 t = a.cs[p];  // cos / sin of phi_i + alpha by angle addition
+    ca = t.x * sc.cos_a - t.y * sc.sin_a;
+    sa = t.y * sc.cos_a + t.x * sc.sin_a;
+    if constexpr (KIND == kKindCos2) di = a.dphi_f[p];
+    xi = a.sx[p];
+    yi = a.sy[p];
+  }
+  // staged index of i itself (the own cell is stencil entry 4); its block
+  const int self = st.prefix[4] + (p - c0) - rlo;
+  float S0 = 0.0f, C0 = 0.0f, S1 = 0.0f, C1 = 0.0f;
+  int n = 0;
+  if (KIND == kKindCos2 && masked) {
+    // pass 2 over the neighbour bitmask of pass 1 (same staged list):
+    // one 16-byte group of four mask words in hand, the next in flight
+    const uint4 *m4 = reinterpret_cast<const uint4 *>(a.nbmask);
+    const uint4 none = make_uint4(0u, 0u, 0u, 0u);
+    const int w0 = jlo / kWarp, w1 = jhi / kWarp;
+    int g = w0 >> 2;
+    uint4 cur = (valid && w0 < w1) ? m4[(size_t)g * n_all + p] : none;
+    uint4 nxt = (valid && ((g + 1) << 2) < w1) ? m4[(size_t)(g + 1) * n_all + p] : none;
+    for (int j0 = jlo; j0 < jhi; j0 += kWarp) {
+      const int w = j0 / kWarp;
+      if ((w >> 2) != g) {
+        ++g;
+        cur = nxt;
+        nxt = (valid && ((g + 1) << 2) < w1) ? m4[(size_t)(g + 1) * n_all + p] : none;
+      }
+      const int sub = w & 3;
+      const uint32_t bits = sub == 0 ? cur.x : sub == 1 ? cur.y : sub == 2 ? cur.z : cur.w;
+      float sc_ = 0.0f, ss_ = 0.0f, sdc = 0.0f, sds = 0.0f;
+#pragma unroll
+      for (int t = 0; t < kWarp; ++t) {
+        if ((bits >> t) & 1u) {
+          const float4 cj = s_c4[j0 + t];
+          const float dj = s_d[j0 + t];
+          sc_ += cj.z;
+          ss_ += cj.w;
+          sdc = fmaf(dj, cj.z, sdc);
+          sds = fmaf(dj, cj.w, sds);
+        }
+      }
+      // sum cos(phi_j - phi_i - alpha) and sum (d_j - d_i) cos(...)
+      const float b0 = fmaf(sc_, ca, ss_ * sa);
+      const float b1 = fmaf(sdc, ca, fmaf(sds, sa, -di * b0));
+      n += __popc(bits);
+      kahan_add(S0, C0, b0);
+      kahan_add(S1, C1, b1);
+    }
+  } else {
+    for (int j0 = jlo; j0 < jhi; j0 += kWarp) {
+      float sc_ = 0.0f, ss_ = 0.0f, sdc = 0.0f, sds = 0.0f, mn = 3.0e38f;
+      uint32_t bits = 0u;
+      const bool self_block = (unsigned)(self - j0) < (unsigned)kWarp;
+      if (!exact_all) {
+        if (__any_sync(0xffffffffu, self_block))
+          block32<KIND, true>(s_c4, s_d, j0, self, fxi, fyi, nmid, -band, sc_, ss_, sdc, sds, bits, mn);
+        else
+          block32<KIND, false>(s_c4, s_d, j0, self, fxi, fyi, nmid, -band, sc_, ss_, sdc, sds, bits, mn);
+      }
+      // the block's alignment terms by angle addition:
+      // sin(phi_j - phi_i - alpha) = sin phi_j ca - cos phi_j sa,
+      // cos(phi_j - phi_i - alpha) = cos phi_j ca + sin phi_j sa
+      float b0, b1 = 0.0f;
+      if constexpr (KIND == kKindSin) {
+        b0 = fmaf(ss_, ca, -sc_ * sa);
+      } else {
+        b0 = fmaf(sc_, ca, ss_ * sa);
+        b1 = fmaf(sdc, ca, fmaf(sds, sa, -di * b0));
+      }
+      // pairs the float test cannot decide: the reference's FP64 test
+      const bool amb = valid && (exact_all || mn <= band);
+      if (__any_sync(0xffffffffu, amb)) {
+        if (amb) {
+          for (int t = 0; t < kWarp; ++t) {
+            const int j = j0 + t;
+            if (j == self || j >= rcnt) continue;
+            const float4 cj = s_c4[j];
+            const float dx = cj.x - fxi, dy = cj.y - fyi;
+            if (!(exact_all || fabsf(cutoff_offset(dx, dy, nmid)) <= band)) continue;
+            int q;
+            const int pj = slot_of(st, rlo + j, q);
+            if (!exact_within(sc, xi, yi, a.sx[pj], a.sy[pj])) continue;
+            if constexpr (KIND == kKindSin) {
+              b0 += fmaf(cj.w, ca, -cj.z * sa);
+            } else {
+              const float tv = fmaf(cj.z, ca, cj.w * sa);
+              b0 += tv;
+              b1 = fmaf(s_d[j] - di, tv, b1);
+            }
+            bits |= 1u << t;
+          }
+        }
+      }
+      n += __popc(bits);
+      kahan_add(S0, C0, b0);
+      if constexpr (KIND == kKindCos2) kahan_add(S1, C1, b1);
+      if (KIND == kKindSin && masked && valid) a.nbmask[mask_at(j0 / kWarp, p, n_all)] = bits;
+    }
+  }
+  if (valid) {
+    red.s0[part][li] = S0 - C0;
+    if constexpr (KIND == kKindCos2) red.s1[part][li] = S1 - C1;
+    red.n[part][li] = n;
+  }
+}
+
+// Parts 0..S-1 of thread tid's particle added, in order, to a running
+// compensated sum.
+template <int KIND>
+__device__ __forceinline__ void add_parts(const TileRed<KIND> &red, int S, int tid, float &ts, float &tc,
+                                          float &ts1, float &tc1, int &tn) {
+  for (int part = 0; part < S; ++part) {
+    kahan_add(ts, tc, red.s0[part][tid]);
+    tn += red.n[part][tid];
+  }
+  if constexpr (KIND == kKindCos2)
+    for (int part = 0; part < S; ++part) kahan_add(ts1, tc1, red.s1[part][tid]);
+}
+
+template <int KIND>
+__device__ __forceinline__ void finish_fp32c(const KArgs &a, int epi, const SysDesc &sd, int p, float s0,
+                                             float s1, int n) {
+  ILane il;
+  load_i<kPrecFP32C, KIND>(a, sd.sc, il, p, true);
+  Acc<kPrecFP32C> acc;
+  acc.init();
+  acc.s0 = s0;
+  if constexpr (KIND == kKindCos2) acc.s1 = s1;
+  acc.n = n;
+  epilogue<kPrecFP32C, KIND>(a, epi, sd, il, acc, a.pidx[p]);
+}
+
+// Heavy cells (tuning SPC_TUNE_HEAVY_UNITS).  A cell whose pair tests
+// (particles x stencil candidates) exceed kHeavyTests, about 1.8 times those
+// of a cell of a uniform 64-per-cell state (64 x 576), and whose list takes
+// at most kSplitRounds staging rounds is not run by the cell-tile kernel: it is
+// cut into units of 32 particles x one staging round, and the units kernel
+// launched after the cell-tile kernel runs every unit on its own CTA.  Cells
+// of a clustered state reach ~6,000 candidates for ~380 particles; as whole
+// 128-particle groups on one CTA each they ran for several times a typical
+// cell and set the end of the single-wave pass.  A unit's four warps take a
+// quarter of its round each; the unit stores its per-particle sums of the
+// round, and the last unit of a 32-particle chunk to finish (a counter per
+// chunk, reset by that unit) adds the rounds in order and finishes the
+// particles.  k_list_units lists the units once per evaluation (both passes
+// see the same cells).  Which cells are heavy, and the order of every sum, depend on
+// the cell alone, so the results do not depend on the CTAs per cell.
+constexpr int kHeavyTests = 65536;
+constexpr int kSplitRounds = 8;
+
+__device__ __forceinline__ bool heavy_cell(const KArgs &a, int n_c, int total, int cap) {
+  return a.units != nullptr && (long long)n_c * total > kHeavyTests && total <= kSplitRounds * cap;
+}
+
+// List the units of every heavy cell of the cell-tile systems (one thread per
+// cell), once per evaluation after the gather, for both passes' units kernels,
+// and mark the heavy cells for the cell-tile kernels to skip.
+// CAP: the form's staging round.
+template <int CAP>
+__global__ void k_list_units(KArgs a) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= a.ncell_tile) return;
+  const int c0 = a.cell_start[c], n_c = a.cell_start[c + 1] - c0;
+  a.cell_heavy[c] = 0;
+  if (n_c == 0) return;
+  const SysDesc &sd = a.sys[a.sys_of_c[c]];
+  if (sd.sc.allpairs) return;
+  Stencil st;
+  stencil_of(a, sd, c, st);
+  const int total = st.prefix[9];
+  if (!heavy_cell(a, n_c, total, CAP)) return;
+  a.cell_heavy[c] = 1;
+  const int rounds = (total + CAP - 1) / CAP;
+  const int units = (n_c + kWarp - 1) / kWarp * rounds;
+  const int base = atomicAdd(a.unit_count, units);
+  for (int u = 0; u < units; ++u) a.units[base + u] = make_int2(c, u);
+}
+
+// UNITS: heavy cells are left to the units kernel (a separate instantiation, so
+// that the kernel without heavy units compiles exactly as before).
+template <int KIND, bool UNITS>
 __global__ void __launch_bounds__(kTileThreads32, kTileMinBlocks32) k_tile_fp32c(KArgs a, int epi) {
   __shared__ float4 s_c4[kTileCap];   // x+shift, y+shift, cos phi, sin phi (padded to 32)
   __shared__ float s_d[KIND == kKindCos2 ? kTileCap : 1];  // pass 2: phase rate (float)
@@ -172,6 +390,9 @@ __global__ void __launch_bounds__(kTileThreads32, kTileMinBlocks32) k_tile_fp32c
   for (int item = blockIdx.x; item < nitems; item += gridDim.x) {
     TileItem ti;
     if (!tile_item<kTileThreads32>(a, item, ti)) continue;
+    if constexpr (UNITS) {
+      if (a.cell_heavy[ti.c]) continue;  // run by the units kernel
+    }
     const int c = ti.c, c0 = ti.c0, cb = ti.cb, ce = ti.ce;
     const SysDesc &sd = a.sys[a.sys_of_c[c]];
     const SysConst &sc = sd.sc;
@@ -184,6 +405,7 @@ __global__ void __launch_bounds__(kTileThreads32, kTileMinBlocks32) k_tile_fp32c
     const int total = st.prefix[9];
     const int rounds = (total + kTileCap - 1) / kTileCap;
     const bool masked = rounds == 1 && a.nbmask != nullptr && !exact_all;
+
     for (int ig = cb; ig < ce; ig += kTileThreads32) {
       const int gi = min(kTileThreads32, ce - ig);
       if (tid < gi) {
@@ -368,6 +590,75 @@ __global__ void __launch_bounds__(kTileThreads32, kTileMinBlocks32) k_tile_fp32c
   }
 }
 
+// The heavy units of an FP32C pass (listed by k_tile_fp32c of the same pass):
+// unit u of cell c is chunk u / rounds (32 particles) x staging round
+// u % rounds, its list split among the four warps.
+template <int KIND>
+__global__ void __launch_bounds__(kTileThreads32, kTileMinBlocks32) k_units_fp32c(KArgs a, int epi) {
+  __shared__ float4 s_c4[kTileCap];
+  __shared__ float s_d[KIND == kKindCos2 ? kTileCap : 1];
+  __shared__ TileRed<KIND> red;
+  __shared__ int s_last;
+  const int n_all = a.n_active;
+  const int tid = threadIdx.x, w = tid / kWarp, lane = tid % kWarp;
+  const int count = *a.unit_count;
+  for (int i = blockIdx.x; i < count; i += gridDim.x) {
+    const int2 e = a.units[i];
+    const int c = e.x, c0 = a.cell_start[c], c1 = a.cell_start[c + 1];
+    const SysDesc &sd = a.sys[a.sys_of_c[c]];
+    const SysConst &sc = sd.sc;
+    const float lo2 = sc.lo2, hi2 = sc.hi2;
+    const float band = 0.5f * (hi2 - lo2), nmid = -0.5f * (hi2 + lo2);
+    const bool exact_all = sc.exact_all != 0;
+    Stencil st;
+    stencil_of(a, sd, c, st);
+    const int total = st.prefix[9];
+    const int rounds = (total + kTileCap - 1) / kTileCap;
+    const bool masked = rounds == 1 && a.nbmask != nullptr && !exact_all;
+    const int k = e.y / rounds, r = e.y - k * rounds;
+    const int ig = c0 + k * kWarp, gi = min(kWarp, c1 - ig);
+    const int rlo = r * kTileCap, rcnt = min(kTileCap, total - rlo);
+    const int rpad = (rcnt + kWarp - 1) & ~(kWarp - 1);
+    __syncthreads();
+    stage_fp32c<KIND>(a, sc, st, rlo, rcnt, rpad, s_c4, s_d);
+    __syncthreads();
+    part_fp32c<KIND>(a, sc, st, s_c4, s_d, red, c0, ig, lane, gi, rlo, rcnt, split_point(rpad, w, 4),
+                     split_point(rpad, w + 1, 4), w, masked, exact_all, band, nmid);
+    __syncthreads();
+    float ts = 0.0f, tc = 0.0f, ts1 = 0.0f, tc1 = 0.0f;
+    int tn = 0;
+    if (tid < gi) add_parts<KIND>(red, 4, tid, ts, tc, ts1, tc1, tn);
+    const int p = ig + tid;
+    if (rounds == 1) {
+      if (tid < gi) finish_fp32c<KIND>(a, epi, sd, p, ts - tc, ts1 - tc1, tn);
+      continue;
+    }
+    if (tid < gi) {
+      a.part_f[(size_t)r * n_all + p] = make_float2(ts - tc, ts1 - tc1);
+      a.part_n[(size_t)r * n_all + p] = tn;
+    }
+    __threadfence();
+    __syncthreads();
+    if (tid == 0) s_last = atomicAdd(&a.unit_done[ig], 1) == rounds - 1;
+    __syncthreads();
+    if (s_last) {
+      __threadfence();
+      if (tid < gi) {
+        float s0 = 0.0f, cc0 = 0.0f, s1 = 0.0f, cc1 = 0.0f;
+        int nn = 0;
+        for (int q = 0; q < rounds; ++q) {
+          const float2 v = __ldcg(&a.part_f[(size_t)q * n_all + p]);
+          kahan_add(s0, cc0, v.x);
+          if constexpr (KIND == kKindCos2) kahan_add(s1, cc1, v.y);
+          nn += __ldcg(&a.part_n[(size_t)q * n_all + p]);
+        }
+        finish_fp32c<KIND>(a, epi, sd, p, s0 - cc0, s1 - cc1, nn);
+      }
+      if (tid == 0) a.unit_done[ig] = 0;  // for the next pass
+    }
+  }
+}
+
 // ---------------------------------------------------------------------------
 // FP32X passes.  The same CTA-per-cell staging, work split and pass-1 masks
 // as FP32C, but each accepted candidate adds its fixed-point (cos phi_j,
@@ -407,7 +698,120 @@ __device__ __forceinline__ void block32x(const float2 *__restrict__ s_xy, const 
   }
 }
 
+// Stage candidates [rlo, rlo + rcnt) of the stencil list (padded to rpad) for
+// the FP32X passes.
 template <int KIND>
+__device__ __forceinline__ void stage_fp32x(const KArgs &a, const SysConst &sc, const Stencil &st, int rlo,
+                                            int rcnt, int rpad, float2 *s_xy, longlong2 *s_v) {
+  for (int k = threadIdx.x; k < rpad; k += blockDim.x) {
+    if (k < rcnt) {
+      int q;
+      const int pj = slot_of(st, rlo + k, q);
+      const float2 f = a.fxy[pj];
+      s_xy[k] = make_float2(f.x + shift_x(q, sc.cell_f), f.y + shift_y(q, sc.cell_f));
+      s_v[k] = KIND == kKindSin ? a.ics[pj] : a.iws[pj];
+    } else {  // padding: far away, never a neighbour, never near the cutoff
+      s_xy[k] = make_float2(3.0e18f, 3.0e18f);
+      s_v[k] = make_longlong2(0, 0);
+    }
+  }
+}
+
+// One warp: particle ig + li of a group of gi (lane li; li >= gi idle) against
+// part [jlo, jhi) of the staged round [rlo, rlo + rcnt); its fixed-point sums
+// and count go to red.*[part][li].  Called by all 32 lanes of the warp.
+template <int KIND>
+__device__ __forceinline__ void part_fp32x(const KArgs &a, const SysConst &sc, const Stencil &st,
+                                           const float2 *s_xy, const longlong2 *s_v, TileRedX &red, int c0,
+                                           int ig, int li, int gi, int rlo, int rcnt, int jlo, int jhi,
+                                           int part, bool masked, bool exact_all, float band, float nmid) {
+  const int n_all = a.n_active;
+  const bool valid = li < gi;
+  const int p = ig + li;
+  float fxi = 3.0e30f, fyi = 3.0e30f;
+  double xi = 0.0, yi = 0.0;
+  if (valid) {
+    const float2 f = a.fxy[p];
+    fxi = f.x;
+    fyi = f.y;
+    xi = a.sx[p];
+    yi = a.sy[p];
+  }
+  const int self = st.prefix[4] + (p - c0) - rlo;
+  long long C = 0, Sn = 0;
+  int n = 0;
+  if (KIND == kKindCos2 && masked) {
+    // pass 2 over the neighbour bitmask of pass 1 (same staged list)
+    const uint4 *m4 = reinterpret_cast<const uint4 *>(a.nbmask);
+    const uint4 none = make_uint4(0u, 0u, 0u, 0u);
+    const int w0 = jlo / kWarp, w1 = jhi / kWarp;
+    int g = w0 >> 2;
+    uint4 cur = (valid && w0 < w1) ? m4[(size_t)g * n_all + p] : none;
+    uint4 nxt = (valid && ((g + 1) << 2) < w1) ? m4[(size_t)(g + 1) * n_all + p] : none;
+    for (int j0 = jlo; j0 < jhi; j0 += kWarp) {
+      const int wd = j0 / kWarp;
+      if ((wd >> 2) != g) {
+        ++g;
+        cur = nxt;
+        nxt = (valid && ((g + 1) << 2) < w1) ? m4[(size_t)(g + 1) * n_all + p] : none;
+      }
+      const int sub = wd & 3;
+      const uint32_t bits = sub == 0 ? cur.x : sub == 1 ? cur.y : sub == 2 ? cur.z : cur.w;
+#pragma unroll
+      for (int t = 0; t < kWarp; ++t) {
+        if ((bits >> t) & 1u) {
+          const longlong2 v = s_v[j0 + t];
+          C += v.x;
+          Sn += v.y;
+        }
+      }
+      n += __popc(bits);
+    }
+  } else {
+    for (int j0 = jlo; j0 < jhi; j0 += kWarp) {
+      float mn = 3.0e38f;
+      uint32_t bits = 0u;
+      const bool self_block = (unsigned)(self - j0) < (unsigned)kWarp;
+      if (!exact_all) {
+        if (__any_sync(0xffffffffu, self_block))
+          block32x<true>(s_xy, s_v, j0, self, fxi, fyi, nmid, -band, C, Sn, bits, mn);
+        else
+          block32x<false>(s_xy, s_v, j0, self, fxi, fyi, nmid, -band, C, Sn, bits, mn);
+      }
+      // pairs the float test cannot decide: the reference's FP64 test
+      const bool amb = valid && (exact_all || mn <= band);
+      if (__any_sync(0xffffffffu, amb)) {
+        if (amb) {
+          for (int t = 0; t < kWarp; ++t) {
+            const int j = j0 + t;
+            if (j == self || j >= rcnt) continue;
+            const float2 cj = s_xy[j];
+            const float dx = cj.x - fxi, dy = cj.y - fyi;
+            if (!(exact_all || fabsf(cutoff_offset(dx, dy, nmid)) <= band)) continue;
+            int q;
+            const int pj = slot_of(st, rlo + j, q);
+            if (!exact_within(sc, xi, yi, a.sx[pj], a.sy[pj])) continue;
+            const longlong2 v = s_v[j];
+            C += v.x;
+            Sn += v.y;
+            bits |= 1u << t;
+          }
+        }
+      }
+      n += __popc(bits);
+      if (KIND == kKindSin && masked && valid) a.nbmask[mask_at(j0 / kWarp, p, n_all)] = bits;
+    }
+  }
+  if (valid) {
+    red.c[part][li] = C;
+    red.s[part][li] = Sn;
+    red.n[part][li] = n;
+  }
+}
+
+// UNITS: heavy cells are left to the units kernel (a separate instantiation, so
+// that the kernel without heavy units compiles exactly as before).
+template <int KIND, bool UNITS>
 __global__ void __launch_bounds__(kTileThreads32, kTileMinBlocks32) k_tile_fp32x(KArgs a, int epi) {
   __shared__ float2 s_xy[kTileCapX];     // x+shift, y+shift (padded to 32)
   __shared__ longlong2 s_v[kTileCapX];   // pass 1: ics, pass 2: iws of the candidate
@@ -418,6 +822,9 @@ __global__ void __launch_bounds__(kTileThreads32, kTileMinBlocks32) k_tile_fp32x
   for (int item = blockIdx.x; item < nitems; item += gridDim.x) {
     TileItem ti;
     if (!tile_item<kTileThreads32>(a, item, ti)) continue;
+    if constexpr (UNITS) {
+      if (a.cell_heavy[ti.c]) continue;  // run by the units kernel
+    }
     const int c = ti.c, c0 = ti.c0, cb = ti.cb, ce = ti.ce;
     const SysDesc &sd = a.sys[a.sys_of_c[c]];
     const SysConst &sc = sd.sc;
@@ -430,6 +837,7 @@ __global__ void __launch_bounds__(kTileThreads32, kTileMinBlocks32) k_tile_fp32x
     const int total = st.prefix[9];
     const int rounds = (total + kTileCapX - 1) / kTileCapX;
     const bool masked = rounds == 1 && a.nbmask != nullptr && !exact_all;
+
     for (int ig = cb; ig < ce; ig += kTileThreads32) {
       const int gi = min(kTileThreads32, ce - ig);
       // thread tid's particle (ig + tid): its sums over all rounds
@@ -558,6 +966,86 @@ __global__ void __launch_bounds__(kTileThreads32, kTileMinBlocks32) k_tile_fp32x
         a.xcnt[ig + tid] = t_n;
       }
       __syncthreads();
+    }
+  }
+}
+
+// The heavy units of an FP32X pass (listed by k_tile_fp32x of the same pass),
+// as k_units_fp32c.  A unit's round sums are exact 64-bit integers (below
+// 2^62: kTileCapX candidates of |v| <= 2^52), added over the rounds in 128
+// bits, so the particle's sums are those of the whole-group path.
+template <int KIND>
+__global__ void __launch_bounds__(kTileThreads32, kTileMinBlocks32) k_units_fp32x(KArgs a, int epi) {
+  __shared__ float2 s_xy[kTileCapX];
+  __shared__ longlong2 s_v[kTileCapX];
+  __shared__ TileRedX red;
+  __shared__ int s_last;
+  const int n_all = a.n_active;
+  const int tid = threadIdx.x, w = tid / kWarp, lane = tid % kWarp;
+  const int count = *a.unit_count;
+  for (int i = blockIdx.x; i < count; i += gridDim.x) {
+    const int2 e = a.units[i];
+    const int c = e.x, c0 = a.cell_start[c], c1 = a.cell_start[c + 1];
+    const SysDesc &sd = a.sys[a.sys_of_c[c]];
+    const SysConst &sc = sd.sc;
+    const float lo2 = sc.lo2, hi2 = sc.hi2;
+    const float band = 0.5f * (hi2 - lo2), nmid = -0.5f * (hi2 + lo2);
+    const bool exact_all = sc.exact_all != 0;
+    const int qv = KIND == kKindSin ? kXQ : sc.xq2;
+    Stencil st;
+    stencil_of(a, sd, c, st);
+    const int total = st.prefix[9];
+    const int rounds = (total + kTileCapX - 1) / kTileCapX;
+    const bool masked = rounds == 1 && a.nbmask != nullptr && !exact_all;
+    const int k = e.y / rounds, r = e.y - k * rounds;
+    const int ig = c0 + k * kWarp, gi = min(kWarp, c1 - ig);
+    const int rlo = r * kTileCapX, rcnt = min(kTileCapX, total - rlo);
+    const int rpad = (rcnt + kWarp - 1) & ~(kWarp - 1);
+    __syncthreads();
+    stage_fp32x<KIND>(a, sc, st, rlo, rcnt, rpad, s_xy, s_v);
+    __syncthreads();
+    part_fp32x<KIND>(a, sc, st, s_xy, s_v, red, c0, ig, lane, gi, rlo, rcnt, split_point(rpad, w, 4),
+                     split_point(rpad, w + 1, 4), w, masked, exact_all, band, nmid);
+    __syncthreads();
+    long long uc = 0, us = 0;
+    int un = 0;
+    if (tid < gi)
+      for (int part = 0; part < 4; ++part) {
+        uc += red.c[part][tid];
+        us += red.s[part][tid];
+        un += red.n[part][tid];
+      }
+    const int p = ig + tid;
+    if (rounds == 1) {
+      if (tid < gi) {
+        a.xsum[p] = make_double2(from_fixed128(uc, qv), from_fixed128(us, qv));
+        a.xcnt[p] = un;
+      }
+      continue;
+    }
+    if (tid < gi) {
+      a.part_x[(size_t)r * n_all + p] = make_longlong2(uc, us);
+      a.part_n[(size_t)r * n_all + p] = un;
+    }
+    __threadfence();
+    __syncthreads();
+    if (tid == 0) s_last = atomicAdd(&a.unit_done[ig], 1) == rounds - 1;
+    __syncthreads();
+    if (s_last) {
+      __threadfence();
+      if (tid < gi) {
+        __int128 sc_ = 0, ss_ = 0;
+        int nn = 0;
+        for (int q = 0; q < rounds; ++q) {
+          const longlong2 v = __ldcg(&a.part_x[(size_t)q * n_all + p]);
+          sc_ += v.x;
+          ss_ += v.y;
+          nn += __ldcg(&a.part_n[(size_t)q * n_all + p]);
+        }
+        a.xsum[p] = make_double2(from_fixed128(sc_, qv), from_fixed128(ss_, qv));
+        a.xcnt[p] = nn;
+      }
+      if (tid == 0) a.unit_done[ig] = 0;  // for the next pass
     }
   }
 }

@@ -2,9 +2,11 @@
 
 * spc_autotune_ex offers every tuning dimension: the kernel choice (all
   cell-tile, the default split, all warp-per-cell), 1, 2 or 4 CTAs per cell,
-  and Verlet skins where the precision and stencil allow them.
+  heavy cells as units (float forms), and Verlet skins where the precision
+  and stencil allow them.
 * Every kernel-choice candidate computes the same neighbour sets: FP64 and
-  FP32X trajectories are bit for bit the same under each of them.
+  FP32X trajectories are bit for bit the same under each of them, and FP32C
+  ones under every CTA split (with heavy units off, and with them on).
 * spc_retune / spc_batch_retune leave the state and the step counters as they
   were, so a run that retunes midway equals one that does not, bit for bit.
 """
@@ -32,34 +34,48 @@ def test_autotune_ex_offers_every_dimension():
     assert {c["sparse_below"] for c in cell} >= {0.0, 1e9}
     assert any(c["neighbour"] == "verlet" for c in cands)
     assert 0 <= best < len(cands) and all(c["ms_per_step"] > 0 for c in cands)
-    # FP32X runs the cell list only
+    assert {c["heavy_units"] for c in cands} == {0}  # FP64 has no heavy units
+    # FP32X runs the cell list only, with and without heavy units
     cx, _ = abi.autotune_ex(N, _params(abi.PRECISION_FP32X), st, trial_steps=5)
-    assert all(c["neighbour"] == "cell" for c in cx) and len(cx) == len(cell)
+    assert all(c["neighbour"] == "cell" for c in cx)
+    assert len([c for c in cx if c["heavy_units"] == 0]) == len(cell)
+    assert {(c["sparse_below"], c["tile_split"]) for c in cx if c["heavy_units"] == 1} == \
+        {(0.0, 1), (0.0, 2), (24.0, 1), (24.0, 2)}
 
 
-@pytest.mark.parametrize("precision", [abi.PRECISION_FP64, abi.PRECISION_FP32X, abi.PRECISION_FP32C])
-def test_kernel_choices_give_identical_trajectories(precision):
+@pytest.mark.parametrize("precision,n,patch", [
+    (abi.PRECISION_FP64, N, 0.45), (abi.PRECISION_FP32X, N, 0.45), (abi.PRECISION_FP32C, N, 0.45),
+    (abi.PRECISION_FP32X, 9000, 0.2), (abi.PRECISION_FP32C, 9000, 0.2)])
+def test_kernel_choices_give_identical_trajectories(precision, n, patch):
     """FP64 and FP32X: every kernel choice; FP32C: every CTA split of the
-    cell-tile kernels (its cell-tile and warp-per-cell kernels sum in
-    different orders).  The state is clustered into a patch so that cells
-    hold several particle groups and the splits really spread them."""
+    cell-tile kernels, with heavy units off and on (its cell-tile and
+    warp-per-cell kernels, and heavy units, sum in different orders).  The
+    particles are clustered into a patch so that cells hold several particle
+    groups and the splits really spread them.  6,000 in a 0.45 x 0.45 patch
+    give heavy cells of ~4,200 candidates; 9,000 in a 0.2 x 0.2 patch share
+    one stencil, more staging rounds than a heavy cell may have, so those
+    cells stay whole groups with heavy units on."""
     rng = np.random.default_rng(91)
-    st = init_state(N, L, 91)
-    st[0::3] = 0.2 + 0.45 * rng.random(N)  # 6,000 particles in a 0.45 x 0.45 patch
-    st[1::3] = 0.2 + 0.45 * rng.random(N)
-    choices = ((0.0, 1), (0.0, 2), (0.0, 4), (24.0, 1), (1e9, 1))
+    st = init_state(n, L, 91)
+    st[0::3] = 0.2 + patch * rng.random(n)
+    st[1::3] = 0.2 + patch * rng.random(n)
+    choices = [((0.0, 1, 0), (0.0, 2, 0), (0.0, 4, 0), (24.0, 1, 0), (1e9, 1, 0))]
+    if precision == abi.PRECISION_FP32X:
+        choices = [choices[0] + ((0.0, 1, 1), (0.0, 2, 1), (24.0, 1, 1))]
     if precision == abi.PRECISION_FP32C:
-        choices = choices[:3]
-    out = []
-    for sb, split in choices:
-        with abi.System(N, _params(precision)) as s:
-            s.set_tuning(abi.TUNE_SPARSE_BELOW, sb)
-            s.set_tuning(abi.TUNE_TILE_SPLIT, split)
-            s.upload_state(st)
-            s.step(0.005, 30)
-            out.append(s.download_state())
-    for o in out[1:]:
-        assert np.array_equal(o, out[0])
+        choices = [choices[0][:3], ((0.0, 1, 1), (0.0, 2, 1), (0.0, 4, 1))]
+    for group in choices:
+        out = []
+        for sb, split, heavy in group:
+            with abi.System(n, _params(precision)) as s:
+                s.set_tuning(abi.TUNE_SPARSE_BELOW, sb)
+                s.set_tuning(abi.TUNE_TILE_SPLIT, split)
+                s.set_tuning(abi.TUNE_HEAVY_UNITS, heavy)
+                s.upload_state(st)
+                s.step(0.005, 30 if n == N else 10)
+                out.append(s.download_state())
+        for o in out[1:]:
+            assert np.array_equal(o, out[0])
 
 
 @pytest.mark.parametrize("precision", [abi.PRECISION_FP64, abi.PRECISION_FP32X])
@@ -73,9 +89,11 @@ def test_retune_midway_leaves_the_run_unchanged(precision):
             if retune:
                 before, ctr = s.download_state(), s.step_counter
                 cands, best = s.retune(0.005, trial_steps=5)
-                assert len(cands) == 7 and 0 <= best < 7
+                nc = 7 if precision == abi.PRECISION_FP64 else 11
+                assert len(cands) == nc and 0 <= best < nc
                 assert np.array_equal(s.download_state(), before) and s.step_counter == ctr
                 assert s.get_tuning(abi.TUNE_TILE_SPLIT) == cands[best]["tile_split"]
+                assert s.get_tuning(abi.TUNE_HEAVY_UNITS) == cands[best]["heavy_units"]
                 s.prepare_graph(0.005, 20)  # captured, not run: state and counter unchanged
                 assert s.graph_nodes() > 0
                 assert np.array_equal(s.download_state(), before) and s.step_counter == ctr
@@ -101,7 +119,7 @@ def test_batch_retune_leaves_the_run_unchanged():
                 before = [b.download(s) for s in slots]
                 status = [b.status(s) for s in slots]
                 cands, best = b.retune(0.01, trial_steps=5)
-                assert len(cands) == 7
+                assert len(cands) == 11
                 assert all(np.array_equal(b.download(s), x) for s, x in zip(slots, before))
                 assert [b.status(s) for s in slots] == status
             b.step(0.01, 40)  # past the budgets: every system stops at 60 steps
