@@ -179,6 +179,10 @@ struct SysHost {
 struct Engine {
   int stepper = 0, precision = 0, device = 0;
   cudaStream_t stream = nullptr;
+  // heavy units: the units kernel runs on `side`, forked from and joined back
+  // to `stream`, beside the cell-tile kernel (float forms)
+  cudaStream_t side = nullptr;
+  cudaEvent_t fork_ev = nullptr, join_ev = nullptr;
   std::vector<void *> allocs;
   std::string err;
   // capacities
@@ -398,6 +402,9 @@ inline int engine_init(Engine *e, int stepper, int precision, int pool_cap, int 
     SPC_TRY(dalloc(e, &a.cell_heavy, (size_t)cell_cap));
     SPC_TRY(dalloc(e, &a.part_n, (size_t)kSplitRounds * N));
     SPC_TRY(dalloc(e, &a.unit_done, N));
+    SPC_CUDA(e, cudaStreamCreateWithFlags(&e->side, cudaStreamNonBlocking));
+    SPC_CUDA(e, cudaEventCreateWithFlags(&e->fork_ev, cudaEventDisableTiming));
+    SPC_CUDA(e, cudaEventCreateWithFlags(&e->join_ev, cudaEventDisableTiming));
   }
   SPC_TRY(dalloc(e, &a.cell_start, (size_t)cell_cap + 1));
   SPC_TRY(dalloc(e, &sys_of_c, (size_t)cell_cap));
@@ -547,6 +554,12 @@ inline void engine_free(Engine *e) {
   }
   if (e->run.copy) cudaStreamDestroy(e->run.copy);
   e->run.copy = nullptr;
+  if (e->side) cudaStreamSynchronize(e->side);
+  if (e->fork_ev) cudaEventDestroy(e->fork_ev);
+  if (e->join_ev) cudaEventDestroy(e->join_ev);
+  if (e->side) cudaStreamDestroy(e->side);
+  e->side = nullptr;
+  e->fork_ev = e->join_ev = nullptr;
   for (void *p : e->allocs) cudaFree(p);
   e->allocs.clear();
   if (e->stream) cudaStreamDestroy(e->stream);
@@ -902,6 +915,22 @@ int launch_pass_t(Engine *e, const KArgs &a, int epi) {
     {
       if (e->ncell_tile > 0) {
         const int grid = std::min(e->ncell_tile * std::max(a.tile_split, 1), 152 * 256);
+        if constexpr ((PREC == kPrecFP32C || PREC == kPrecFP32X) && KIND != kKindNb) {
+          if (a.units) {
+            // the heavy cells' units (listed after the gather) run beside the
+            // cell-tile kernel, each filling the SMs the other leaves idle; the
+            // units kernel's CTAs loop over the units and take four of the
+            // seven CTA slots of an SM, so the cell-tile kernel starts at once
+            SPC_CUDA(e, cudaEventRecord(e->fork_ev, st));
+            SPC_CUDA(e, cudaStreamWaitEvent(e->side, e->fork_ev, 0));
+            if constexpr (PREC == kPrecFP32C)
+              k_units_fp32c<KIND><<<152 * 4, kTileThreads32, 0, e->side>>>(a, epi);
+            else
+              k_units_fp32x<KIND><<<152 * 4, kTileThreads32, 0, e->side>>>(a, epi);
+            SPC_LAUNCHED(e);
+            SPC_CUDA(e, cudaEventRecord(e->join_ev, e->side));
+          }
+        }
         if constexpr (PREC == kPrecFP32C) {
           if (a.units)
             k_tile_fp32c<KIND, true><<<grid, kTileThreads32, 0, st>>>(a, epi);
@@ -915,15 +944,8 @@ int launch_pass_t(Engine *e, const KArgs &a, int epi) {
         } else
           k_tile_fp64<KIND><<<grid, kTileThreads64, 0, st>>>(a, epi);
         SPC_LAUNCHED(e);
-        if constexpr ((PREC == kPrecFP32C || PREC == kPrecFP32X) && KIND != kKindNb) {
-          if (a.units) {  // the heavy cells' units the cell-tile kernel listed
-            if constexpr (PREC == kPrecFP32C)
-              k_units_fp32c<KIND><<<152 * kTileMinBlocks32, kTileThreads32, 0, st>>>(a, epi);
-            else
-              k_units_fp32x<KIND><<<152 * kTileMinBlocks32, kTileThreads32, 0, st>>>(a, epi);
-            SPC_LAUNCHED(e);
-          }
-        }
+        if constexpr ((PREC == kPrecFP32C || PREC == kPrecFP32X) && KIND != kKindNb)
+          if (a.units) SPC_CUDA(e, cudaStreamWaitEvent(st, e->join_ev, 0));
       }
       if (e->ncell_warp > 0) {
         const int grid = std::min(blocks_for(e->ncell_warp, kWarpPassWarps), 152 * 64);
