@@ -127,3 +127,38 @@ def test_batch_retune_leaves_the_run_unchanged():
             assert all(b.status(s)[1] == 0 for s in slots)
     for x, y in zip(*finals):
         assert np.array_equal(x, y)
+
+
+@pytest.mark.parametrize("precision", [abi.PRECISION_FP32X, abi.PRECISION_FP32C])
+def test_heavy_units_graph_equals_eager(precision):
+    """With heavy units the units kernel runs on a second stream beside the
+    cell-tile kernel (parallel branches of the step graph): captured graph
+    replays and eager steps give the same bits, and FP32X gives the bits of
+    the run without heavy units."""
+    rng = np.random.default_rng(94)
+    st = init_state(N, L, 94)
+    st[0::3] = 0.2 + 0.45 * rng.random(N)
+    st[1::3] = 0.2 + 0.45 * rng.random(N)
+    out = {}
+    for heavy, graph in ((1, False), (1, True), (0, False)):
+        with abi.System(N, _params(precision)) as s:
+            s.set_tuning(abi.TUNE_SPARSE_BELOW, 0.0)
+            s.set_tuning(abi.TUNE_HEAVY_UNITS, heavy)
+            assert s.get_tuning(abi.TUNE_HEAVY_UNITS) == heavy
+            s.upload_state(st)
+            for _ in range(3):
+                s.step(0.005, 10, graph=graph)
+            out[(heavy, graph)] = s.download_state()
+    assert np.array_equal(out[(1, False)], out[(1, True)])
+    if precision == abi.PRECISION_FP32X:
+        assert np.array_equal(out[(1, False)], out[(0, False)])
+
+
+def test_heavy_units_refused_for_fp64():
+    with abi.System(N, _params(abi.PRECISION_FP64)) as s:
+        with pytest.raises(abi.SpcError):
+            s.set_tuning(abi.TUNE_HEAVY_UNITS, 1)
+        for bad in (-1.0, 2.0, 0.5):
+            with pytest.raises(abi.SpcError):
+                s.set_tuning(abi.TUNE_HEAVY_UNITS, bad)
+        s.set_tuning(abi.TUNE_HEAVY_UNITS, 0)
