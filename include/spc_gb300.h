@@ -106,7 +106,8 @@ typedef struct spc_params {
 
 typedef struct spc_handle spc_handle;
 
-/* Library / version. */
+/* Library / version.  SPC_ABI_VERSION changes with any layout change of the
+ * structs above or below (3: spc_tuning gained heavy_units). */
 int spc_abi_version(void);
 const char *spc_last_error(const spc_handle *h); /* h may be NULL: last global error */
 

@@ -918,15 +918,16 @@ int launch_pass_t(Engine *e, const KArgs &a, int epi) {
         if constexpr ((PREC == kPrecFP32C || PREC == kPrecFP32X) && KIND != kKindNb) {
           if (a.units) {
             // the heavy cells' units (listed after the gather) run beside the
-            // cell-tile kernel, each filling the SMs the other leaves idle; the
-            // units kernel's CTAs loop over the units and take four of the
-            // seven CTA slots of an SM, so the cell-tile kernel starts at once
+            // cell-tile kernel, each filling the SMs the other leaves idle.
+            // One CTA per unit up to 16 per SM (CTAs past the unit count
+            // return at once, a larger count is taken in turn): measured
+            // against 3, 4, 6, 7 and 10 per SM, the most units in flight won.
             SPC_CUDA(e, cudaEventRecord(e->fork_ev, st));
             SPC_CUDA(e, cudaStreamWaitEvent(e->side, e->fork_ev, 0));
             if constexpr (PREC == kPrecFP32C)
-              k_units_fp32c<KIND><<<152 * 4, kTileThreads32, 0, e->side>>>(a, epi);
+              k_units_fp32c<KIND><<<152 * 16, kTileThreads32, 0, e->side>>>(a, epi);
             else
-              k_units_fp32x<KIND><<<152 * 4, kTileThreads32, 0, e->side>>>(a, epi);
+              k_units_fp32x<KIND><<<152 * 16, kTileThreads32, 0, e->side>>>(a, epi);
             SPC_LAUNCHED(e);
             SPC_CUDA(e, cudaEventRecord(e->join_ev, e->side));
           }
