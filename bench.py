@@ -811,7 +811,7 @@ def tune_form(abi, w, precision, rank=0):
 
 
 def run_form(abi, torch, w, precision, steps, warmup, rank, dist, params=None, sparse_below=None,
-             e2e=True, tile_split=None, heavy_units=None):
+             e2e=True, tile_split=None, cell_units=None):
     """Device-timed graph replays of the workload; then (e2e) the same through
     the C-ABI with host buffers, and a per-phase profile.
 
@@ -829,8 +829,8 @@ def run_form(abi, torch, w, precision, steps, warmup, rank, dist, params=None, s
         s.set_tuning(abi.TUNE_SPARSE_BELOW, sparse_below)
     if tile_split is not None:
         s.set_tuning(abi.TUNE_TILE_SPLIT, tile_split)
-    if heavy_units is not None:
-        s.set_tuning(abi.TUNE_HEAVY_UNITS, heavy_units)
+    if cell_units is not None:
+        s.set_tuning(abi.TUNE_CELL_UNITS, cell_units)
     s.upload_state(st)
     s.upload_omega(omega)
     stream = torch.cuda.ExternalStream(s.stream)
@@ -902,7 +902,7 @@ def apply_tuning(abi, s, tun):
     """Set a cell-list handle's kernel choice from a tuning candidate."""
     s.set_tuning(abi.TUNE_SPARSE_BELOW, tun["sparse_below"])
     s.set_tuning(abi.TUNE_TILE_SPLIT, tun["tile_split"])
-    s.set_tuning(abi.TUNE_HEAVY_UNITS, tun.get("heavy_units", 0))
+    s.set_tuning(abi.TUNE_CELL_UNITS, tun.get("cell_units", 0))
 
 
 def phase_sample(abi, w, params, s, state, omega, dt):
@@ -912,7 +912,7 @@ def phase_sample(abi, w, params, s, state, omega, dt):
     measured handle, its graph and its trajectory are left as they are."""
     with abi.System(w["n"], params) as c:
         if params.neighbour == abi.NEIGHBOUR_CELL:
-            for key in (abi.TUNE_SPARSE_BELOW, abi.TUNE_TILE_SPLIT, abi.TUNE_HEAVY_UNITS):
+            for key in (abi.TUNE_SPARSE_BELOW, abi.TUNE_TILE_SPLIT, abi.TUNE_CELL_UNITS):
                 c.set_tuning(key, s.get_tuning(key))
         c.upload_omega(omega)
         c.upload_state(state)
@@ -1071,9 +1071,9 @@ def main():
     ap.add_argument("--skin", type=float, default=None)
     ap.add_argument("--tile-split", type=int, default=None,
                     help="--form: CTAs per cell of the cell-tile passes (0: the default, 1)")
-    ap.add_argument("--heavy-units", type=int, choices=[0, 1], default=None,
-                    help="--form / --ncu-case (FP32C, FP32X): run heavy cells as units in a second "
-                         "launch of each pass (SPC_TUNE_HEAVY_UNITS)")
+    ap.add_argument("--cell-units", type=int, choices=[0, 1], default=None,
+                    help="--form / --ncu-case (FP32C, FP32X): run the cells as units of 32 particles x "
+                         "one staging round in a second launch of each pass (SPC_TUNE_CELL_UNITS)")
     ap.add_argument("--save-final-states", default=None,
                     help="headline run: write each form's state after the whole run to "
                          "<dir>/final_state_<form>.npz")
@@ -1283,8 +1283,8 @@ def main():
                     s.set_tuning(abi.TUNE_SPARSE_BELOW, args.sparse_below)
                 if args.tile_split is not None:
                     s.set_tuning(abi.TUNE_TILE_SPLIT, args.tile_split)
-                if args.heavy_units is not None:
-                    s.set_tuning(abi.TUNE_HEAVY_UNITS, args.heavy_units)
+                if args.cell_units is not None:
+                    s.set_tuning(abi.TUNE_CELL_UNITS, args.cell_units)
             s.upload_state(st)
             s.upload_omega(omega)
             s.step(w["dt"], 3)
@@ -1337,7 +1337,7 @@ def main():
             p.skin = args.skin
         ms, e2e_ms, prof, _, launches = run_form(abi, torch, w, prec, args.steps, args.warmup,
                                                  rank, dist, p, tile_split=args.tile_split,
-                                                 heavy_units=args.heavy_units)
+                                                 cell_units=args.cell_units)
         if rank == 0:
             print(json.dumps({"form": args.form, "neighbour": args.neighbour, "skin": p.skin,
                               "tile_split": args.tile_split,
@@ -1387,7 +1387,7 @@ def main():
     best, tun, _ = tuned[head]
     ms_w, _, _, _, _ = run_form(abi, torch, w, dict(forms)[head], args.steps, args.warmup, rank,
                                 dist, best, tun["sparse_below"], e2e=False,
-                                tile_split=tun["tile_split"], heavy_units=tun["heavy_units"])
+                                tile_split=tun["tile_split"], cell_units=tun["cell_units"])
     hbm, peak_kind = peaks()
     # per-phase launch durations averaged over the run: a CUDA-event profile
     # after each bench step (on a copy of the state, outside the timers)

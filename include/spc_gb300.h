@@ -107,7 +107,7 @@ typedef struct spc_params {
 typedef struct spc_handle spc_handle;
 
 /* Library / version.  SPC_ABI_VERSION changes with any layout change of the
- * structs above or below (3: spc_tuning gained heavy_units). */
+ * structs above or below (3: spc_tuning gained cell_units). */
 int spc_abi_version(void);
 const char *spc_last_error(const spc_handle *h); /* h may be NULL: last global error */
 
@@ -237,16 +237,17 @@ int spc_profile_steps(spc_handle *h, double dt, int32_t nsteps, double *out_ms, 
  * on one CTA and only cells that hold several groups (a clustered state) are
  * spread out.  spc_get_tuning returns the split in effect.  Results are
  * bitwise independent of it in every precision.
- * SPC_TUNE_HEAVY_UNITS (FP32C and FP32X handles): 1 runs the heavy cells of
- * the cell-tile passes as units of 32 particles x one staging round of their
- * candidate list, each unit on its own CTA in a second launch of the pass; 0
- * (the default) runs them as whole particle groups.  A heavy cell has more
- * than 65,536 pair tests (particles x candidates) and at most 8 staging
- * rounds: the dense cells of a clustered state.  With 1, FP32X results are
- * unchanged (exact sums) and FP32C sums of heavy cells are added in another
- * fixed order; either way they do not depend on SPC_TUNE_TILE_SPLIT.
+ * SPC_TUNE_CELL_UNITS (FP32C and FP32X handles): 1 runs the cells of the
+ * cell-tile passes as units of 32 particles x one staging round of their
+ * candidate list (cells of more than 8 staging rounds stay whole particle
+ * groups), each unit on its own CTA in a second launch of each pass, beside
+ * the cell-tile kernel; 0 (the default) runs every cell as whole particle
+ * groups.  It pays on clustered states, where whole groups leave most SMs
+ * idle at the end of a pass.  With 1, FP32X results are unchanged (exact
+ * sums) and FP32C sums are added in another fixed order; either way they do
+ * not depend on SPC_TUNE_TILE_SPLIT.  Refused for FP64 handles.
  * spc_get_tuning reads a knob back. */
-enum { SPC_TUNE_SPARSE_BELOW = 1, SPC_TUNE_VERLET_ROW_LIMIT = 2, SPC_TUNE_TILE_SPLIT = 3, SPC_TUNE_HEAVY_UNITS = 4 };
+enum { SPC_TUNE_SPARSE_BELOW = 1, SPC_TUNE_VERLET_ROW_LIMIT = 2, SPC_TUNE_TILE_SPLIT = 3, SPC_TUNE_CELL_UNITS = 4 };
 int spc_set_tuning(spc_handle *h, int32_t key, double value);
 int spc_get_tuning(const spc_handle *h, int32_t key, double *value);
 
@@ -263,7 +264,7 @@ int spc_get_tuning(const spc_handle *h, int32_t key, double *value);
  * *count the number of candidates.  The caller's state is not touched. */
 /* One tuning candidate and its measured cost (no counterpart in the
  * reference): the neighbour method and skin, the SPC_TUNE_SPARSE_BELOW,
- * SPC_TUNE_TILE_SPLIT and SPC_TUNE_HEAVY_UNITS values, and milliseconds per
+ * SPC_TUNE_TILE_SPLIT and SPC_TUNE_CELL_UNITS values, and milliseconds per
  * step. */
 typedef struct spc_tuning {
   int32_t neighbour;    /* SPC_NEIGHBOUR_* */
@@ -271,7 +272,7 @@ typedef struct spc_tuning {
   double skin;          /* Verlet skin (0 for the cell list) */
   double sparse_below;  /* SPC_TUNE_SPARSE_BELOW value */
   double ms_per_step;   /* measured */
-  int32_t heavy_units;  /* SPC_TUNE_HEAVY_UNITS value */
+  int32_t cell_units;  /* SPC_TUNE_CELL_UNITS value */
 } spc_tuning;
 
 /* Autotuner over every tuning dimension (no counterpart in the reference):

@@ -179,7 +179,7 @@ struct SysHost {
 struct Engine {
   int stepper = 0, precision = 0, device = 0;
   cudaStream_t stream = nullptr;
-  // heavy units: the units kernel runs on `side`, forked from and joined back
+  // cell units: the units kernel runs on `side`, forked from and joined back
   // to `stream`, beside the cell-tile kernel (float forms)
   cudaStream_t side = nullptr;
   cudaEvent_t fork_ev = nullptr, join_ev = nullptr;
@@ -216,10 +216,10 @@ struct Engine {
   double sparse_below = kSparseBelowDefault;
   // tuning: CTAs per cell of the cell-tile kernels (0: chosen per layout)
   int tile_split_tune = 0;
-  // tuning: heavy cells of the float cell-tile passes run as units (1) or as
+  // tuning: the cells of the float cell-tile passes run as units (1) or as
   // whole groups (0)
-  int heavy_units_tune = 0;
-  // the heavy-unit buffers (float forms; allocated at init)
+  int cell_units_tune = 0;
+  // the cell-unit buffers (float forms; allocated at init)
   int2 *units_buf = nullptr;
   std::vector<int> slot_layout;  // slot -> layout index (-1 if inactive)
   // noise injection (single-system handles)
@@ -324,13 +324,13 @@ inline void engine_footprint(int stepper, int precision, long long *per_particle
   if (precision == SPC_PRECISION_FP32C) b += 8 + 4 + (long long)kMaskWords * 4;  // cs, dphi_f, masks
   if (precision == SPC_PRECISION_FP32X)
     b += 16 + 16 + 8 + 16 + 4 + (long long)kMaskWords * 4;  // ics, iws, scos, xsum, xcnt, masks
-  if (precision != SPC_PRECISION_FP64)  // heavy units: round sums, counts, chunk counters, list
+  if (precision != SPC_PRECISION_FP64)  // cell units: round sums, counts, chunk counters, list
     b += kSplitRounds * ((precision == SPC_PRECISION_FP32X ? 16 : 8) + 4) + 4 + kSplitRounds * 8 / 32;
   if (precision == SPC_PRECISION_FP64) b += 8 + 8 + 4;                          // vortex-arrays outputs
   b += 12 * 8 + 4 + 4;                       // AoS staging, histogram share
   *per_particle = b;
   *per_cell = 4 + 4 + (precision != SPC_PRECISION_FP64 ? kSplitRounds * 8 + 1 : 0);  // cell_start,
-                                                                      // sys_of_c, heavy-unit list and flag
+                                                                      // sys_of_c, unit list and flag
 }
 
 inline int engine_init(Engine *e, int stepper, int precision, int pool_cap, int sys_cap, int cell_cap) {
@@ -395,11 +395,11 @@ inline int engine_init(Engine *e, int stepper, int precision, int pool_cap, int 
     SPC_TRY(dalloc(e, &a.part_x, (size_t)kSplitRounds * N));
   }
   if (precision != SPC_PRECISION_FP64) {
-    // a heavy cell of n_c particles lists ceil(n_c / 32) x (at most
+    // a unit cell of n_c particles lists ceil(n_c / 32) x (at most
     // kSplitRounds) units, so (N / 32 + cells) x kSplitRounds entries hold any layout
     SPC_TRY(dalloc(e, &e->units_buf, ((N + kWarp - 1) / kWarp + (size_t)cell_cap) * kSplitRounds));
     SPC_TRY(dalloc(e, &a.unit_count, 1));
-    SPC_TRY(dalloc(e, &a.cell_heavy, (size_t)cell_cap));
+    SPC_TRY(dalloc(e, &a.cell_unit, (size_t)cell_cap));
     SPC_TRY(dalloc(e, &a.part_n, (size_t)kSplitRounds * N));
     SPC_TRY(dalloc(e, &a.unit_done, N));
     SPC_CUDA(e, cudaStreamCreateWithFlags(&e->side, cudaStreamNonBlocking));
@@ -738,7 +738,7 @@ inline int engine_layout(Engine *e) {
   a.ncell_total = e->ncell_total;
   a.ncell_tile = e->ncell_tile;
   a.tile_split = tile_split_for(e->tile_split_tune);
-  a.units = e->heavy_units_tune ? e->units_buf : nullptr;
+  a.units = e->cell_units_tune ? e->units_buf : nullptr;
   a.va_c0 = e->ncell_tile + e->ncell_warp;
   a.va_c1 = a.va_c0 + e->ncell_va;
   a.n_ap = (int)ap.size();
@@ -850,7 +850,7 @@ inline int eval_cells(Engine *e, KArgs &a, int rk_form, int kq, double kcdt, boo
   else
     k_gather<kPrecFP64><<<blocks_for(n + 1, 256), 256, 0, st>>>(a);
   SPC_LAUNCHED(e);
-  if (a.units && e->ncell_tile > 0 && !e->verlet) {  // the heavy cells' units of this evaluation
+  if (a.units && e->ncell_tile > 0 && !e->verlet) {  // the cell units of this evaluation
     if (e->precision == SPC_PRECISION_FP32C)
       k_list_units<kTileCap><<<blocks_for(e->ncell_tile, 128), 128, 0, st>>>(a);
     else
@@ -917,7 +917,7 @@ int launch_pass_t(Engine *e, const KArgs &a, int epi) {
         const int grid = std::min(e->ncell_tile * std::max(a.tile_split, 1), 152 * 256);
         if constexpr ((PREC == kPrecFP32C || PREC == kPrecFP32X) && KIND != kKindNb) {
           if (a.units) {
-            // the heavy cells' units (listed after the gather) run beside the
+            // the cell units (listed after the gather) run beside the
             // cell-tile kernel, each filling the SMs the other leaves idle.
             // One CTA per unit up to 16 per SM (CTAs past the unit count
             // return at once, a larger count is taken in turn): measured
@@ -1114,12 +1114,12 @@ inline int engine_set_tuning(Engine *e, int key, double value) {
     drop_graph(e);
     return SPC_OK;
   }
-  if (key == SPC_TUNE_HEAVY_UNITS) {
-    if (value != 0.0 && value != 1.0) return fail(e, SPC_ERR_INVALID, "heavy units must be 0 or 1");
+  if (key == SPC_TUNE_CELL_UNITS) {
+    if (value != 0.0 && value != 1.0) return fail(e, SPC_ERR_INVALID, "cell units must be 0 or 1");
     if (value == 1.0 && e->precision == SPC_PRECISION_FP64)
-      return fail(e, SPC_ERR_INVALID, "heavy units apply to the FP32C and FP32X cell-tile passes");
-    if ((int)value != e->heavy_units_tune) {
-      e->heavy_units_tune = (int)value;
+      return fail(e, SPC_ERR_INVALID, "cell units apply to the FP32C and FP32X cell-tile passes");
+    if ((int)value != e->cell_units_tune) {
+      e->cell_units_tune = (int)value;
       e->dirty = true;
     }
     return SPC_OK;
@@ -1153,8 +1153,8 @@ inline int engine_get_tuning(const Engine *e, int key, double *value) {
     *value = e->sparse_below;
     return SPC_OK;
   }
-  if (key == SPC_TUNE_HEAVY_UNITS) {
-    *value = (double)e->heavy_units_tune;
+  if (key == SPC_TUNE_CELL_UNITS) {
+    *value = (double)e->cell_units_tune;
     return SPC_OK;
   }
   if (key == SPC_TUNE_TILE_SPLIT) {  // the split in effect
@@ -1170,10 +1170,10 @@ inline int engine_get_tuning(const Engine *e, int key, double *value) {
 struct TuneCand {
   double sparse;
   int split;
-  int heavy;
+  int units;
 };
 
-// The kernel-choice candidates; heavy units (float forms) with one and two
+// The kernel-choice candidates; cell units (float forms) with one and two
 // CTAs per cell.
 inline std::vector<TuneCand> kernel_candidates(int precision) {
   std::vector<TuneCand> c;
@@ -1201,7 +1201,7 @@ inline int engine_retune(Engine *e, double dt, int trial, spc_tuning *out, int c
   SPC_TRY(engine_set_device(e));
   SPC_TRY(engine_layout(e));
   std::vector<TuneCand> cands = e->verlet ? std::vector<TuneCand>{{e->sparse_below, e->tile_split_tune,
-                                                                    e->heavy_units_tune}}
+                                                                    e->cell_units_tune}}
                                           : kernel_candidates(e->precision);
   const size_t P = (size_t)e->pool_cap;
   std::vector<double *> live = {e->a.x, e->a.y, e->a.phi};
@@ -1233,7 +1233,7 @@ inline int engine_retune(Engine *e, double dt, int trial, spc_tuning *out, int c
     return SPC_OK;
   };
   const double sb0 = e->sparse_below;
-  const int split0 = e->tile_split_tune, heavy0 = e->heavy_units_tune;
+  const int split0 = e->tile_split_tune, units0 = e->cell_units_tune;
   cudaEvent_t ev[2] = {nullptr, nullptr};
   cudaError_t ce = copy_all(true);
   if (ce == cudaSuccess) ce = cudaEventCreate(&ev[0]);
@@ -1244,7 +1244,7 @@ inline int engine_retune(Engine *e, double dt, int trial, spc_tuning *out, int c
   for (size_t k = 0; k < cands.size() && rc == SPC_OK; ++k) {
     e->sparse_below = cands[k].sparse;
     e->tile_split_tune = cands[k].split;
-    e->heavy_units_tune = cands[k].heavy;
+    e->cell_units_tune = cands[k].units;
     e->dirty = true;
     rc = engine_steps(e, dt, trial, false, nullptr, 0);
     if (rc == SPC_OK) rc = restore();
@@ -1264,7 +1264,7 @@ inline int engine_retune(Engine *e, double dt, int trial, spc_tuning *out, int c
       out[k].skin = 0.0;
       out[k].sparse_below = cands[k].sparse;
       out[k].ms_per_step = per;
-      out[k].heavy_units = cands[k].heavy;
+      out[k].cell_units = cands[k].units;
     }
     if (rc == SPC_OK && per < best_ms) {
       best_ms = per;
@@ -1278,13 +1278,13 @@ inline int engine_retune(Engine *e, double dt, int trial, spc_tuning *out, int c
   if (rc != SPC_OK) {  // keep the caller's settings
     e->sparse_below = sb0;
     e->tile_split_tune = split0;
-    e->heavy_units_tune = heavy0;
+    e->cell_units_tune = units0;
     e->dirty = true;
     return rc;
   }
   e->sparse_below = cands[best_k].sparse;
   e->tile_split_tune = cands[best_k].split;
-  e->heavy_units_tune = cands[best_k].heavy;
+  e->cell_units_tune = cands[best_k].units;
   e->dirty = true;
   if (count) *count = (int)cands.size();
   if (best) *best = best_k;

@@ -97,15 +97,15 @@ struct KArgs {
   double *va_vx, *va_vy;             // vortex arrays: pass-1 velocity components, cell order
   int *va_cnt2;                      // vortex arrays: cohesion partners, cell order
   uint32_t *nbmask;                  // FP32C: pass-1 neighbour bitmasks (mask_at), or null
-  // Heavy cells of the float cell-tile passes (SPC_TUNE_HEAVY_UNITS; units
-  // null when off): the units the cell-tile kernel lists for the units kernel
+  // Cell units of the float cell-tile passes (SPC_TUNE_CELL_UNITS; units
+  // null when off): the units k_list_units lists for the units kernel
   // (cell, unit), their count (zeroed by k_gather), per staging
   // round r and cell-order slot p at [r * n_active + p] a unit's sums (FP32C:
   // float pair, FP32X: fixed-point pair) and counts, and a completion counter
   // per 32-particle chunk, indexed by its first slot (zero between launches).
   int2 *units;
   int *unit_count;
-  uint8_t *cell_heavy;  // per cell-tile cell: 1 if heavy (written with the list)
+  uint8_t *cell_unit;  // per cell-tile cell: 1 if it runs as units (written with the list)
   float2 *part_f;
   longlong2 *part_x;
   int *part_n;
@@ -228,7 +228,7 @@ __global__ void k_gather(KArgs a) {
   // leave the first-digit histogram table zero for the next stage kernel
   for (int k = p; k < a.hist_len; k += n + 1) a.hist[k] = 0u;
   if (p == n) {
-    if (a.unit_count) *a.unit_count = 0;  // this evaluation's heavy units (k_list_units)
+    if (a.unit_count) *a.unit_count = 0;  // this evaluation's cell units (k_list_units)
     return;
   }
   const int d = (int)a.svals[p];

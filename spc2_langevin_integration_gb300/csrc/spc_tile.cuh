@@ -328,54 +328,53 @@ __device__ __forceinline__ void finish_fp32c(const KArgs &a, int epi, const SysD
   epilogue<kPrecFP32C, KIND>(a, epi, sd, il, acc, a.pidx[p]);
 }
 
-// Heavy cells (tuning SPC_TUNE_HEAVY_UNITS).  A cell whose pair tests
-// (particles x stencil candidates) exceed kHeavyTests, about 1.8 times those
-// of a cell of a uniform 64-per-cell state (64 x 576), and whose list takes
-// at most kSplitRounds staging rounds is not run by the cell-tile kernel: it is
-// cut into units of 32 particles x one staging round, and the units kernel
-// launched after the cell-tile kernel runs every unit on its own CTA.  Cells
-// of a clustered state reach ~6,000 candidates for ~380 particles; as whole
-// 128-particle groups on one CTA each they ran for several times a typical
-// cell and set the end of the single-wave pass.  A unit's four warps take a
+// Cell units (tuning SPC_TUNE_CELL_UNITS).  Every cell whose candidate list
+// takes at most kSplitRounds staging rounds is cut into units of 32 particles
+// x one staging round, and the units kernel runs each unit on its own CTA,
+// beside the cell-tile kernel, which keeps only the cells of longer lists.
+// On a clustered state the cell-tile kernel's one CTA per 128-particle group
+// is badly balanced: a cell of a cluster holds up to ~380 particles with
+// ~6,000 candidates, several times a typical cell's work, and its groups set
+// the end of the single-wave pass while most SMs idle.  Units of ~32 x 1,024
+// pair tests spread that work over every SM.  A unit's four warps take a
 // quarter of its round each; the unit stores its per-particle sums of the
 // round, and the last unit of a 32-particle chunk to finish (a counter per
 // chunk, reset by that unit) adds the rounds in order and finishes the
 // particles.  k_list_units lists the units once per evaluation (both passes
-// see the same cells).  Which cells are heavy, and the order of every sum, depend on
-// the cell alone, so the results do not depend on the CTAs per cell.
-constexpr int kHeavyTests = 65536;
+// see the same cells).  Which cells are units, and the order of every sum,
+// depend on the cell alone, so the results do not depend on the CTAs per cell.
 constexpr int kSplitRounds = 8;
 
-__device__ __forceinline__ bool heavy_cell(const KArgs &a, int n_c, int total, int cap) {
-  return a.units != nullptr && (long long)n_c * total > kHeavyTests && total <= kSplitRounds * cap;
+__device__ __forceinline__ bool unit_cell(const KArgs &a, int n_c, int total, int cap) {
+  return a.units != nullptr && n_c > 0 && total <= kSplitRounds * cap;
 }
 
-// List the units of every heavy cell of the cell-tile systems (one thread per
+// List the units of every unit cell of the cell-tile systems (one thread per
 // cell), once per evaluation after the gather, for both passes' units kernels,
-// and mark the heavy cells for the cell-tile kernels to skip.
+// and mark those cells for the cell-tile kernels to skip.
 // CAP: the form's staging round.
 template <int CAP>
 __global__ void k_list_units(KArgs a) {
   const int c = blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= a.ncell_tile) return;
   const int c0 = a.cell_start[c], n_c = a.cell_start[c + 1] - c0;
-  a.cell_heavy[c] = 0;
+  a.cell_unit[c] = 0;
   if (n_c == 0) return;
   const SysDesc &sd = a.sys[a.sys_of_c[c]];
   if (sd.sc.allpairs) return;
   Stencil st;
   stencil_of(a, sd, c, st);
   const int total = st.prefix[9];
-  if (!heavy_cell(a, n_c, total, CAP)) return;
-  a.cell_heavy[c] = 1;
+  if (!unit_cell(a, n_c, total, CAP)) return;
+  a.cell_unit[c] = 1;
   const int rounds = (total + CAP - 1) / CAP;
   const int units = (n_c + kWarp - 1) / kWarp * rounds;
   const int base = atomicAdd(a.unit_count, units);
   for (int u = 0; u < units; ++u) a.units[base + u] = make_int2(c, u);
 }
 
-// UNITS: heavy cells are left to the units kernel (a separate instantiation, so
-// that the kernel without heavy units compiles exactly as before).
+// UNITS: unit cells are left to the units kernel (a separate instantiation, so
+// that the kernel without cell units compiles exactly as before).
 template <int KIND, bool UNITS>
 __global__ void __launch_bounds__(kTileThreads32, kTileMinBlocks32) k_tile_fp32c(KArgs a, int epi) {
   __shared__ float4 s_c4[kTileCap];   // x+shift, y+shift, cos phi, sin phi (padded to 32)
@@ -391,7 +390,7 @@ __global__ void __launch_bounds__(kTileThreads32, kTileMinBlocks32) k_tile_fp32c
     TileItem ti;
     if (!tile_item<kTileThreads32>(a, item, ti)) continue;
     if constexpr (UNITS) {
-      if (a.cell_heavy[ti.c]) continue;  // run by the units kernel
+      if (a.cell_unit[ti.c]) continue;  // run by the units kernel
     }
     const int c = ti.c, c0 = ti.c0, cb = ti.cb, ce = ti.ce;
     const SysDesc &sd = a.sys[a.sys_of_c[c]];
@@ -590,7 +589,7 @@ __global__ void __launch_bounds__(kTileThreads32, kTileMinBlocks32) k_tile_fp32c
   }
 }
 
-// The heavy units of an FP32C pass (listed by k_tile_fp32c of the same pass):
+// The units of an FP32C pass (listed by k_list_units after the gather):
 // unit u of cell c is chunk u / rounds (32 particles) x staging round
 // u % rounds, its list split among the four warps.
 template <int KIND>
@@ -809,8 +808,8 @@ __device__ __forceinline__ void part_fp32x(const KArgs &a, const SysConst &sc, c
   }
 }
 
-// UNITS: heavy cells are left to the units kernel (a separate instantiation, so
-// that the kernel without heavy units compiles exactly as before).
+// UNITS: unit cells are left to the units kernel (a separate instantiation, so
+// that the kernel without cell units compiles exactly as before).
 template <int KIND, bool UNITS>
 __global__ void __launch_bounds__(kTileThreads32, kTileMinBlocks32) k_tile_fp32x(KArgs a, int epi) {
   __shared__ float2 s_xy[kTileCapX];     // x+shift, y+shift (padded to 32)
@@ -823,7 +822,7 @@ __global__ void __launch_bounds__(kTileThreads32, kTileMinBlocks32) k_tile_fp32x
     TileItem ti;
     if (!tile_item<kTileThreads32>(a, item, ti)) continue;
     if constexpr (UNITS) {
-      if (a.cell_heavy[ti.c]) continue;  // run by the units kernel
+      if (a.cell_unit[ti.c]) continue;  // run by the units kernel
     }
     const int c = ti.c, c0 = ti.c0, cb = ti.cb, ce = ti.ce;
     const SysDesc &sd = a.sys[a.sys_of_c[c]];
@@ -970,7 +969,7 @@ __global__ void __launch_bounds__(kTileThreads32, kTileMinBlocks32) k_tile_fp32x
   }
 }
 
-// The heavy units of an FP32X pass (listed by k_tile_fp32x of the same pass),
+// The units of an FP32X pass (listed by k_list_units after the gather),
 // as k_units_fp32c.  A unit's round sums are exact 64-bit integers (below
 // 2^62: kTileCapX candidates of |v| <= 2^52), added over the rounds in 128
 // bits, so the particle's sums are those of the whole-group path.

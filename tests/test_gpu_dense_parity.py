@@ -18,8 +18,8 @@ sums, :429-645 for the SRK form):
 * SRK-form right-hand sides (derivative and additional derivative) within
   1e-12 of the oracle's on the scale rule, for FP64 cell-tile, warp-per-cell
   and Verlet rows and for FP32X; FP32C within its 2e-6 bound; the float
-  cell-tile kernels also with heavy units (the patch and clustered states'
-  dense cells run as units of 32 particles x one staging round);
+  cell-tile kernels also with cell units (cells run as units of 32
+  particles x one staging round);
 * 10 SRK steps under the library's Philox noise (the exported normals fed to
   the oracle) within 1e-9 for the same FP64 and FP32X variants.
 """
@@ -81,13 +81,13 @@ def _state(name):
 
 
 def _system(n, L, prm, variant, st, omega, seed=5):
-    prec, nb, sb, heavy = VARIANTS[variant]
+    prec, nb, sb, units = VARIANTS[variant]
     s = abi.System(n, abi.make_params(L=L, stepper=abi.STEPPER_SRK, model=abi.MODEL_VORTEX,
                                       precision=prec, neighbour=nb, skin=0.05, seed=seed, **prm))
     if sb is not None:
         s.set_tuning(abi.TUNE_SPARSE_BELOW, sb)
-    if heavy:
-        s.set_tuning(abi.TUNE_HEAVY_UNITS, 1)
+    if units:
+        s.set_tuning(abi.TUNE_CELL_UNITS, 1)
     s.upload_state(st)
     s.upload_omega(omega)
     return s

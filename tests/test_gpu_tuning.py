@@ -2,11 +2,11 @@
 
 * spc_autotune_ex offers every tuning dimension: the kernel choice (all
   cell-tile, the default split, all warp-per-cell), 1, 2 or 4 CTAs per cell,
-  heavy cells as units (float forms), and Verlet skins where the precision
+  cell units (float forms), and Verlet skins where the precision
   and stencil allow them.
 * Every kernel-choice candidate computes the same neighbour sets: FP64 and
   FP32X trajectories are bit for bit the same under each of them, and FP32C
-  ones under every CTA split (with heavy units off, and with them on).
+  ones under every CTA split (with cell units off, and with them on).
 * spc_retune / spc_batch_retune leave the state and the step counters as they
   were, so a run that retunes midway equals one that does not, bit for bit.
 """
@@ -34,12 +34,12 @@ def test_autotune_ex_offers_every_dimension():
     assert {c["sparse_below"] for c in cell} >= {0.0, 1e9}
     assert any(c["neighbour"] == "verlet" for c in cands)
     assert 0 <= best < len(cands) and all(c["ms_per_step"] > 0 for c in cands)
-    assert {c["heavy_units"] for c in cands} == {0}  # FP64 has no heavy units
-    # FP32X runs the cell list only, with and without heavy units
+    assert {c["cell_units"] for c in cands} == {0}  # FP64 has no cell units
+    # FP32X runs the cell list only, with and without cell units
     cx, _ = abi.autotune_ex(N, _params(abi.PRECISION_FP32X), st, trial_steps=5)
     assert all(c["neighbour"] == "cell" for c in cx)
-    assert len([c for c in cx if c["heavy_units"] == 0]) == len(cell)
-    assert {(c["sparse_below"], c["tile_split"]) for c in cx if c["heavy_units"] == 1} == \
+    assert len([c for c in cx if c["cell_units"] == 0]) == len(cell)
+    assert {(c["sparse_below"], c["tile_split"]) for c in cx if c["cell_units"] == 1} == \
         {(0.0, 1), (0.0, 2), (24.0, 1), (24.0, 2)}
 
 
@@ -48,13 +48,14 @@ def test_autotune_ex_offers_every_dimension():
     (abi.PRECISION_FP32X, 9000, 0.2), (abi.PRECISION_FP32C, 9000, 0.2)])
 def test_kernel_choices_give_identical_trajectories(precision, n, patch):
     """FP64 and FP32X: every kernel choice; FP32C: every CTA split of the
-    cell-tile kernels, with heavy units off and on (its cell-tile and
-    warp-per-cell kernels, and heavy units, sum in different orders).  The
+    cell-tile kernels, with cell units off and on (its cell-tile and
+    warp-per-cell kernels, and cell units, sum in different orders).  The
     particles are clustered into a patch so that cells hold several particle
     groups and the splits really spread them.  6,000 in a 0.45 x 0.45 patch
-    give heavy cells of ~4,200 candidates; 9,000 in a 0.2 x 0.2 patch share
-    one stencil, more staging rounds than a heavy cell may have, so those
-    cells stay whole groups with heavy units on."""
+    give cells of ~4,200 candidates, which cell units cut into units of 32
+    particles x one staging round; 9,000 in a 0.2 x 0.2 patch share one
+    stencil, more staging rounds than a cell may be cut into, so those cells
+    stay whole groups with cell units on."""
     rng = np.random.default_rng(91)
     st = init_state(n, L, 91)
     st[0::3] = 0.2 + patch * rng.random(n)
@@ -66,11 +67,11 @@ def test_kernel_choices_give_identical_trajectories(precision, n, patch):
         choices = [choices[0][:3], ((0.0, 1, 1), (0.0, 2, 1), (0.0, 4, 1))]
     for group in choices:
         out = []
-        for sb, split, heavy in group:
+        for sb, split, units in group:
             with abi.System(n, _params(precision)) as s:
                 s.set_tuning(abi.TUNE_SPARSE_BELOW, sb)
                 s.set_tuning(abi.TUNE_TILE_SPLIT, split)
-                s.set_tuning(abi.TUNE_HEAVY_UNITS, heavy)
+                s.set_tuning(abi.TUNE_CELL_UNITS, units)
                 s.upload_state(st)
                 s.step(0.005, 30 if n == N else 10)
                 out.append(s.download_state())
@@ -93,7 +94,7 @@ def test_retune_midway_leaves_the_run_unchanged(precision):
                 assert len(cands) == nc and 0 <= best < nc
                 assert np.array_equal(s.download_state(), before) and s.step_counter == ctr
                 assert s.get_tuning(abi.TUNE_TILE_SPLIT) == cands[best]["tile_split"]
-                assert s.get_tuning(abi.TUNE_HEAVY_UNITS) == cands[best]["heavy_units"]
+                assert s.get_tuning(abi.TUNE_CELL_UNITS) == cands[best]["cell_units"]
                 s.prepare_graph(0.005, 20)  # captured, not run: state and counter unchanged
                 assert s.graph_nodes() > 0
                 assert np.array_equal(s.download_state(), before) and s.step_counter == ctr
@@ -130,35 +131,35 @@ def test_batch_retune_leaves_the_run_unchanged():
 
 
 @pytest.mark.parametrize("precision", [abi.PRECISION_FP32X, abi.PRECISION_FP32C])
-def test_heavy_units_graph_equals_eager(precision):
-    """With heavy units the units kernel runs on a second stream beside the
+def test_cell_units_graph_equals_eager(precision):
+    """With cell units the units kernel runs on a second stream beside the
     cell-tile kernel (parallel branches of the step graph): captured graph
     replays and eager steps give the same bits, and FP32X gives the bits of
-    the run without heavy units."""
+    the run without cell units."""
     rng = np.random.default_rng(94)
     st = init_state(N, L, 94)
     st[0::3] = 0.2 + 0.45 * rng.random(N)
     st[1::3] = 0.2 + 0.45 * rng.random(N)
     out = {}
-    for heavy, graph in ((1, False), (1, True), (0, False)):
+    for units, graph in ((1, False), (1, True), (0, False)):
         with abi.System(N, _params(precision)) as s:
             s.set_tuning(abi.TUNE_SPARSE_BELOW, 0.0)
-            s.set_tuning(abi.TUNE_HEAVY_UNITS, heavy)
-            assert s.get_tuning(abi.TUNE_HEAVY_UNITS) == heavy
+            s.set_tuning(abi.TUNE_CELL_UNITS, units)
+            assert s.get_tuning(abi.TUNE_CELL_UNITS) == units
             s.upload_state(st)
             for _ in range(3):
                 s.step(0.005, 10, graph=graph)
-            out[(heavy, graph)] = s.download_state()
+            out[(units, graph)] = s.download_state()
     assert np.array_equal(out[(1, False)], out[(1, True)])
     if precision == abi.PRECISION_FP32X:
         assert np.array_equal(out[(1, False)], out[(0, False)])
 
 
-def test_heavy_units_refused_for_fp64():
+def test_cell_units_refused_for_fp64():
     with abi.System(N, _params(abi.PRECISION_FP64)) as s:
         with pytest.raises(abi.SpcError):
-            s.set_tuning(abi.TUNE_HEAVY_UNITS, 1)
+            s.set_tuning(abi.TUNE_CELL_UNITS, 1)
         for bad in (-1.0, 2.0, 0.5):
             with pytest.raises(abi.SpcError):
-                s.set_tuning(abi.TUNE_HEAVY_UNITS, bad)
-        s.set_tuning(abi.TUNE_HEAVY_UNITS, 0)
+                s.set_tuning(abi.TUNE_CELL_UNITS, bad)
+        s.set_tuning(abi.TUNE_CELL_UNITS, 0)
