@@ -163,3 +163,22 @@ def test_cell_units_refused_for_fp64():
             with pytest.raises(abi.SpcError):
                 s.set_tuning(abi.TUNE_CELL_UNITS, bad)
         s.set_tuning(abi.TUNE_CELL_UNITS, 0)
+
+
+@pytest.mark.parametrize("stepper", [abi.STEPPER_RK4, abi.STEPPER_EULER])
+def test_cell_units_fp32x_other_steppers_bitwise(stepper):
+    """The units kernel serves every evaluation of a step (RK4's four, Euler's
+    one): FP32X with cell units gives the bits of the run without them."""
+    rng = np.random.default_rng(95)
+    st = init_state(N, L, 95)
+    st[0::3] = 0.2 + 0.45 * rng.random(N)
+    st[1::3] = 0.2 + 0.45 * rng.random(N)
+    out = []
+    for units in (0, 1):
+        with abi.System(N, _params(abi.PRECISION_FP32X, stepper)) as s:
+            s.set_tuning(abi.TUNE_SPARSE_BELOW, 0.0)
+            s.set_tuning(abi.TUNE_CELL_UNITS, units)
+            s.upload_state(st)
+            s.step(0.005, 12, graph=True)
+            out.append(s.download_state())
+    assert np.array_equal(out[0], out[1])
