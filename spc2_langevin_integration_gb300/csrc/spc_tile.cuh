@@ -159,7 +159,10 @@ __device__ __forceinline__ void block32(const float4 *__restrict__ s_c4, const f
 }
 
 // Stage candidates [rlo, rlo + rcnt) of the stencil list (padded to rpad) for
-// the FP32C passes.
+// the FP32C passes.  This and part_fp32c serve the units kernel; the cell-tile
+// kernel keeps the same code inline, as it was before the units existed (a
+// version of it that called these helpers compiled to more spills and ran
+// pass 1 slower).
 template <int KIND>
 __device__ __forceinline__ void stage_fp32c(const KArgs &a, const SysConst &sc, const Stencil &st, int rlo,
                                             int rcnt, int rpad, float4 *s_c4, float *s_d) {
@@ -404,7 +407,6 @@ __global__ void __launch_bounds__(kTileThreads32, kTileMinBlocks32) k_tile_fp32c
     const int total = st.prefix[9];
     const int rounds = (total + kTileCap - 1) / kTileCap;
     const bool masked = rounds == 1 && a.nbmask != nullptr && !exact_all;
-
     for (int ig = cb; ig < ce; ig += kTileThreads32) {
       const int gi = min(kTileThreads32, ce - ig);
       if (tid < gi) {
@@ -698,7 +700,8 @@ __device__ __forceinline__ void block32x(const float2 *__restrict__ s_xy, const 
 }
 
 // Stage candidates [rlo, rlo + rcnt) of the stencil list (padded to rpad) for
-// the FP32X passes.
+// the FP32X passes (with part_fp32x, for the units kernel; the cell-tile
+// kernel keeps the same code inline, as stage_fp32c says).
 template <int KIND>
 __device__ __forceinline__ void stage_fp32x(const KArgs &a, const SysConst &sc, const Stencil &st, int rlo,
                                             int rcnt, int rpad, float2 *s_xy, longlong2 *s_v) {
@@ -836,7 +839,6 @@ __global__ void __launch_bounds__(kTileThreads32, kTileMinBlocks32) k_tile_fp32x
     const int total = st.prefix[9];
     const int rounds = (total + kTileCapX - 1) / kTileCapX;
     const bool masked = rounds == 1 && a.nbmask != nullptr && !exact_all;
-
     for (int ig = cb; ig < ce; ig += kTileThreads32) {
       const int gi = min(kTileThreads32, ce - ig);
       // thread tid's particle (ig + tid): its sums over all rounds
