@@ -54,12 +54,15 @@ ALG_BYTES_STEP = 168 + 8      # survey accounting for the whole SRK step (+ omeg
 # counts both).
 PHASE_KERNELS = {
     "fp32c": {"stage": ["k_stage"], "sort": ["k_scan_digits", "k_radix_scatter"],
-              "gather": ["k_gather<1>"], "pass1": ["k_tile_fp32c<0>", "k_warp_fp32c<0>"],
-              "pass2": ["k_tile_fp32c<1>", "k_warp_fp32c<1>"]},
+              "gather": ["k_gather<1>", "k_list_units (cell units on)"],
+              "pass1": ["k_tile_fp32c<0>", "k_units_fp32c<0> (cell units on)", "k_warp_fp32c<0>"],
+              "pass2": ["k_tile_fp32c<1>", "k_units_fp32c<1> (cell units on)", "k_warp_fp32c<1>"]},
     "fp32x": {"stage": ["k_stage"], "sort": ["k_scan_digits", "k_radix_scatter"],
-              "gather": ["k_gather<2>"],
-              "pass1": ["k_tile_fp32x<0>", "k_warp_fp32x<0>", "k_epilogue_fp32x<0>"],
-              "pass2": ["k_tile_fp32x<1>", "k_warp_fp32x<1>", "k_epilogue_fp32x<1>"]},
+              "gather": ["k_gather<2>", "k_list_units (cell units on)"],
+              "pass1": ["k_tile_fp32x<0>", "k_units_fp32x<0> (cell units on)", "k_warp_fp32x<0>",
+                        "k_epilogue_fp32x<0>"],
+              "pass2": ["k_tile_fp32x<1>", "k_units_fp32x<1> (cell units on)", "k_warp_fp32x<1>",
+                        "k_epilogue_fp32x<1>"]},
     "fp64": {"stage": ["k_stage"], "sort": ["k_scan_digits", "k_radix_scatter"],
              "gather": ["k_gather<0>", "k_vgather<0>"], "pass1": ["k_vtile<0,0>", "k_tile_fp64<0>"],
              "pass2": ["k_vtile<0,1>", "k_tile_fp64<1>"]},
@@ -69,10 +72,14 @@ PHASE_KERNELS = {
 # summed over the phase's kernels; keyed by (form, phase).  FP32C pass 2 reads
 # the pass-1 neighbour masks (~3.5 MB here) on top of its algorithmic bytes.
 NCU_TRAFFIC = {
-    ("fp32c", "pass1"): {"bytes": 2.41e6, "state": "initial; the same at the clustered state"},
-    ("fp32c", "pass2"): {"bytes": 1.007e7, "state": "clustered (step 4,000, tests/golden/states)"},
-    ("fp32x", "pass1"): {"bytes": 5.59e6, "state": "initial (k_tile_fp32x<0> + k_epilogue_fp32x<0>)"},
-    ("fp32x", "pass2"): {"bytes": 1.398e7, "state": "initial (k_tile_fp32x<1> + k_epilogue_fp32x<1>)"},
+    ("fp32c", "pass1"): {"bytes": 2.53e6, "state": "clustered (step 4,000, tests/golden/states), "
+                                                  "cell units: k_units_fp32c<0> + k_tile_fp32c<0,1>"},
+    ("fp32c", "pass2"): {"bytes": 1.017e7, "state": "clustered, cell units: k_units_fp32c<1> + "
+                                                   "k_tile_fp32c<1,1>"},
+    ("fp32x", "pass1"): {"bytes": 5.83e6, "state": "clustered, cell units: k_units_fp32x<0> + "
+                                                  "k_tile_fp32x<0,1> + k_epilogue_fp32x<0>"},
+    ("fp32x", "pass2"): {"bytes": 1.257e7, "state": "clustered, cell units: k_units_fp32x<1> + "
+                                                   "k_tile_fp32x<1,1> + k_epilogue_fp32x<1>"},
 }
 
 
