@@ -944,13 +944,13 @@ def run_configured(abi, torch, w, precision, params, tuning, steps, warmup, rank
     `warmup` bench steps run first (graph capture, caches); then the state and
     the step counter are reset, so the timed steps are the configured run.
     After each bench step, outside the timers, the global and local order
-    parameters are recorded (the drift series), and a handle whose cost per
-    step has moved by more than 25% since its last tuning is tuned again on
-    the current, clustering state: a cell-list handle in place (spc_retune:
-    kernel choice and CTAs per cell; state and step counter are left as they
-    were), a Verlet-row handle by spc_autotune_ex over every method, moving
-    to a new handle (state, frequencies and step counter carried over) when
-    another method wins.  The step graph is captured again before the next
+    parameters are recorded (the drift series), and the handle is tuned again
+    on the current, clustering state: a cell-list handle after every bench
+    step, in place (spc_retune: kernel choice, CTAs per cell, cell units;
+    state and step counter are left as they were), a Verlet-row handle when
+    its cost per step has moved by more than 25% since its last tuning, by
+    spc_autotune_ex over every method, moving to a new handle (state,
+    frequencies and step counter carried over) when another method wins.  The step graph is captured again before the next
     bench step (spc_prepare_graph), so no capture falls inside the timers.
     sample_phases: after each bench step, also a phase profile and the
     neighbour work on a copy of the state (phase_sample), for the roofline
@@ -1005,9 +1005,13 @@ def run_configured(abi, torch, w, precision, params, tuning, steps, warmup, rank
         cost = ev[k][0].elapsed_time(ev[k][1]) / per
         if sample_phases:
             samples.append(phase_sample(abi, w, params, s, host, omega, dt))
-        if tuned_at is None:
+        # a cell-list handle retunes in place after every bench step (a few
+        # dozen eager steps, outside the timers); a Verlet-row handle, whose
+        # retune builds a handle per candidate, when its cost has moved by 25%
+        moved = tuned_at is not None and abs(cost - tuned_at) > 0.25 * tuned_at
+        if tuned_at is None and params.neighbour != abi.NEIGHBOUR_CELL:
             tuned_at = cost
-        elif abs(cost - tuned_at) > 0.25 * tuned_at and k + 1 < steps:
+        elif (params.neighbour == abi.NEIGHBOUR_CELL or moved) and k + 1 < steps:
             if params.neighbour == abi.NEIGHBOUR_CELL:
                 cands, best = s.retune(dt, trial_steps=10)
                 choice = cands[best]
