@@ -182,3 +182,44 @@ def test_cell_units_fp32x_other_steppers_bitwise(stepper):
             s.step(0.005, 12, graph=True)
             out.append(s.download_state())
     assert np.array_equal(out[0], out[1])
+
+
+def test_cell_units_in_a_batch_with_admissions_equal_alone():
+    """A served FP32X batch with cell units on, whose layout changes between
+    calls (a system released, another admitted): every system's state equals
+    the same system run alone without cell units, bit for bit."""
+    rng = np.random.default_rng(96)
+
+    def clustered(n, Lb, seed):
+        st = init_state(n, Lb, seed)
+        st[0::3] = 0.1 * Lb + 0.4 * Lb * rng.random(n)
+        st[1::3] = 0.1 * Lb + 0.4 * Lb * rng.random(n)
+        return st
+
+    systems = [(3000, 1.2, dict(PRM, rho=0.15)), (5000, 1.5, dict(PRM, rho=0.12)),
+               (2000, 1.0, dict(PRM, rho=0.2))]
+    states = [clustered(n, Lb, 97 + k) for k, (n, Lb, _) in enumerate(systems)]
+
+    def params(k):
+        n, Lb, p = systems[k]
+        return abi.make_params(L=Lb, stepper=abi.STEPPER_SRK, precision=abi.PRECISION_FP32X, seed=5,
+                               system_id=k, **p)
+
+    ntot = sum(n for n, _, _ in systems)
+    ctot = sum(abi.cells_of(Lb, p["rho"]) for _, Lb, p in systems)
+    with abi.Batch(abi.STEPPER_SRK, abi.PRECISION_FP32X, 3, ntot, ctot) as b:
+        b.set_tuning(abi.TUNE_SPARSE_BELOW, 0.0)
+        b.set_tuning(abi.TUNE_CELL_UNITS, 1)
+        s0 = b.admit(systems[0][0], params(0), states[0])
+        s1 = b.admit(systems[1][0], params(1), states[1])
+        b.step(0.005, 10, graph=True)
+        b.release(s0)
+        s2 = b.admit(systems[2][0], params(2), states[2])
+        b.step(0.005, 10, graph=True)
+        got = {1: b.download(s1), 2: b.download(s2)}
+    for k, nsteps in ((1, 20), (2, 10)):
+        with abi.System(systems[k][0], params(k)) as s:
+            s.set_tuning(abi.TUNE_SPARSE_BELOW, 0.0)
+            s.upload_state(states[k])
+            s.step(0.005, nsteps)
+            assert np.array_equal(s.download_state(), got[k]), k
