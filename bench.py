@@ -985,6 +985,7 @@ def run_configured(abi, torch, w, precision, params, tuning, steps, warmup, rank
     ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
           for _ in range(steps)]
     wall, series, retunes, samples = [], [], [], []
+    launches = 0
     tuned_at = None  # ms per simulation step when last tuned
     if dist is not None:
         dist.barrier()
@@ -1000,6 +1001,7 @@ def run_configured(abi, torch, w, precision, params, tuning, steps, warmup, rank
         ev[k][1].record(stream)
         s.download_state(host)
         wall.append((time.perf_counter() - t0) * 1e3)
+        launches += s.graph_nodes() * reps  # the kernels of the graph this bench step replayed
         o = s.order_params()
         series.append((per * (k + 1), o["R"], o["R_local"]))
         cost = ev[k][0].elapsed_time(ev[k][1]) / per
@@ -1037,7 +1039,6 @@ def run_configured(abi, torch, w, precision, params, tuning, steps, warmup, rank
         dist.barrier()
     ms = reduce_max(dist, sum(a.elapsed_time(b) for a, b in ev))
     e2e_ms = reduce_max(dist, sum(wall))
-    launches = s.graph_nodes() * reps * steps
     prof = s.profile_steps(dt, 20)  # on the final (clustered) state
     final_state = host.copy()
     del host
