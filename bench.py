@@ -670,6 +670,54 @@ def va_inputs(w):
     return st
 
 
+def run_choices():
+    """The float forms' kernel choices side by side on one GPU: whole cell
+    tiles (one CTA per cell), cell units (SPC_TUNE_CELL_UNITS) and sub-cells
+    (SPC_TUNE_SUBCELLS, units of half cells over the half stencils), each
+    with a per-phase CUDA-event profile of 20 eager steps (stage, sort,
+    gather with the unit listing, pass 1, pass 2, whole step) and the
+    graph-replayed step (50 steps, CUDA events on the handle's stream).
+    States: the headline workload's seeded initial state, its clustered
+    state after 4,000 FP64 steps (tests/golden/states) and a uniform system
+    four times denser (N = 262,144 in the same box: 256 particles per cell)."""
+    import torch
+    from spc2_langevin_integration_gb300 import abi
+    w = WORKLOAD
+    st0, om0 = init_inputs(w)
+    z = np.load(os.path.join(ROOT, "tests", "golden", "states", "vortex_clustered_n65536.npz"))
+    wd = dict(w, n=4 * w["n"])
+    std, omd = init_inputs(wd)
+    cases = {"initial": (w, st0, om0), "clustered": (w, z["state"].copy(), z["omega"].copy()),
+             "dense_n262144": (wd, std, omd)}
+    rows = {}
+    for form, prec in (("fp32c", abi.PRECISION_FP32C), ("fp32x", abi.PRECISION_FP32X)):
+        for cname, (ww, st, om) in cases.items():
+            p = workload_params(abi, ww, prec)
+            p.neighbour = abi.NEIGHBOUR_CELL
+            res = {}
+            for label, units, sub in (("tiles", 0, 0), ("units", 1, 0), ("subcells", 0, 1)):
+                with abi.System(ww["n"], p) as s:
+                    s.set_tuning(abi.TUNE_SPARSE_BELOW, 0.0)
+                    s.set_tuning(abi.TUNE_CELL_UNITS, units)
+                    s.set_tuning(abi.TUNE_SUBCELLS, sub)
+                    s.upload_state(st)
+                    s.upload_omega(om)
+                    s.step(ww["dt"], 5)
+                    prof = {k: round(v * 1e3, 1) for k, v in s.profile_steps(ww["dt"], 20).items()}
+                    s.prepare_graph(ww["dt"], 50)
+                    s.step(ww["dt"], 50, graph=True)
+                    stream = torch.cuda.ExternalStream(s.stream)
+                    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                    s.synchronize()
+                    e0.record(stream)
+                    s.step(ww["dt"], 50, graph=True)
+                    e1.record(stream)
+                    e1.synchronize()
+                    res[label] = {"phases_us": prof, "graph_step_us": round(e0.elapsed_time(e1) / 50 * 1e3, 1)}
+            rows[f"{form}_{cname}"] = res
+    return rows
+
+
 def run_va(steps, cpu=True):
     """The vortex-arrays model (VortexArraysSystemPtr) with the reference's
     vortex-array parameters (SimulationEnginePtr.cpp:131-139, box side 1 ->
@@ -818,7 +866,7 @@ def tune_form(abi, w, precision, rank=0):
 
 
 def run_form(abi, torch, w, precision, steps, warmup, rank, dist, params=None, sparse_below=None,
-             e2e=True, tile_split=None, cell_units=None):
+             e2e=True, tile_split=None, cell_units=None, subcells=None):
     """Device-timed graph replays of the workload; then (e2e) the same through
     the C-ABI with host buffers, and a per-phase profile.
 
@@ -838,6 +886,8 @@ def run_form(abi, torch, w, precision, steps, warmup, rank, dist, params=None, s
         s.set_tuning(abi.TUNE_TILE_SPLIT, tile_split)
     if cell_units is not None:
         s.set_tuning(abi.TUNE_CELL_UNITS, cell_units)
+    if subcells is not None:
+        s.set_tuning(abi.TUNE_SUBCELLS, subcells)
     s.upload_state(st)
     s.upload_omega(omega)
     stream = torch.cuda.ExternalStream(s.stream)
@@ -910,6 +960,7 @@ def apply_tuning(abi, s, tun):
     s.set_tuning(abi.TUNE_SPARSE_BELOW, tun["sparse_below"])
     s.set_tuning(abi.TUNE_TILE_SPLIT, tun["tile_split"])
     s.set_tuning(abi.TUNE_CELL_UNITS, tun.get("cell_units", 0))
+    s.set_tuning(abi.TUNE_SUBCELLS, tun.get("subcells", 0))
 
 
 def phase_sample(abi, w, params, s, state, omega, dt):
@@ -919,7 +970,8 @@ def phase_sample(abi, w, params, s, state, omega, dt):
     measured handle, its graph and its trajectory are left as they are."""
     with abi.System(w["n"], params) as c:
         if params.neighbour == abi.NEIGHBOUR_CELL:
-            for key in (abi.TUNE_SPARSE_BELOW, abi.TUNE_TILE_SPLIT, abi.TUNE_CELL_UNITS):
+            for key in (abi.TUNE_SPARSE_BELOW, abi.TUNE_TILE_SPLIT, abi.TUNE_CELL_UNITS,
+                        abi.TUNE_SUBCELLS):
                 c.set_tuning(key, s.get_tuning(key))
         c.upload_omega(omega)
         c.upload_state(state)
@@ -946,7 +998,8 @@ def run_configured(abi, torch, w, precision, params, tuning, steps, warmup, rank
     After each bench step, outside the timers, the global and local order
     parameters are recorded (the drift series), and the handle is tuned again
     on the current, clustering state: a cell-list handle after every bench
-    step, in place (spc_retune: kernel choice, CTAs per cell, cell units;
+    step, in place (spc_retune: kernel choice, CTAs per cell, cell units,
+    sub-cells;
     state and step counter are left as they were), a Verlet-row handle when
     its cost per step has moved by more than 25% since its last tuning, by
     spc_autotune_ex over every method, moving to a new handle (state,
@@ -1086,6 +1139,9 @@ def main():
     ap.add_argument("--cell-units", type=int, choices=[0, 1], default=None,
                     help="--form / --ncu-case (FP32C, FP32X): run the cells as units of 32 particles x "
                          "one staging round in a second launch of each pass (SPC_TUNE_CELL_UNITS)")
+    ap.add_argument("--subcells", type=int, choices=[0, 1], default=None,
+                    help="--form / --ncu-case (FP32C, FP32X): bin into half-cells and run the cells as "
+                         "units of their halves (SPC_TUNE_SUBCELLS)")
     ap.add_argument("--save-final-states", default=None,
                     help="headline run: write each form's state after the whole run to "
                          "<dir>/final_state_<form>.npz")
@@ -1098,7 +1154,7 @@ def main():
                     help="--ncu-case fp32c/fp64: the cell-list passes instead of the Verlet rows")
     ap.add_argument("--workload",
                     choices=["vortex", "ensemble", "serve", "drift", "drift-ensemble", "drift-oracle",
-                             "large", "va", "observed"],
+                             "large", "va", "observed", "choices"],
                     default="vortex",
                     help="vortex: the headline single-system line; ensemble: 512 systems in one "
                          "batch; serve: the Poisson request stream; drift: FP32C vs FP64 order "
@@ -1106,7 +1162,8 @@ def main():
                          "drift of the 512-system ensemble against FP64 over 5,000 steps; "
                          "large: Chimera RK4, N=2^22, L=64; va: the "
                          "vortex-arrays model, N=51,200, L=8; observed: the headline workload "
-                         "with a frame every 10 steps, per-step loop vs the device loop")
+                         "with a frame every 10 steps, per-step loop vs the device loop; choices: "
+                         "phase profiles of cell tiles, cell units and sub-cells (float forms)")
     ap.add_argument("--sparse-below", type=float, default=None,
                     help="ensemble: neighbour-kernel tuning (mean particles per cell below "
                          "which a system runs the warp-per-cell passes)")
@@ -1164,6 +1221,10 @@ def main():
                               "cpu_baseline": cpu}))
         if dist is not None:
             dist.destroy_process_group()
+        return
+    if args.workload == "choices":
+        print(json.dumps({"workload": "choices", "config": WORKLOAD, "unit": "us per SRK step",
+                          "rows": run_choices()}))
         return
     if args.workload == "va":
         print(json.dumps({"metric": "particle-steps/s", "workload": VA["name"], "config": VA,
@@ -1297,6 +1358,8 @@ def main():
                     s.set_tuning(abi.TUNE_TILE_SPLIT, args.tile_split)
                 if args.cell_units is not None:
                     s.set_tuning(abi.TUNE_CELL_UNITS, args.cell_units)
+                if args.subcells is not None:
+                    s.set_tuning(abi.TUNE_SUBCELLS, args.subcells)
             s.upload_state(st)
             s.upload_omega(omega)
             s.step(w["dt"], 3)
@@ -1349,7 +1412,7 @@ def main():
             p.skin = args.skin
         ms, e2e_ms, prof, _, launches = run_form(abi, torch, w, prec, args.steps, args.warmup,
                                                  rank, dist, p, tile_split=args.tile_split,
-                                                 cell_units=args.cell_units)
+                                                 cell_units=args.cell_units, subcells=args.subcells)
         if rank == 0:
             print(json.dumps({"form": args.form, "neighbour": args.neighbour, "skin": p.skin,
                               "tile_split": args.tile_split,
@@ -1399,7 +1462,8 @@ def main():
     best, tun, _ = tuned[head]
     ms_w, _, _, _, _ = run_form(abi, torch, w, dict(forms)[head], args.steps, args.warmup, rank,
                                 dist, best, tun["sparse_below"], e2e=False,
-                                tile_split=tun["tile_split"], cell_units=tun["cell_units"])
+                                tile_split=tun["tile_split"], cell_units=tun["cell_units"],
+                                subcells=tun.get("subcells", 0))
     hbm, peak_kind = peaks()
     # per-phase launch durations averaged over the run: a CUDA-event profile
     # after each bench step (on a copy of the state, outside the timers)

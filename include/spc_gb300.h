@@ -27,7 +27,7 @@
 extern "C" {
 #endif
 
-#define SPC_ABI_VERSION 3
+#define SPC_ABI_VERSION 4
 
 typedef enum spc_status {
   SPC_OK = 0,
@@ -107,7 +107,7 @@ typedef struct spc_params {
 typedef struct spc_handle spc_handle;
 
 /* Library / version.  SPC_ABI_VERSION changes with any layout change of the
- * structs above or below (3: spc_tuning gained cell_units). */
+ * structs above or below (3: spc_tuning gained cell_units; 4: subcells). */
 int spc_abi_version(void);
 const char *spc_last_error(const spc_handle *h); /* h may be NULL: last global error */
 
@@ -246,8 +246,26 @@ int spc_profile_steps(spc_handle *h, double dt, int32_t nsteps, double *out_ms, 
  * idle at the end of a pass.  With 1, FP32X results are unchanged (exact
  * sums) and FP32C sums are added in another fixed order; either way they do
  * not depend on SPC_TUNE_TILE_SPLIT.  Refused for FP64 handles.
+ * SPC_TUNE_SUBCELLS (FP32C and FP32X cell-list handles; the cell-size
+ * dimension): 1 bins each cell of side L/int(L/rho) into a lower and an
+ * upper half and runs the cells of at most 8 staging rounds as cell units of
+ * their halves (with SPC_TUNE_CELL_UNITS 0 as well).  A half needs only the
+ * near half of the row beyond it: the far half is more than a cell side
+ * (>= rho) away, so about 7.5 of the 9 stencil cells are tested.  0 (the
+ * default) keeps whole cells.  The neighbour sets are those of whole cells:
+ * FP32X results are unchanged, FP32C sums are added in another fixed
+ * order.  (An excluded pair could only count as a neighbour if the cell side
+ * equalled rho to within rounding and the pair lay within rounding of the
+ * cutoff, across the half boundary, with |dx| below ~1e-8 rho.)  Neighbour
+ * diagnostics keep whole cells.  Refused for FP64 and Verlet handles.
  * spc_get_tuning reads a knob back. */
-enum { SPC_TUNE_SPARSE_BELOW = 1, SPC_TUNE_VERLET_ROW_LIMIT = 2, SPC_TUNE_TILE_SPLIT = 3, SPC_TUNE_CELL_UNITS = 4 };
+enum {
+  SPC_TUNE_SPARSE_BELOW = 1,
+  SPC_TUNE_VERLET_ROW_LIMIT = 2,
+  SPC_TUNE_TILE_SPLIT = 3,
+  SPC_TUNE_CELL_UNITS = 4,
+  SPC_TUNE_SUBCELLS = 5
+};
 int spc_set_tuning(spc_handle *h, int32_t key, double value);
 int spc_get_tuning(const spc_handle *h, int32_t key, double *value);
 
@@ -264,8 +282,8 @@ int spc_get_tuning(const spc_handle *h, int32_t key, double *value);
  * *count the number of candidates.  The caller's state is not touched. */
 /* One tuning candidate and its measured cost (no counterpart in the
  * reference): the neighbour method and skin, the SPC_TUNE_SPARSE_BELOW,
- * SPC_TUNE_TILE_SPLIT and SPC_TUNE_CELL_UNITS values, and milliseconds per
- * step. */
+ * SPC_TUNE_TILE_SPLIT, SPC_TUNE_CELL_UNITS and SPC_TUNE_SUBCELLS values, and
+ * milliseconds per step. */
 typedef struct spc_tuning {
   int32_t neighbour;    /* SPC_NEIGHBOUR_* */
   int32_t tile_split;   /* CTAs per cell of the cell-tile passes */
@@ -273,6 +291,7 @@ typedef struct spc_tuning {
   double sparse_below;  /* SPC_TUNE_SPARSE_BELOW value */
   double ms_per_step;   /* measured */
   int32_t cell_units;  /* SPC_TUNE_CELL_UNITS value */
+  int32_t subcells;    /* SPC_TUNE_SUBCELLS value */
 } spc_tuning;
 
 /* Autotuner over every tuning dimension (no counterpart in the reference):

@@ -23,6 +23,7 @@ TUNE_SPARSE_BELOW = 1
 TUNE_VERLET_ROW_LIMIT = 2
 TUNE_TILE_SPLIT = 3
 TUNE_CELL_UNITS = 4
+TUNE_SUBCELLS = 5
 
 SPC_OK = 0
 ERRORS = {
@@ -61,13 +62,14 @@ class Tuning(C.Structure):
     _fields_ = [
         ("neighbour", C.c_int32), ("tile_split", C.c_int32), ("skin", C.c_double),
         ("sparse_below", C.c_double), ("ms_per_step", C.c_double), ("cell_units", C.c_int32),
+        ("subcells", C.c_int32),
     ]
 
     def as_dict(self):
         return {"neighbour": "verlet" if self.neighbour == NEIGHBOUR_VERLET else "cell",
                 "tile_split": self.tile_split, "skin": self.skin,
                 "sparse_below": self.sparse_below, "cell_units": self.cell_units,
-                "ms_per_step": self.ms_per_step}
+                "subcells": self.subcells, "ms_per_step": self.ms_per_step}
 
 
 _lib = None

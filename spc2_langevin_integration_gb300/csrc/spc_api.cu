@@ -765,13 +765,14 @@ int spc_autotune_ex(const spc_params *p, int32_t n, const double *aos3n, const d
   if (rc) return fail(nullptr, rc, "%s", why.c_str());
   std::vector<spc_tuning> cands;
   for (const TuneCand &c : kernel_candidates(p->precision))
-    cands.push_back({SPC_NEIGHBOUR_CELL, c.split, 0.0, c.sparse, 0.0, c.units});
+    cands.push_back({SPC_NEIGHBOUR_CELL, c.split, 0.0, c.sparse, 0.0, c.units, c.subcells});
   for (double f : {0.1, 0.2, 0.4}) {
     if (p->precision == SPC_PRECISION_FP32X) break;  // the FP32X form runs the cell list
     spc_params q = *p;
     q.neighbour = SPC_NEIGHBOUR_VERLET;
     q.skin = f * p->rho;
-    if (make_sysconst(q, n).vR > 0) cands.push_back({SPC_NEIGHBOUR_VERLET, 1, q.skin, kSparseBelowDefault, 0.0, 0});
+    if (make_sysconst(q, n).vR > 0)
+      cands.push_back({SPC_NEIGHBOUR_VERLET, 1, q.skin, kSparseBelowDefault, 0.0, 0, 0});
   }
   int best_k = 0;
   for (size_t k = 0; k < cands.size(); ++k) {
@@ -786,6 +787,7 @@ int spc_autotune_ex(const spc_params *p, int32_t n, const double *aos3n, const d
       rc = spc_set_tuning(h, SPC_TUNE_SPARSE_BELOW, cands[k].sparse_below);
       if (rc == SPC_OK) rc = spc_set_tuning(h, SPC_TUNE_TILE_SPLIT, cands[k].tile_split);
       if (rc == SPC_OK) rc = spc_set_tuning(h, SPC_TUNE_CELL_UNITS, cands[k].cell_units);
+      if (rc == SPC_OK) rc = spc_set_tuning(h, SPC_TUNE_SUBCELLS, cands[k].subcells);
     }
     double t = 0.0;
     float f = 0.0f;

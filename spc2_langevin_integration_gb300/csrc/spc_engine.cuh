@@ -219,8 +219,13 @@ struct Engine {
   // tuning: the cells of the float cell-tile passes run as units (1) or as
   // whole groups (0)
   int cell_units_tune = 0;
-  // the cell-unit buffers (float forms; allocated at init)
+  // tuning: the float cell-tile passes bin into half-cell sub-cells and run
+  // every cell of at most kSplitRounds rounds as units of its halves (1)
+  int subcells_tune = 0;
+  // the cell-unit and sub-cell buffers (float forms; allocated at init)
   int2 *units_buf = nullptr;
+  int *cell_mid_buf = nullptr;
+  uint8_t *cell_near_buf = nullptr;
   std::vector<int> slot_layout;  // slot -> layout index (-1 if inactive)
   // noise injection (single-system handles)
   double *d_noise = nullptr;
@@ -329,8 +334,8 @@ inline void engine_footprint(int stepper, int precision, long long *per_particle
   if (precision == SPC_PRECISION_FP64) b += 8 + 8 + 4;                          // vortex-arrays outputs
   b += 12 * 8 + 4 + 4;                       // AoS staging, histogram share
   *per_particle = b;
-  *per_cell = 4 + 4 + (precision != SPC_PRECISION_FP64 ? kSplitRounds * 8 + 1 : 0);  // cell_start,
-                                                                      // sys_of_c, unit list and flag
+  // cell_start, sys_of_c; float forms: unit list (two halves' worth), flag, sub-cell split and flag
+  *per_cell = 4 + 4 + (precision != SPC_PRECISION_FP64 ? 2 * kSplitRounds * 8 + 1 + 4 + 1 : 0);
 }
 
 inline int engine_init(Engine *e, int stepper, int precision, int pool_cap, int sys_cap, int cell_cap) {
@@ -396,8 +401,12 @@ inline int engine_init(Engine *e, int stepper, int precision, int pool_cap, int 
   }
   if (precision != SPC_PRECISION_FP64) {
     // a unit cell of n_c particles lists ceil(n_c / 32) x (at most
-    // kSplitRounds) units, so (N / 32 + cells) x kSplitRounds entries hold any layout
-    SPC_TRY(dalloc(e, &e->units_buf, ((N + kWarp - 1) / kWarp + (size_t)cell_cap) * kSplitRounds));
+    // kSplitRounds) units, or with sub-cells ceil(n_0 / 32) + ceil(n_1 / 32)
+    // (n_0 + n_1 = n_c) times that, so (N / 32 + 2 cells) x kSplitRounds
+    // entries hold any layout
+    SPC_TRY(dalloc(e, &e->units_buf, ((N + kWarp - 1) / kWarp + 2 * (size_t)cell_cap) * kSplitRounds));
+    SPC_TRY(dalloc(e, &e->cell_mid_buf, (size_t)cell_cap));
+    SPC_TRY(dalloc(e, &e->cell_near_buf, (size_t)cell_cap));
     SPC_TRY(dalloc(e, &a.unit_count, 1));
     SPC_TRY(dalloc(e, &a.cell_unit, (size_t)cell_cap));
     SPC_TRY(dalloc(e, &a.part_n, (size_t)kSplitRounds * N));
@@ -669,6 +678,11 @@ inline int system_class(const Engine *e, const SysHost &h) {
   return (double)h.n < e->sparse_below * (double)h.ncell ? 1 : 0;
 }
 
+// Sub-cells are in effect: asked for, on a float form's cell-list engine.
+inline bool subcells_on(const Engine *e) {
+  return e->subcells_tune && e->precision != SPC_PRECISION_FP64 && !e->verlet;
+}
+
 // Rebuild the device layout tables from the host mirror.
 // What a captured step graph bakes in beyond device pointers: kernel grid
 // sizes and the counts passed by value.  A layout that leaves these unchanged
@@ -678,7 +692,8 @@ inline std::vector<long long> launch_shape(const Engine *e) {
   const KArgs &a = e->a;
   return {e->nsys, e->n_active, e->ncell_total, e->ntiles, e->radix_bits, e->sort_passes, e->ncell_tile,
           e->ncell_warp, e->ncell_va, e->n_ap_all, e->has_cells, a.n_ap, a.tile_split, a.hist_len,
-          e->ap_items, e->ap_items_all, e->ap_items_small, e->ap_items_all_small, a.units != nullptr};
+          e->ap_items, e->ap_items_all, e->ap_items_small, e->ap_items_all_small, a.units != nullptr,
+          a.cell_mid != nullptr};
 }
 
 inline int engine_layout(Engine *e) {
@@ -726,8 +741,11 @@ inline int engine_layout(Engine *e) {
   e->n_active = dense;
   e->ncell_total = cells;
   e->ntiles = std::max(1, (dense + kSortTile - 1) / kSortTile);
+  // sub-cells: two sort keys per cell
+  const bool sub = subcells_on(e);
+  const int nkeys = sub ? 2 * cells : cells;
   int bits = 1;
-  while (bits < 31 && (1u << bits) < (unsigned)std::max(cells, 2)) ++bits;
+  while (bits < 31 && (1u << bits) < (unsigned)std::max(nkeys, 2)) ++bits;
   e->sort_passes = (bits + 10) / 11;
   e->radix_bits = (bits + e->sort_passes - 1) / e->sort_passes;
   e->has_cells = ncell_tile + ncell_warp > 0;
@@ -738,7 +756,9 @@ inline int engine_layout(Engine *e) {
   a.ncell_total = e->ncell_total;
   a.ncell_tile = e->ncell_tile;
   a.tile_split = tile_split_for(e->tile_split_tune);
-  a.units = e->cell_units_tune ? e->units_buf : nullptr;
+  a.units = (e->cell_units_tune || sub) ? e->units_buf : nullptr;
+  a.cell_mid = sub ? e->cell_mid_buf : nullptr;
+  a.cell_near = sub ? e->cell_near_buf : nullptr;
   a.va_c0 = e->ncell_tile + e->ncell_warp;
   a.va_c1 = a.va_c0 + e->ncell_va;
   a.n_ap = (int)ap.size();
@@ -779,6 +799,11 @@ inline int eval_cells(Engine *e, KArgs &a, int rk_form, int kq, double kcdt, boo
 // need the reference's current cells) runs the cell-list binning and leaves
 // the build stale.
 inline int eval_stage(Engine *e, KArgs &a, int rk_form, int kq, double kcdt, bool verlet_ok = true) {
+  // diagnostics visit each cell's members in ascending index: no sub-cells
+  if (!verlet_ok) {
+    a.cell_mid = nullptr;
+    a.cell_near = nullptr;
+  }
   if (!e->verlet) return eval_cells(e, a, rk_form, kq, kcdt);
   if (!verlet_ok) {
     e->verlet_stale = true;
@@ -1124,6 +1149,16 @@ inline int engine_set_tuning(Engine *e, int key, double value) {
     }
     return SPC_OK;
   }
+  if (key == SPC_TUNE_SUBCELLS) {
+    if (value != 0.0 && value != 1.0) return fail(e, SPC_ERR_INVALID, "sub-cells must be 0 or 1");
+    if (value == 1.0 && (e->precision == SPC_PRECISION_FP64 || e->verlet))
+      return fail(e, SPC_ERR_INVALID, "sub-cells apply to the FP32C and FP32X cell-list passes");
+    if ((int)value != e->subcells_tune) {
+      e->subcells_tune = (int)value;
+      e->dirty = true;
+    }
+    return SPC_OK;
+  }
   if (key == SPC_TUNE_TILE_SPLIT) {
     if (!(value >= 0.0) || !(value <= 8.0) || value != std::floor(value))
       return fail(e, SPC_ERR_INVALID, "tile split must be an integer in [0, 8]");
@@ -1157,6 +1192,10 @@ inline int engine_get_tuning(const Engine *e, int key, double *value) {
     *value = (double)e->cell_units_tune;
     return SPC_OK;
   }
+  if (key == SPC_TUNE_SUBCELLS) {
+    *value = (double)e->subcells_tune;
+    return SPC_OK;
+  }
   if (key == SPC_TUNE_TILE_SPLIT) {  // the split in effect
     *value = (double)tile_split_for(e->tile_split_tune);
     return SPC_OK;
@@ -1171,20 +1210,24 @@ struct TuneCand {
   double sparse;
   int split;
   int units;
+  int subcells;
 };
 
 // The kernel-choice candidates; cell units (float forms) with one and two
-// CTAs per cell.
+// CTAs per cell, and sub-cells (float forms; their units replace the
+// cell-tile kernel for all but the longest lists, so one CTA per cell).
 inline std::vector<TuneCand> kernel_candidates(int precision) {
   std::vector<TuneCand> c;
   for (double sb : {0.0, kSparseBelowDefault, 1e9})
     for (int split : {1, 2, 4}) {
       if (sb == 1e9 && split != 1) continue;  // no cell-tile systems left: the split does nothing
-      c.push_back({sb, split, 0});
+      c.push_back({sb, split, 0, 0});
     }
-  if (precision != SPC_PRECISION_FP64)
+  if (precision != SPC_PRECISION_FP64) {
     for (double sb : {0.0, kSparseBelowDefault})
-      for (int split : {1, 2}) c.push_back({sb, split, 1});
+      for (int split : {1, 2}) c.push_back({sb, split, 1, 0});
+    for (double sb : {0.0, kSparseBelowDefault}) c.push_back({sb, 1, 1, 1});
+  }
   return c;
 }
 
@@ -1201,7 +1244,7 @@ inline int engine_retune(Engine *e, double dt, int trial, spc_tuning *out, int c
   SPC_TRY(engine_set_device(e));
   SPC_TRY(engine_layout(e));
   std::vector<TuneCand> cands = e->verlet ? std::vector<TuneCand>{{e->sparse_below, e->tile_split_tune,
-                                                                    e->cell_units_tune}}
+                                                                    e->cell_units_tune, e->subcells_tune}}
                                           : kernel_candidates(e->precision);
   const size_t P = (size_t)e->pool_cap;
   std::vector<double *> live = {e->a.x, e->a.y, e->a.phi};
@@ -1233,7 +1276,7 @@ inline int engine_retune(Engine *e, double dt, int trial, spc_tuning *out, int c
     return SPC_OK;
   };
   const double sb0 = e->sparse_below;
-  const int split0 = e->tile_split_tune, units0 = e->cell_units_tune;
+  const int split0 = e->tile_split_tune, units0 = e->cell_units_tune, sub0 = e->subcells_tune;
   cudaEvent_t ev[2] = {nullptr, nullptr};
   cudaError_t ce = copy_all(true);
   if (ce == cudaSuccess) ce = cudaEventCreate(&ev[0]);
@@ -1245,6 +1288,7 @@ inline int engine_retune(Engine *e, double dt, int trial, spc_tuning *out, int c
     e->sparse_below = cands[k].sparse;
     e->tile_split_tune = cands[k].split;
     e->cell_units_tune = cands[k].units;
+    e->subcells_tune = cands[k].subcells;
     e->dirty = true;
     rc = engine_steps(e, dt, trial, false, nullptr, 0);
     if (rc == SPC_OK) rc = restore();
@@ -1265,6 +1309,7 @@ inline int engine_retune(Engine *e, double dt, int trial, spc_tuning *out, int c
       out[k].sparse_below = cands[k].sparse;
       out[k].ms_per_step = per;
       out[k].cell_units = cands[k].units;
+      out[k].subcells = cands[k].subcells;
     }
     if (rc == SPC_OK && per < best_ms) {
       best_ms = per;
@@ -1279,12 +1324,14 @@ inline int engine_retune(Engine *e, double dt, int trial, spc_tuning *out, int c
     e->sparse_below = sb0;
     e->tile_split_tune = split0;
     e->cell_units_tune = units0;
+    e->subcells_tune = sub0;
     e->dirty = true;
     return rc;
   }
   e->sparse_below = cands[best_k].sparse;
   e->tile_split_tune = cands[best_k].split;
   e->cell_units_tune = cands[best_k].units;
+  e->subcells_tune = cands[best_k].subcells;
   e->dirty = true;
   if (count) *count = (int)cands.size();
   if (best) *best = best_k;

@@ -81,6 +81,13 @@ struct KArgs {
   uint32_t *keys, *vals;             // unsorted (global cell key, dense index)
   const uint32_t *skeys, *svals;     // sorted
   int *cell_start;
+  // Sub-cells (SPC_TUNE_SUBCELLS; null when off): the sort key is 2c + h, h = 1
+  // for the upper half of cell c (row_offset at least half a cell), and the
+  // upper half starts at cell_mid[c].  cell_near[c] = 1 when a particle of
+  // cell c lies within kNearHalf cell sides of the half line (cleared by
+  // k_stage, set by k_gather).
+  int *cell_mid;
+  uint8_t *cell_near;
   // cell order
   double *sx, *sy, *sphi;
   float2 *fxy;                       // prefilter coordinates relative to the cell origin
@@ -148,15 +155,40 @@ struct KArgs {
   unsigned long long *vrebuilds;
 };
 
+// Global cell of cell-order slot p (its sort key, halved with sub-cells).
+__device__ __forceinline__ int cell_of_slot(const KArgs &a, int p) {
+  const int k = (int)a.skeys[p];
+  return a.cell_mid ? k >> 1 : k;
+}
+
+// Sub-cells: a stage y's offset above the lower edge of its cell row cy.  It
+// decides the half (upper when >= cell / 2) in k_stage and the near flag in
+// k_gather, the same expression in both.
+__device__ __forceinline__ double row_offset(const SysConst &sc, double y, int cy) {
+  return dsub(y, dmul((double)cy, sc.cell));
+}
+
+// A half's stencil leaves out the far half of the row beyond it.  The pairs
+// left out are more than a cell side (>= rho) apart unless both particles
+// lie within rounding of the half line, so each cell records whether any of
+// its particles lies within kNearHalf cell sides of the line, and a far cell
+// stays whole when both it and the half's own cell do.  2^-20 of a cell is
+// far above the rounding of the row offsets and of the reference's distance
+// (a few ulps of L, L < 2^30 cells), and holds ~2e-6 of the particles.
+constexpr double kNearHalf = 0x1p-20;
+
 // ---------------------------------------------------------------------------
 // k_stage: rk = s + (k_coef*dt) * k_prev (ChimeraSystem.cpp:274-276), the copy
 // wrap and cell key (:295-308).  kq < 0 means k_prev is all zeros (the Euler
 // stepper's zero-filled buffer, StochasticEulerStepper.hpp:34); rk_form = 0 is
-// the SRK form, whose stage state is the state itself (:456-458).
+// the SRK form, whose stage state is the state itself (:456-458).  With
+// sub-cells the key also carries the half of the cell (the upper half when
+// the stage y is at least half a cell above the cell's lower edge).
 // With hist_bits > 0 the kernel also counts the first radix digit per sort
 // tile into hist (tile-major [tile][digit], zero on entry): a block-local
 // shared histogram, then one global atomic per non-empty bin.
 constexpr int kStageThreads = 256;
+
 constexpr int kMaxHistBits = 11;
 
 __global__ void __launch_bounds__(kStageThreads)
@@ -169,6 +201,8 @@ __global__ void __launch_bounds__(kStageThreads)
     for (int k = threadIdx.x; k < R; k += blockDim.x) h[k] = 0;
     __syncthreads();
   }
+  if (a.cell_mid)  // this evaluation's near flags (set by k_gather)
+    for (int c = d; c < a.ncell_total; c += gridDim.x * blockDim.x) a.cell_near[c] = 0;
   if (d < a.n_active) {
     const SysDesc &sd = a.sys[a.sys_of_p[d]];
     const SysConst &sc = sd.sc;
@@ -185,7 +219,7 @@ __global__ void __launch_bounds__(kStageThreads)
     uint32_t key;
     if (sc.allpairs) {
       // all pairs use the unwrapped stage positions (ChimeraSystem.cpp:135-153)
-      key = (uint32_t)sd.c0;
+      key = a.cell_mid ? 2u * (uint32_t)sd.c0 : (uint32_t)sd.c0;
     } else {
       wrap_if_outside(sc, x, y);
       int clamped = 0;
@@ -193,6 +227,7 @@ __global__ void __launch_bounds__(kStageThreads)
       const int cy = cell_coord(sc, y, clamped);
       if (clamped) atomicAdd(a.clamped, 1ull);
       key = (uint32_t)(sd.c0 + cy * sc.nc + cx);
+      if (a.cell_mid) key = 2u * key + (row_offset(sc, y, cy) >= 0.5 * sc.cell ? 1u : 0u);
     }
     a.st_x[d] = x;
     a.st_y[d] = y;
@@ -224,7 +259,10 @@ __global__ void k_gather(KArgs a) {
   const int n = a.n_active;
   if (p > n) return;
   // the cell start table of the sorted keys (one thread per slot and one past the end)
-  cell_bounds_at(a.skeys, n, a.ncell_total, a.cell_start, p);
+  if (a.cell_mid)
+    half_bounds_at(a.skeys, n, a.ncell_total, a.cell_start, a.cell_mid, p);
+  else
+    cell_bounds_at(a.skeys, n, a.ncell_total, a.cell_start, p);
   // leave the first-digit histogram table zero for the next stage kernel
   for (int k = p; k < a.hist_len; k += n + 1) a.hist[k] = 0u;
   if (p == n) {
@@ -241,12 +279,14 @@ __global__ void k_gather(KArgs a) {
   a.pidx[p] = sd.pool_p0 + (d - sd.dense_p0);
   if (a.vsys) {  // Verlet build: remember each slot's system and cell until the next build
     a.vsys[p] = a.sys_of_p[d];
-    a.vcell[p] = (int)a.skeys[p];
+    a.vcell[p] = cell_of_slot(a, p);
   }
   if (!sc.allpairs) {
-    const int key = (int)a.skeys[p] - sd.c0;
+    const int key = cell_of_slot(a, p) - sd.c0;
     const int cx = key % sc.nc, cy = key / sc.nc;
     a.fxy[p] = make_float2((float)(x - (double)cx * sc.cell), (float)(y - (double)cy * sc.cell));
+    if (a.cell_mid && fabs(row_offset(sc, y, cy) - 0.5 * sc.cell) < kNearHalf * sc.cell)
+      a.cell_near[sd.c0 + key] = 1;
   }
   if constexpr (PREC == kPrecFP32C) {
     float s, c;
@@ -650,7 +690,7 @@ template <int KIND>
 __global__ void __launch_bounds__(256) k_epilogue_fp32x(KArgs a, int epi) {
   const int p = blockIdx.x * blockDim.x + threadIdx.x;
   if (p >= a.n_active) return;
-  const SysDesc &sd = a.sys[a.sys_of_c[a.skeys[p]]];
+  const SysDesc &sd = a.sys[a.sys_of_c[cell_of_slot(a, p)]];
   const SysConst &sc = sd.sc;
   if (sc.allpairs) return;
   ILane il;

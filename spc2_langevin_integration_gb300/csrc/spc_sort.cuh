@@ -275,4 +275,21 @@ __device__ __forceinline__ void cell_bounds_at(const uint32_t *__restrict__ skey
   for (int c = lo + 1; c <= hi; ++c) cell_start[c] = p;
 }
 
+// The same for sub-cell keys 2c + h (h = 1: the upper half of cell c):
+// cell_start[c] = first sorted position with key >= 2c, cell_mid[c] = first
+// with key >= 2c + 1, for c in [0, ncell] and [0, ncell).  Every entry is
+// written exactly once.
+__device__ __forceinline__ void half_bounds_at(const uint32_t *__restrict__ skeys, int n, int ncell,
+                                               int *__restrict__ cell_start, int *__restrict__ cell_mid,
+                                               int p) {
+  const int lo = (p == 0) ? -1 : (int)skeys[p - 1];
+  const int hi = (p == n) ? 2 * ncell : min((int)skeys[p], 2 * ncell);
+  for (int k = lo + 1; k <= hi; ++k) {
+    if (k & 1)
+      cell_mid[k >> 1] = p;
+    else
+      cell_start[k >> 1] = p;
+  }
+}
+
 }  // namespace spc

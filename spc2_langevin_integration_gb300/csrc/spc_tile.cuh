@@ -39,15 +39,30 @@ struct Stencil {
   int prefix[10];  // offsets of each stencil cell in the staged list
 };
 
-__device__ __forceinline__ void stencil_of(const KArgs &a, const SysDesc &sd, int c, Stencil &s) {
+// half < 0: the 3x3 stencil of cell c.  half 0 / 1 (sub-cells): the stencil
+// of the lower / upper half of cell c.  A particle of the lower half is more
+// than a cell side (>= rho) below the upper half of the row above, so that
+// row's entries keep only their lower half [start, mid); the upper half's
+// stencil keeps the upper half [mid, end) of the row below.  The own cell
+// (entry 4) stays whole, and so does a far cell when both it and cell c hold
+// a particle near the half line (cell_near, kNearHalf).
+__device__ __forceinline__ void stencil_of(const KArgs &a, const SysDesc &sd, int c, Stencil &s,
+                                           int half = -1) {
   const SysConst &sc = sd.sc;
   const int nc = sc.nc, cl = c - sd.c0, cx = cl % nc, cy = cl / nc;
+  const bool near = half >= 0 && a.cell_near[c];
   s.prefix[0] = 0;
 #pragma unroll
   for (int q = 0; q < 9; ++q) {
     const int ox = (q % 3) - 1, oy = (q / 3) - 1;
     const int cj = sd.c0 + adjust_cell(cy + oy, nc) * nc + adjust_cell(cx + ox, nc);
-    const int ja = a.cell_start[cj], jb = a.cell_start[cj + 1];
+    int ja = a.cell_start[cj], jb = a.cell_start[cj + 1];
+    if (half >= 0 && oy == (half == 0 ? 1 : -1) && !(near && a.cell_near[cj])) {
+      if (half == 0)
+        jb = a.cell_mid[cj];
+      else
+        ja = a.cell_mid[cj];
+    }
     s.start[q] = ja;
     s.prefix[q + 1] = s.prefix[q] + (jb - ja);
   }
@@ -370,6 +385,21 @@ __global__ void k_list_units(KArgs a) {
   const int total = st.prefix[9];
   if (!unit_cell(a, n_c, total, CAP)) return;
   a.cell_unit[c] = 1;
+  if (a.cell_mid) {
+    // sub-cells: each half's units over its own stencil, listed as (2c + half, u)
+    const int mid = a.cell_mid[c];
+    for (int h = 0; h < 2; ++h) {
+      const int n_h = h ? c0 + n_c - mid : mid - c0;
+      if (n_h == 0) continue;
+      Stencil sh;
+      stencil_of(a, sd, c, sh, h);
+      const int rounds = (sh.prefix[9] + CAP - 1) / CAP;
+      const int units = (n_h + kWarp - 1) / kWarp * rounds;
+      const int base = atomicAdd(a.unit_count, units);
+      for (int u = 0; u < units; ++u) a.units[base + u] = make_int2(2 * c + h, u);
+    }
+    return;
+  }
   const int rounds = (total + CAP - 1) / CAP;
   const int units = (n_c + kWarp - 1) / kWarp * rounds;
   const int base = atomicAdd(a.unit_count, units);
@@ -605,19 +635,23 @@ __global__ void __launch_bounds__(kTileThreads32, kTileMinBlocks32) k_units_fp32
   const int count = *a.unit_count;
   for (int i = blockIdx.x; i < count; i += gridDim.x) {
     const int2 e = a.units[i];
-    const int c = e.x, c0 = a.cell_start[c], c1 = a.cell_start[c + 1];
+    // the unit's cell and, with sub-cells, its half: particles [g0, g1)
+    const int c = a.cell_mid ? e.x >> 1 : e.x, half = a.cell_mid ? e.x & 1 : -1;
+    const int c0 = a.cell_start[c];
+    const int g0 = half == 1 ? a.cell_mid[c] : c0;
+    const int g1 = half == 0 ? a.cell_mid[c] : a.cell_start[c + 1];
     const SysDesc &sd = a.sys[a.sys_of_c[c]];
     const SysConst &sc = sd.sc;
     const float lo2 = sc.lo2, hi2 = sc.hi2;
     const float band = 0.5f * (hi2 - lo2), nmid = -0.5f * (hi2 + lo2);
     const bool exact_all = sc.exact_all != 0;
     Stencil st;
-    stencil_of(a, sd, c, st);
+    stencil_of(a, sd, c, st, half);
     const int total = st.prefix[9];
     const int rounds = (total + kTileCap - 1) / kTileCap;
     const bool masked = rounds == 1 && a.nbmask != nullptr && !exact_all;
     const int k = e.y / rounds, r = e.y - k * rounds;
-    const int ig = c0 + k * kWarp, gi = min(kWarp, c1 - ig);
+    const int ig = g0 + k * kWarp, gi = min(kWarp, g1 - ig);
     const int rlo = r * kTileCap, rcnt = min(kTileCap, total - rlo);
     const int rpad = (rcnt + kWarp - 1) & ~(kWarp - 1);
     __syncthreads();
@@ -986,7 +1020,11 @@ __global__ void __launch_bounds__(kTileThreads32, kTileMinBlocks32) k_units_fp32
   const int count = *a.unit_count;
   for (int i = blockIdx.x; i < count; i += gridDim.x) {
     const int2 e = a.units[i];
-    const int c = e.x, c0 = a.cell_start[c], c1 = a.cell_start[c + 1];
+    // the unit's cell and, with sub-cells, its half: particles [g0, g1)
+    const int c = a.cell_mid ? e.x >> 1 : e.x, half = a.cell_mid ? e.x & 1 : -1;
+    const int c0 = a.cell_start[c];
+    const int g0 = half == 1 ? a.cell_mid[c] : c0;
+    const int g1 = half == 0 ? a.cell_mid[c] : a.cell_start[c + 1];
     const SysDesc &sd = a.sys[a.sys_of_c[c]];
     const SysConst &sc = sd.sc;
     const float lo2 = sc.lo2, hi2 = sc.hi2;
@@ -994,12 +1032,12 @@ __global__ void __launch_bounds__(kTileThreads32, kTileMinBlocks32) k_units_fp32
     const bool exact_all = sc.exact_all != 0;
     const int qv = KIND == kKindSin ? kXQ : sc.xq2;
     Stencil st;
-    stencil_of(a, sd, c, st);
+    stencil_of(a, sd, c, st, half);
     const int total = st.prefix[9];
     const int rounds = (total + kTileCapX - 1) / kTileCapX;
     const bool masked = rounds == 1 && a.nbmask != nullptr && !exact_all;
     const int k = e.y / rounds, r = e.y - k * rounds;
-    const int ig = c0 + k * kWarp, gi = min(kWarp, c1 - ig);
+    const int ig = g0 + k * kWarp, gi = min(kWarp, g1 - ig);
     const int rlo = r * kTileCapX, rcnt = min(kTileCapX, total - rlo);
     const int rpad = (rcnt + kWarp - 1) & ~(kWarp - 1);
     __syncthreads();

@@ -17,7 +17,7 @@ def test_library_builds_and_loads():
     path = build.build_library()
     assert path.endswith("libspc_gb300.so")
     L = abi.lib()
-    assert L.spc_abi_version() == 3
+    assert L.spc_abi_version() == 4
 
 
 @needs_nvcc

@@ -33,11 +33,11 @@ def test_apply_tuning_sets_every_knob():
             self.set[key] = value
 
     class Abi:
-        TUNE_SPARSE_BELOW, TUNE_TILE_SPLIT, TUNE_CELL_UNITS = 1, 3, 4
+        TUNE_SPARSE_BELOW, TUNE_TILE_SPLIT, TUNE_CELL_UNITS, TUNE_SUBCELLS = 1, 3, 4, 5
 
     h = Handle()
-    bench.apply_tuning(Abi, h, {"sparse_below": 24.0, "tile_split": 2, "cell_units": 1})
-    assert h.set == {1: 24.0, 3: 2, 4: 1}
+    bench.apply_tuning(Abi, h, {"sparse_below": 24.0, "tile_split": 2, "cell_units": 1, "subcells": 1})
+    assert h.set == {1: 24.0, 3: 2, 4: 1, 5: 1}
     h = Handle()
-    bench.apply_tuning(Abi, h, {"sparse_below": 0.0, "tile_split": 1})  # no cell-units key
-    assert h.set == {1: 0.0, 3: 1, 4: 0}
+    bench.apply_tuning(Abi, h, {"sparse_below": 0.0, "tile_split": 1})  # no cell-unit / sub-cell keys
+    assert h.set == {1: 0.0, 3: 1, 4: 0, 5: 0}

@@ -19,7 +19,8 @@ sums, :429-645 for the SRK form):
   1e-12 of the oracle's on the scale rule, for FP64 cell-tile, warp-per-cell
   and Verlet rows and for FP32X; FP32C within its 2e-6 bound; the float
   cell-tile kernels also with cell units (cells run as units of 32
-  particles x one staging round);
+  particles x one staging round) and with sub-cells (units of half cells
+  over the half stencils);
 * 10 SRK steps under the library's Philox noise (the exported normals fed to
   the oracle) within 1e-9 for the same FP64 and FP32X variants.
 """
@@ -39,16 +40,18 @@ pytestmark = pytest.mark.gpu
 FP32C_TOL = 2e-6
 STATES_DIR = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "states")
 VORTEX = dict(v0=0.02, sigma=2.0, rho=0.25, alpha=0.0, D_phi=0.01)
-# variant: (precision, neighbour, SPARSE_BELOW tuning, HEAVY_UNITS tuning)
+# variant: (precision, neighbour, SPARSE_BELOW tuning, cell units: 1, or sub-cells: 2)
 VARIANTS = {
     "fp64_tile": (abi.PRECISION_FP64, abi.NEIGHBOUR_CELL, 0.0, 0),
     "fp64_warp": (abi.PRECISION_FP64, abi.NEIGHBOUR_CELL, 1e9, 0),
     "fp64_verlet": (abi.PRECISION_FP64, abi.NEIGHBOUR_VERLET, None, 0),
     "fp32x_tile": (abi.PRECISION_FP32X, abi.NEIGHBOUR_CELL, 0.0, 0),
     "fp32x_units": (abi.PRECISION_FP32X, abi.NEIGHBOUR_CELL, 0.0, 1),
+    "fp32x_subcells": (abi.PRECISION_FP32X, abi.NEIGHBOUR_CELL, 0.0, 2),
     "fp32x_warp": (abi.PRECISION_FP32X, abi.NEIGHBOUR_CELL, 1e9, 0),
     "fp32c_tile": (abi.PRECISION_FP32C, abi.NEIGHBOUR_CELL, 0.0, 0),
     "fp32c_units": (abi.PRECISION_FP32C, abi.NEIGHBOUR_CELL, 0.0, 1),
+    "fp32c_subcells": (abi.PRECISION_FP32C, abi.NEIGHBOUR_CELL, 0.0, 2),
     "fp32c_warp": (abi.PRECISION_FP32C, abi.NEIGHBOUR_CELL, 1e9, 0),
 }
 STATE_NAMES = ["patch_n4096", "vortex_initial_n65536", "vortex_clustered_n65536"]
@@ -86,8 +89,10 @@ def _system(n, L, prm, variant, st, omega, seed=5):
                                       precision=prec, neighbour=nb, skin=0.05, seed=seed, **prm))
     if sb is not None:
         s.set_tuning(abi.TUNE_SPARSE_BELOW, sb)
-    if units:
+    if units == 1:
         s.set_tuning(abi.TUNE_CELL_UNITS, 1)
+    if units == 2:
+        s.set_tuning(abi.TUNE_SUBCELLS, 1)
     s.upload_state(st)
     s.upload_omega(omega)
     return s
