@@ -325,3 +325,29 @@ def test_cell_units_in_a_batch_with_admissions_equal_alone():
             s.step(0.005, nsteps)
             for key in got:
                 assert np.array_equal(s.download_state(), got[key][k]), (key, k)
+
+
+def test_subcells_with_sparse_systems_in_a_batch_bitwise():
+    """Sub-cells sort every cell of the batch by half, the sparse systems'
+    cells too (their warp-per-cell kernels find their own slot by position
+    in the staged list, not by index order): an FP32X batch of dense
+    (cell-tile) and sparse (warp-per-cell) systems gives the bits of the
+    same batch without sub-cells."""
+    systems = [(6000, 1.5, dict(PRM, rho=0.12)), (400, 1.6, dict(PRM, rho=0.1)),
+               (900, 2.0, dict(PRM, rho=0.2))]
+    ntot = sum(n for n, _, _ in systems)
+    ctot = sum(abi.cells_of(Lb, p["rho"]) for _, Lb, p in systems)
+    out = []
+    for sub in (0, 1):
+        with abi.Batch(abi.STEPPER_EULER, abi.PRECISION_FP32X, 3, ntot, ctot) as b:
+            b.set_tuning(abi.TUNE_SUBCELLS, sub)
+            assert b.get_tuning(abi.TUNE_SPARSE_BELOW) == 24.0
+            slots = [b.admit(n, abi.make_params(L=Lb, stepper=abi.STEPPER_EULER,
+                                                precision=abi.PRECISION_FP32X, seed=8, system_id=k, **p),
+                             init_state(n, Lb, 120 + k))
+                     for k, (n, Lb, p) in enumerate(systems)]
+            b.step(0.01, 10)
+            b.step(0.01, 10, graph=True)
+            out.append([b.download(s) for s in slots])
+    for x, y in zip(*out):
+        assert np.array_equal(x, y)
