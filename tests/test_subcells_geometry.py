@@ -1,4 +1,5 @@
-"""Sub-cells (SPC_TUNE_SUBCELLS), restated on the CPU: the binning of
+"""Sub-cells (SPC_TUNE_SUBCELLS), restated on the CPU: the cell and half
+bounds of the sorted keys (csrc/spc_sort.cuh half_bounds_at), the binning of
 csrc/spc_kernels.cuh (cell_coord, row_offset: the half of each particle, the
 near flag of each cell) and the half stencils of csrc/spc_tile.cuh
 (stencil_of with half 0 / 1), checked against the reference's own cutoff test
@@ -125,3 +126,33 @@ def test_half_stencils_hold_fewer_candidates():
     tests_whole = (cnt.sum(2) * whole).sum()
     tests_half = (cnt[:, :, 0] * lower).sum() + (cnt[:, :, 1] * upper).sum()
     assert 0.80 < tests_half / tests_whole < 0.87  # 7.5 of 9 stencil cells
+
+
+def half_bounds(skeys, ncell):
+    """half_bounds_at (csrc/spc_sort.cuh) for every slot p in [0, n], with a
+    count of the writes to each entry."""
+    n = len(skeys)
+    start = np.full(ncell + 1, -1)
+    mid = np.full(ncell, -1)
+    writes = np.zeros(2 * ncell + 1, dtype=int)
+    for p in range(n + 1):
+        lo = -1 if p == 0 else int(skeys[p - 1])
+        hi = 2 * ncell if p == n else min(int(skeys[p]), 2 * ncell)
+        for k in range(lo + 1, hi + 1):
+            writes[k] += 1
+            if k & 1:
+                mid[k >> 1] = p
+            else:
+                start[k >> 1] = p
+    return start, mid, writes
+
+
+def test_half_bounds_against_searchsorted():
+    rng = np.random.default_rng(3)
+    for ncell, n in ((1, 0), (1, 5), (7, 40), (64, 300), (50, 3)):
+        keys = np.sort(rng.integers(0, 2 * ncell, n)) if n else np.zeros(0, dtype=int)
+        start, mid, writes = half_bounds(keys, ncell)
+        assert np.all(writes == 1)  # every entry exactly once
+        assert np.array_equal(start, np.searchsorted(keys, 2 * np.arange(ncell + 1), "left"))
+        assert np.array_equal(mid, np.searchsorted(keys, 2 * np.arange(ncell) + 1, "left"))
+        assert np.all(start[:-1] <= mid) and np.all(mid <= start[1:])
