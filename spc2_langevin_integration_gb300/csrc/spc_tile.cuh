@@ -361,6 +361,10 @@ __device__ __forceinline__ void finish_fp32c(const KArgs &a, int epi, const SysD
 // particles.  k_list_units lists the units once per evaluation (both passes
 // see the same cells).  Which cells are units, and the order of every sum,
 // depend on the cell alone, so the results do not depend on the CTAs per cell.
+// With sub-cells (SPC_TUNE_SUBCELLS, cell_mid set) each half of a unit cell
+// is cut the same way over its own half stencil (stencil_of with half 0 / 1)
+// and listed as (2c + half, u); the cell stays a unit cell on its whole
+// stencil's round count, which bounds both halves'.
 constexpr int kSplitRounds = 8;
 
 __device__ __forceinline__ bool unit_cell(const KArgs &a, int n_c, int total, int cap) {
